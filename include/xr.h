@@ -1,0 +1,245 @@
+/*
+ * xr.h -- C ABI of the GB300-native ReSTIR GI frame pipeline (libxr.so).
+ *
+ * This is the drop-in boundary for the reference's ReSTIR GI render pass
+ * (0Setsuna0/XVK_Ray).  Every entry point names the reference interface it
+ * replaces.  Plain C types only: pointers, sizes, POD structs.  No exception
+ * crosses the ABI; every call returns an xr_status and the message of the last
+ * failure is available from xr_last_error().
+ *
+ * Threading: one context per host thread.  All work of a context is ordered on
+ * its own CUDA stream; xr_render_frame() is asynchronous, xr_read_output(),
+ * xr_read_buffer() and xr_sync() synchronise.
+ */
+#ifndef XR_H
+#define XR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XR_API_VERSION 1
+
+typedef int32_t xr_status;
+enum {
+    XR_OK = 0,
+    XR_ERR_INVALID_ARGUMENT = 1,
+    XR_ERR_CUDA = 2,
+    XR_ERR_OUT_OF_MEMORY = 3,
+    XR_ERR_STATE = 4,          /* call out of order (e.g. render before the BVH is built) */
+    XR_ERR_OVERFLOW = 5,       /* a device-side bound (traversal stack, queue) was exceeded */
+    XR_ERR_TIMEOUT = 6,        /* a bounded device-side wait gave up */
+    XR_ERR_UNSUPPORTED = 7
+};
+
+typedef struct XrContext XrContext;
+
+/* src/Asset/Vertex.h:11-16 (AVertex, 36 B) == shader/HLSL/ReSTIRGI/Vertex.hlsl:2-8 */
+typedef struct XrVertex {
+    float pos[3];
+    float normal[3];
+    float tex_coord[2];
+    int32_t material_index;
+} XrVertex;
+
+/* src/Asset/Material.h:117-166 (AMaterial, 32 B) == Material.hlsl:7-14.
+   material_model: 0 Lambertian, 1 Metallic (GGX conductor, roughness = fuzziness),
+   4 DiffuseLight (emits base_color * 4, BSDF.hlsl:27-32), 5 Plastic (GGX coat
+   over Lambert, roughness = fuzziness).  Models 1 and 5 are extensions of this
+   library (the reference renders only 0 and 4). */
+typedef struct XrMaterial {
+    float base_color[4];
+    int32_t base_color_texture_index;
+    float fuzziness;
+    float refraction_index;
+    uint32_t material_model;
+} XrMaterial;
+enum { XR_MAT_LAMBERTIAN = 0, XR_MAT_METALLIC = 1, XR_MAT_DIELECTRIC = 2, XR_MAT_ISOTROPIC = 3,
+       XR_MAT_DIFFUSE_LIGHT = 4, XR_MAT_PLASTIC = 5 };
+
+/* src/Asset/Scene.cpp:37 -- per-model uvec2{indexOffset, vertexOffset}; indices
+   of a model are relative to its vertexOffset (Ray.rchit.hlsl:29-40). */
+typedef struct XrMeshRange {
+    uint32_t index_offset;
+    uint32_t vertex_offset;
+} XrMeshRange;
+
+/* src/Asset/UniformBuffer.h:16-32 (UniformBufferObject, 412 B), glm column-major
+   matrices.  number_of_bounces is the path depth; has_sky_box and reuse are
+   0/1; current_frame drives the RNG and the reservoir ping-pong. */
+typedef struct XrUniformBufferObject {
+    float view[16];
+    float view_prev[16];
+    float projection[16];
+    float projection_prev[16];
+    float view_inverse[16];
+    float projection_inverse[16];
+    uint32_t spp;
+    uint32_t total_number_of_samples;
+    uint32_t number_of_bounces;
+    uint32_t random_seed;
+    uint32_t has_sky_box;
+    uint32_t reuse;
+    uint32_t current_frame;
+} XrUniformBufferObject;
+
+/* Render-pass parameters.  In the reference these are shader #defines and UI
+   toggles (ReSTIRGITemporalReuse.rgen.hlsl:3, ReSTIRGISpatialReuse.rgen.hlsl:4-6,
+   src/Editor/UI.cpp:178-204). */
+typedef struct XrParams {
+    uint32_t width, height;
+    uint32_t compat_reference;   /* 1: reproduce the reference bit for bit, quirks included
+                                    (aliased previous G-buffer, no-op visibility, M caps 30/300,
+                                    6 neighbours in 5 px, RNG reuse across passes) */
+    uint32_t temporal_on;        /* merge the previous frame's reservoir */
+    uint32_t spatial_on;         /* run spatial reuse (corrected mode; compat always runs it) */
+    uint32_t m_cap_temporal;     /* corrected mode, <= 255 */
+    uint32_t m_cap_spatial;      /* corrected mode, <= 255 */
+    uint32_t n_neighbours;       /* corrected mode, <= 32 */
+    float radius_px;             /* corrected mode */
+    uint32_t visibility;         /* corrected mode: trace a shadow ray per reused neighbour */
+    uint32_t seed;               /* corrected mode: mixed into every pass's RNG stream */
+    uint32_t write_pt;           /* also write the plain 1-spp path-traced radiance */
+    uint32_t write_hdr;          /* also write the linear radiance before tone mapping */
+} XrParams;
+
+/* Defaults for BASELINE-style corrected rendering: temporal + spatial on, M cap
+   20 / 120, 5 neighbours, 30 px, visibility on, seed 1. */
+void xr_params_default(XrParams* p, uint32_t width, uint32_t height);
+/* The reference's own constants (compat_reference = 1). */
+void xr_params_reference(XrParams* p, uint32_t width, uint32_t height);
+
+typedef struct XrDeviceDesc {
+    int32_t device;              /* CUDA ordinal */
+    uint32_t width, height;      /* swap-chain extent (src/main.cpp:52) */
+} XrDeviceDesc;
+
+typedef struct XrStats {
+    uint32_t frames;
+    uint32_t error_flags;        /* device-side flags seen so far (XR_DEVFLAG_*) */
+    float ms_initial, ms_temporal, ms_spatial, ms_frame;   /* last frame, CUDA events */
+    uint64_t rays_traced;        /* closest-hit rays of the last frame */
+    uint64_t shadow_rays;        /* any-hit rays of the last frame */
+    uint32_t bvh_nodes, bvh_triangles, bvh_depth;
+    float ms_bvh_build;
+} XrStats;
+enum { XR_DEVFLAG_STACK_OVERFLOW = 1u, XR_DEVFLAG_QUEUE_OVERFLOW = 2u, XR_DEVFLAG_BAD_INDEX = 4u };
+
+/* ---- lifetime: replaces Application/ApplicationRT/ApplicationReSTIRGI construction
+        (src/Vulkan/RayTracing/ApplicationReSTIRGI.cpp:25-29) ---- */
+xr_status xr_create(const XrDeviceDesc* desc, XrContext** out);
+void xr_destroy(XrContext* ctx);
+
+/* ---- scene: replaces AScene's concatenation + GPU upload (src/Asset/Scene.cpp:16-87).
+        Host arrays are copied; the caller keeps ownership. ---- */
+xr_status xr_upload_scene(XrContext* ctx,
+                          const XrVertex* vertices, uint32_t vertex_count,
+                          const uint32_t* indices, uint32_t index_count,
+                          const XrMaterial* materials, uint32_t material_count,
+                          const XrMeshRange* ranges, uint32_t range_count);
+
+/* ---- replaces ApplicationRT::CreateAccelerationStructures (ApplicationRT.cpp:55-66):
+        LBVH from 63-bit Morton codes, collapsed to an 8-wide compressed BVH. ---- */
+xr_status xr_build_bvh(XrContext* ctx);
+
+/* ---- replaces InitReSTIRGITracer (ApplicationReSTIRGI.cpp:304-374) + UI toggles ---- */
+xr_status xr_set_params(XrContext* ctx, const XrParams* params);
+xr_status xr_get_params(XrContext* ctx, XrParams* params);
+
+/* ---- replaces ApplicationReSTIRGI::Render (ApplicationReSTIRGI.cpp:150-275):
+        initial sample -> temporal reuse -> spatial reuse + shading, stream ordered.
+        The UBO is the one PathTracer::GetUniformBufferObject builds
+        (src/pathTracer.cpp:169-201). ---- */
+xr_status xr_render_frame(XrContext* ctx, const XrUniformBufferObject* ubo);
+
+/* Output images (the reference's OutputImage, ApplicationReSTIRGI.cpp:248-271). */
+enum {
+    XR_OUT_LDR8 = 0,   /* width*height RGBA8: ACES + gamma 1/2.2 */
+    XR_OUT_HDR = 1,    /* width*height float4: linear radiance before tone mapping */
+    XR_OUT_PT = 2      /* width*height float4: plain 1-spp path-traced radiance (write_pt) */
+};
+xr_status xr_read_output(XrContext* ctx, uint32_t which, void* host, size_t bytes);
+/* Device pointer of an output image (valid until the next xr_set_params/xr_destroy). */
+xr_status xr_output_device_ptr(XrContext* ctx, uint32_t which, void** device_ptr);
+xr_status xr_sync(XrContext* ctx);
+xr_status xr_get_stats(XrContext* ctx, XrStats* stats);
+/* CUDA events on the context stream (slots 0..7) for callers that time work
+   without access to the stream; xr_event_elapsed synchronises on slot b. */
+xr_status xr_event_record(XrContext* ctx, uint32_t slot);
+xr_status xr_event_elapsed(XrContext* ctx, uint32_t slot_a, uint32_t slot_b, float* ms);
+
+/* ---- parity/debug access in the reference's own layouts ---- */
+enum {
+    XR_BUF_SAMPLES = 0,     /* N x ReSTIRGISample (96 B, ReSTIRGICommon.hlsl:6-20) */
+    XR_BUF_TEMPORAL = 1,    /* 2N x ReSTIRGIReservoir (112 B, ReSTIRGICommon.hlsl:22-30) */
+    XR_BUF_SPATIAL = 2      /* 2N (compat) or N (corrected) x ReSTIRGIReservoir */
+};
+/* Reads (or, for fixed-candidate checks, writes) a pipeline buffer converted
+   to/from the reference layout.  Fields the corrected layout does not store read
+   back as 0.  *bytes_out receives the full size when host is NULL. */
+xr_status xr_read_buffer(XrContext* ctx, uint32_t which, void* host, size_t bytes, size_t* bytes_out);
+xr_status xr_write_buffer(XrContext* ctx, uint32_t which, const void* host, size_t bytes);
+/* Runs one pass on the buffers as they are: 1 = temporal, 2 = spatial. */
+xr_status xr_run_pass(XrContext* ctx, const XrUniformBufferObject* ubo, uint32_t pass);
+
+/* ---- closest-hit / any-hit queries on the built BVH (TraceRay semantics of
+        ReSTIRGIInitialSample.rgen.hlsl:90-98 and ReSTIRGISpatialReuse.rgen.hlsl:44-62).
+        rays: n x 8 floats {o.xyz, tmin, d.xyz, tmax} in host memory.  prim = -1 on
+        miss; t and bary (b1, b2) are written on a hit.  Ties: lowest primitive id. */
+xr_status xr_trace_rays(XrContext* ctx, const float* rays, uint32_t n, int32_t any_hit,
+                        int32_t* prim, float* t, float* bary);
+/* Same on device pointers, asynchronous on the context stream. */
+xr_status xr_trace_rays_device(XrContext* ctx, const float* d_rays, uint32_t n, int32_t any_hit,
+                               int32_t* d_prim, float* d_t, float* d_bary);
+
+/* ---- host helpers (no GPU work) ---- */
+/* Camera for one frame: replaces PathTracer::GetUniformBufferObject
+   (src/pathTracer.cpp:169-201) with glm::perspective(fov, aspect, 0.001, 1000),
+   projection[1][1] *= -1, depth zero-to-one.  prev may be NULL (first frame). */
+typedef struct XrCamera {
+    float position[3];
+    float yaw_deg, pitch_deg;    /* view = R(pitch, yaw) * T(-position) (src/Editor/Camera.cpp:21-27) */
+    float fov_deg;
+} XrCamera;
+xr_status xr_camera_ubo(const XrCamera* cam, uint32_t width, uint32_t height,
+                        const XrUniformBufferObject* prev, uint32_t current_frame,
+                        uint32_t number_of_bounces, uint32_t has_sky_box, uint32_t reuse,
+                        XrUniformBufferObject* out);
+
+/* Procedural scenes (deterministic).  Call once with NULL arrays to get the
+   counts, then with arrays of at least those sizes. */
+typedef struct XrSceneData {
+    XrVertex* vertices; uint32_t vertex_count;
+    uint32_t* indices; uint32_t index_count;
+    XrMaterial* materials; uint32_t material_count;
+    XrCamera camera;             /* the scene's default camera */
+} XrSceneData;
+/* Cornell box: 5 walls + 2 rotated boxes (15 / -18 deg) + a 0.5 x 0.5 light of
+   radiance (17, 12, 4); Lambertian (0.73)/(0.65,0.05,0.05)/(0.12,0.45,0.15). */
+xr_status xr_scene_cornell(XrSceneData* out);
+/* Ground plane + n_objects icospheres (subdivision 2) and boxes, scale U[0.2,2],
+   random rotation, GGX roughness U[0.05,1], albedo U[0.1,0.9], metallic
+   Bernoulli(0.3), n_lights emissive quads of radiance U[5,50]. */
+typedef struct XrProceduralDesc {
+    uint32_t seed;
+    uint32_t n_objects;          /* 4096 -> ~1M triangles */
+    uint32_t n_lights;           /* 16 */
+    float extent;                /* objects are placed in [-extent, extent]^2 */
+    uint32_t sphere_subdiv;      /* 2 -> 320 triangles per sphere */
+} XrProceduralDesc;
+xr_status xr_scene_procedural(const XrProceduralDesc* desc, XrSceneData* out);
+
+/* Page-locked host memory for the read-back images (cudaMallocHost). */
+xr_status xr_alloc_host(size_t bytes, void** ptr);
+void xr_free_host(void* ptr);
+
+const char* xr_last_error(const XrContext* ctx);   /* ctx may be NULL: last global error */
+uint32_t xr_api_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XR_H */

@@ -1,0 +1,110 @@
+/*
+ * xr_oracle.h -- C ABI of the CPU oracle for the ReSTIR GI frame pipeline.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The oracle is the checker for the CUDA path: only
+ * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg (and its
+ * reference arm) may load it.  The product library never links or calls it.
+ *
+ * It restates, in plain C++17 with OpenMP over pixels, the reference's HLSL:
+ *   shader/HLSL/random.hlsl:1-20                       (RNG)
+ *   shader/HLSL/ReSTIRGI/Sampling.hlsl:4-56            (ONB, hemisphere, reprojection)
+ *   shader/HLSL/ReSTIRGI/BSDF.hlsl:7-57                (Lambertian / diffuse light)
+ *   shader/HLSL/ReSTIRGI/Ray.rchit.hlsl:26-60          (hit attributes)
+ *   shader/HLSL/ReSTIRGI/Ray.rmiss.hlsl:3-8            (miss)
+ *   shader/HLSL/ReSTIRGI/ReSTIRGICommon.hlsl:6-131     (reservoirs, similarity, ACES)
+ *   shader/HLSL/ReSTIRGI/ReSTIRGIInitialSample.rgen.hlsl:35-214
+ *   shader/HLSL/ReSTIRGI/ReSTIRGITemporalReuse.rgen.hlsl:33-151
+ *   shader/HLSL/ReSTIRGI/ReSTIRGISpatialReuse.rgen.hlsl:35-183
+ * plus the host data flow of src/Vulkan/RayTracing/ApplicationReSTIRGI.cpp:150-275.
+ *
+ * Parity status: the reference has no tests, fixtures or golden vectors and its
+ * Vulkan ray-tracing path cannot run without a graphics stack, so this oracle is
+ * pinned only by known-answer tests derived from the formulas themselves
+ * (tests/golden/) -- "parity unpinned" by reference outputs.
+ *
+ * Arithmetic contract shared with the CUDA path: every float operation is a
+ * single IEEE-754 binary32 operation in the order written (built with
+ * -ffp-contract=off), sqrt and division are correctly rounded, sin/cos come from
+ * sincos_xr (Cody-Waite reduction + Taylor polynomials, oracle.cpp), and
+ * traversal returns the closest hit with ties broken by the lowest primitive id.
+ */
+#ifndef XR_ORACLE_H
+#define XR_ORACLE_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Mirrors XrParams in include/xr.h field for field. */
+typedef struct OrParams {
+    uint32_t width, height;
+    uint32_t compat_reference;   /* 1: reproduce the reference's behaviour bit for bit */
+    uint32_t temporal_on, spatial_on;
+    uint32_t m_cap_temporal, m_cap_spatial;
+    uint32_t n_neighbours;
+    float    radius_px;
+    uint32_t visibility;         /* 1: trace spatial shadow rays (correct mode only) */
+    uint32_t seed;
+    uint32_t write_pt;           /* also produce the plain 1-spp path-traced estimate */
+    uint32_t write_hdr;          /* (the oracle always keeps the linear image) */
+} OrParams;
+
+/* Mirrors the reference UniformBufferObject (src/Asset/UniformBuffer.h:16-32), 412 B. */
+typedef struct OrUBO {
+    float view[16], view_prev[16], projection[16], projection_prev[16];
+    float view_inverse[16], projection_inverse[16];
+    uint32_t spp, total_number_of_samples, number_of_bounces, random_seed;
+    uint32_t has_sky_box, reuse, current_frame;
+} OrUBO;
+
+enum {
+    OR_BUF_SAMPLES = 0,     /* N  x 24 words, ReSTIRGISample layout (ReSTIRGICommon.hlsl:6-20) */
+    OR_BUF_TEMPORAL = 1,    /* 2N x 28 words, ReSTIRGIReservoir layout (ReSTIRGICommon.hlsl:22-30) */
+    OR_BUF_SPATIAL = 2,     /* 2N x 28 words */
+    OR_BUF_HDR = 3,         /* N x 4 float: linear colour before ACES */
+    OR_BUF_LDR = 4,         /* N x 4 u8: ACES + gamma 1/2.2, rounded */
+    OR_BUF_PT = 5,          /* N x 4 float: plain 1-spp path-traced radiance */
+    OR_BUF_GBUF_POS = 6,    /* N x 4 float (x_view, valid) */
+    OR_BUF_MOTION = 7,      /* N x 2 float (after RG16F rounding in compat mode) */
+    OR_BUF_WRITTEN = 8      /* N x u32: 1 where this frame wrote the output image */
+};
+
+/* ---- known-answer helpers (random.hlsl, Sampling.hlsl) ---- */
+uint32_t or_init_random_seed(uint32_t x, uint32_t y, uint32_t width, uint32_t frame);
+void or_random_sequence(uint32_t state, uint32_t n, uint32_t* out_u32, float* out_f);
+void or_sincos(const float* a, uint32_t n, float* s, float* c);
+void or_oct_roundtrip(const float* n3, uint32_t count, uint32_t bits, float* out3, uint32_t* codes);
+
+/* ---- scene + traversal ---- */
+void* or_scene_create(const float* vertices, uint32_t nv, const uint32_t* indices, uint32_t ntri,
+                      const float* materials, uint32_t nm);
+void or_scene_destroy(void* scene);
+/* rays: n x 8 floats (o.xyz, tmin, d.xyz, tmax). any_hit=1 stops at the first hit.
+   prim: -1 on miss.  t, bary (b1, b2) are written on hit. */
+void or_trace(void* scene, const float* rays, uint32_t n, int any_hit,
+              int32_t* prim, float* t, float* bary);
+
+/* ---- the frame pipeline ---- */
+void* or_renderer_create(void* scene, const OrParams* params);
+void or_renderer_destroy(void* r);
+int or_render_frame(void* r, const OrUBO* ubo);
+/* Fixed-candidate checks: load samples (N x 24 words, as read back from the
+   CUDA path), optionally the temporal reservoirs, then run one reuse pass. */
+int or_set_samples(void* r, const float* samples_words, const OrUBO* ubo);
+/* Corrected mode: makes the current G-buffer the previous one (end of a frame). */
+int or_end_frame(void* r);
+int or_run_pass(void* r, const OrUBO* ubo, int pass);   /* 1 = temporal, 2 = spatial */
+size_t or_read(void* r, int which, void* dst, size_t bytes);
+int or_write_temporal(void* r, const float* words, size_t bytes);
+
+/* FP64-accumulated plain path tracer (same path semantics as the initial-sample
+   pass): frames [frame0, frame0+spp) each contribute one sample per pixel. */
+int or_pt_reference(void* scene, const OrParams* params, const OrUBO* ubo,
+                    uint32_t frame0, uint32_t spp, double* out_rgb);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,213 @@
+"""Python view of the C ABI: scenes as numpy arrays, a Renderer per context.
+
+Every call goes through libxr.so; numpy holds host arrays only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data if a is not None and a.size else 0
+
+
+@dataclass
+class Scene:
+    """Flat scene arrays in the reference's upload layout (src/Asset/Scene.cpp:16-49).
+
+    vertices: (nv, 9) float32 -- pos3, normal3, uv2, material index (int32 bits)
+    indices:  (ni,)  uint32, relative to the owning range's vertex offset
+    materials: (nm, 8) float32 -- base colour4, texture index (int32 bits),
+               fuzziness, refraction index, model (uint32 bits)
+    ranges:   (nr, 2) uint32 -- (index offset, vertex offset) per model
+    """
+    vertices: np.ndarray
+    indices: np.ndarray
+    materials: np.ndarray
+    ranges: np.ndarray
+    camera: L.XrCamera
+
+    @property
+    def n_triangles(self) -> int:
+        return int(self.indices.size // 3)
+
+    def global_indices(self) -> np.ndarray:
+        """Absolute vertex index per index slot (each range's vertex offset applied)."""
+        out = self.indices.astype(np.uint32).copy()
+        offs = list(self.ranges[:, 0]) + [self.indices.size]
+        for r in range(self.ranges.shape[0]):
+            out[offs[r]:offs[r + 1]] += self.ranges[r, 1]
+        return out
+
+    @staticmethod
+    def _generate(fn, *args) -> "Scene":
+        lib = L.load()
+        d = L.XrSceneData()
+        L.check(fn(*args, C.byref(d)))
+        v = np.zeros((d.vertex_count, 9), np.float32)
+        i = np.zeros(d.index_count, np.uint32)
+        m = np.zeros((d.material_count, 8), np.float32)
+        d.vertices, d.indices, d.materials = _ptr(v), _ptr(i), _ptr(m)
+        L.check(fn(*args, C.byref(d)))
+        cam = L.XrCamera()
+        C.memmove(C.byref(cam), C.byref(d.camera), C.sizeof(cam))
+        return Scene(v, i, m, np.zeros((1, 2), np.uint32), cam)
+
+    @staticmethod
+    def cornell() -> "Scene":
+        return Scene._generate(L.load().xr_scene_cornell)
+
+    @staticmethod
+    def procedural(seed: int = 1, n_objects: int = 4096, n_lights: int = 16, extent: float = 40.0,
+                   sphere_subdiv: int = 2) -> "Scene":
+        desc = L.XrProceduralDesc(seed, n_objects, n_lights, extent, sphere_subdiv)
+        lib = L.load()
+        return Scene._generate(lib.xr_scene_procedural, C.byref(desc))
+
+
+def params_default(width: int, height: int, **kw) -> L.XrParams:
+    p = L.XrParams()
+    L.load().xr_params_default(C.byref(p), width, height)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def params_reference(width: int, height: int, **kw) -> L.XrParams:
+    p = L.XrParams()
+    L.load().xr_params_reference(C.byref(p), width, height)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def camera_ubo(cam: L.XrCamera, width: int, height: int, prev: L.XrUniformBufferObject | None, frame: int,
+               bounces: int, sky: bool = False, reuse: bool = True) -> L.XrUniformBufferObject:
+    """PathTracer::GetUniformBufferObject (src/pathTracer.cpp:169-201)."""
+    out = L.XrUniformBufferObject()
+    L.check(L.load().xr_camera_ubo(C.byref(cam), width, height, C.byref(prev) if prev is not None else None, frame,
+                                   bounces, 1 if sky else 0, 1 if reuse else 0, C.byref(out)))
+    return out
+
+
+def ubo_bytes(u: L.XrUniformBufferObject) -> bytes:
+    return C.string_at(C.addressof(u), C.sizeof(u))
+
+
+class Renderer:
+    """One libxr context (one GPU, one stream)."""
+
+    def __init__(self, width: int, height: int, device: int = 0):
+        lib = L.load()
+        self._lib = lib
+        h = C.c_void_p()
+        L.check(lib.xr_create(C.byref(L.XrDeviceDesc(device, width, height)), C.byref(h)))
+        self.ctx = h
+        self.width, self.height = width, height
+
+    def _c(self, status: int) -> None:
+        L.check(status, self.ctx)
+
+    def close(self) -> None:
+        if self.ctx:
+            self._lib.xr_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- scene / BVH --
+    def upload_scene(self, scene: Scene) -> None:
+        v = np.ascontiguousarray(scene.vertices, np.float32)
+        i = np.ascontiguousarray(scene.indices, np.uint32)
+        m = np.ascontiguousarray(scene.materials, np.float32)
+        r = np.ascontiguousarray(scene.ranges, np.uint32)
+        self._c(self._lib.xr_upload_scene(self.ctx, _ptr(v), v.shape[0], _ptr(i), i.size, _ptr(m), m.shape[0],
+                                          _ptr(r), r.shape[0]))
+
+    def build_bvh(self) -> None:
+        self._c(self._lib.xr_build_bvh(self.ctx))
+
+    def set_params(self, p: L.XrParams) -> None:
+        self._c(self._lib.xr_set_params(self.ctx, C.byref(p)))
+        self.width, self.height = p.width, p.height
+
+    # -- frames --
+    def render(self, ubo: L.XrUniformBufferObject) -> None:
+        self._c(self._lib.xr_render_frame(self.ctx, C.byref(ubo)))
+
+    def sync(self) -> None:
+        self._c(self._lib.xr_sync(self.ctx))
+
+    def read_output(self, which: int = L.XR_OUT_LDR8, out: np.ndarray | None = None) -> np.ndarray:
+        n = self.width * self.height
+        if out is None:
+            out = np.empty((n, 4), np.uint8 if which == L.XR_OUT_LDR8 else np.float32)
+        self._c(self._lib.xr_read_output(self.ctx, which, _ptr(out), out.nbytes))
+        return out
+
+    def output_device_ptr(self, which: int = L.XR_OUT_LDR8) -> int:
+        p = C.c_void_p()
+        self._c(self._lib.xr_output_device_ptr(self.ctx, which, C.byref(p)))
+        return p.value
+
+    def stats(self) -> L.XrStats:
+        s = L.XrStats()
+        self._c(self._lib.xr_get_stats(self.ctx, C.byref(s)))
+        return s
+
+    # -- parity access in the reference layouts --
+    def read_buffer(self, which: int) -> np.ndarray:
+        n = C.c_size_t()
+        self._c(self._lib.xr_read_buffer(self.ctx, which, None, 0, C.byref(n)))
+        words = 24 if which == L.XR_BUF_SAMPLES else 28
+        out = np.empty(n.value // 4, np.uint32)
+        self._c(self._lib.xr_read_buffer(self.ctx, which, _ptr(out), out.nbytes, None))
+        return out.reshape(-1, words)
+
+    def write_buffer(self, which: int, words: np.ndarray) -> None:
+        w = np.ascontiguousarray(words, np.uint32)
+        self._c(self._lib.xr_write_buffer(self.ctx, which, _ptr(w), w.nbytes))
+
+    def run_pass(self, ubo: L.XrUniformBufferObject, pass_id: int) -> None:
+        self._c(self._lib.xr_run_pass(self.ctx, C.byref(ubo), pass_id))
+
+    def trace(self, rays: np.ndarray, any_hit: bool = False):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        bary = np.empty((n, 2), np.float32)
+        self._c(self._lib.xr_trace_rays(self.ctx, _ptr(rays), n, 1 if any_hit else 0, _ptr(prim), _ptr(t),
+                                        _ptr(bary)))
+        return prim, t, bary
+
+
+class PinnedBuffer:
+    """Page-locked host memory (cudaMallocHost) viewed as a numpy array."""
+
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        L.check(L.load().xr_alloc_host(nbytes, C.byref(p)))
+        self.ptr = p.value
+        self.nbytes = nbytes
+        self.array = np.ctypeslib.as_array((C.c_uint8 * nbytes).from_address(self.ptr))
+
+    def free(self) -> None:
+        if self.ptr:
+            L.load().xr_free_host(self.ptr)
+            self.ptr = None

@@ -1,0 +1,524 @@
+// bvh_build.cu -- GPU LBVH build collapsed to the 8-wide compressed BVH.
+//
+// Replaces the driver-built bottom/top-level acceleration structures of the
+// reference (ApplicationRT.cpp:186-258, XVKBLGeometry.cpp:8-38,
+// XVKAccelerationStructure.cpp:15-96: one opaque BLAS per model, identity
+// instances).  Steps, all on the context stream:
+//   1. per-triangle bounds, scene centroid bounds (warp reductions + atomics)
+//   2. 63-bit Morton codes of the box centres (21 bits per axis)
+//   3. stable LSD radix sort of (code, primitive) pairs, 8 passes of 8 bits
+//   4. Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees and
+//      k-d Trees" (HPG 2012) binary radix tree; equal codes split by index
+//   5. bottom-up bounds, second arrival at a node computes its box
+//   6. top-down collapse, one level per launch: each wide node takes up to 8
+//      children by repeatedly opening the child of largest surface area
+//      (subtrees of more than 3 triangles first), children of <= 3 triangles
+//      become leaves, slots are assigned by octant of the child centre so that a
+//      ray visits near children first, boxes are quantised to 8 bits.
+#include <algorithm>
+#include <vector>
+
+#include "device_math.cuh"
+#include "xr_internal.h"
+
+namespace xr {
+namespace {
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+
+__device__ __forceinline__ uint32_t f2o(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float o2f(uint32_t u) {
+    uint32_t v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(v);
+#else
+    float f;
+    memcpy(&f, &v, 4);
+    return f;
+#endif
+}
+
+// bounds[0..2] centroid min, [3..5] centroid max, [6] largest |coordinate|
+__global__ void k_tri_prep(const uint4* __restrict__ tri_idx, const float4* __restrict__ vpos, uint32_t ntri,
+                           float4* __restrict__ tri_lo, float4* __restrict__ tri_hi, uint32_t* __restrict__ bounds) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY}, amax = 0.0f;
+    if (t < ntri) {
+        uint4 id = tri_idx[t];
+        float4 a = vpos[id.x], b = vpos[id.y], c = vpos[id.z];
+        float3 lo = f3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+        float3 hi = f3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+        tri_lo[t] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+        tri_hi[t] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+        float cx = (lo.x + hi.x) * 0.5f, cy = (lo.y + hi.y) * 0.5f, cz = (lo.z + hi.z) * 0.5f;
+        cmin[0] = cmax[0] = cx; cmin[1] = cmax[1] = cy; cmin[2] = cmax[2] = cz;
+        amax = fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(lo.y)), fmaxf(fabsf(lo.z), fabsf(hi.x))),
+                     fmaxf(fabsf(hi.y), fabsf(hi.z)));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int k = 0; k < 3; k++) {
+            cmin[k] = fminf(cmin[k], __shfl_xor_sync(0xFFFFFFFFu, cmin[k], off));
+            cmax[k] = fmaxf(cmax[k], __shfl_xor_sync(0xFFFFFFFFu, cmax[k], off));
+        }
+        amax = fmaxf(amax, __shfl_xor_sync(0xFFFFFFFFu, amax, off));
+    }
+    if ((threadIdx.x & 31) == 0 && cmin[0] <= cmax[0]) {
+        for (int k = 0; k < 3; k++) {
+            atomicMin(&bounds[k], f2o(cmin[k]));
+            atomicMax(&bounds[3 + k], f2o(cmax[k]));
+        }
+        atomicMax(&bounds[6], __float_as_uint(amax));
+    }
+}
+
+__device__ __forceinline__ uint64_t spread21(uint32_t v) {
+    uint64_t x = v & 0x1FFFFFu;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float4* __restrict__ tri_lo, const float4* __restrict__ tri_hi, uint32_t ntri,
+                         const uint32_t* __restrict__ bounds, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    float4 lo = tri_lo[t], hi = tri_hi[t];
+    float c[3] = {(lo.x + hi.x) * 0.5f, (lo.y + hi.y) * 0.5f, (lo.z + hi.z) * 0.5f};
+    uint32_t q[3];
+    for (int k = 0; k < 3; k++) {
+        float mn = o2f(bounds[k]), mx = o2f(bounds[3 + k]);
+        float ext = mx - mn;
+        float u = ext > 0.0f ? (c[k] - mn) / ext : 0.5f;
+        u = fminf(fmaxf(u, 0.0f), 1.0f);
+        q[k] = min((uint32_t)(u * 2097152.0f), 2097151u);
+    }
+    keys[t] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
+    vals[t] = t;
+}
+
+// ---- stable LSD radix sort, 8 bits per pass ----
+constexpr int kSortThreads = 256;
+
+__global__ void k_sort_hist(const uint64_t* __restrict__ keys, uint32_t n, uint32_t chunk, int shift,
+                            uint32_t* __restrict__ hist, uint32_t nblocks) {
+    __shared__ uint32_t h[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    uint32_t b = blockIdx.x, beg = b * chunk, end = min(n, beg + chunk);
+    for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x)
+        atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 0xFFu], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i * nblocks + b] = h[i];
+}
+
+// exclusive scan of hist[256 * nblocks] in one block
+__global__ void k_sort_scan(uint32_t* __restrict__ hist, uint32_t total) {
+    __shared__ uint32_t part[1024];
+    uint32_t per = (total + blockDim.x - 1) / blockDim.x;
+    uint32_t beg = threadIdx.x * per, end = min(total, beg + per);
+    uint32_t s = 0;
+    for (uint32_t i = beg; i < end; i++) s += hist[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (uint32_t i = 0; i < blockDim.x; i++) { uint32_t v = part[i]; part[i] = acc; acc += v; }
+    }
+    __syncthreads();
+    uint32_t acc = part[threadIdx.x];
+    for (uint32_t i = beg; i < end; i++) { uint32_t v = hist[i]; hist[i] = acc; acc += v; }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint64_t* __restrict__ kin,
+                                                               const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+                                                               uint32_t* __restrict__ vout, uint32_t n, uint32_t chunk, int shift,
+                                                               const uint32_t* __restrict__ hist, uint32_t nblocks) {
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wcnt[kSortThreads / 32][256];
+    const uint32_t b = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) base[i] = hist[i * nblocks + b];
+    const uint32_t beg = b * chunk, end = min(n, beg + chunk);
+    for (uint32_t tile = beg; tile < end; tile += kSortThreads) {
+        for (int i = threadIdx.x; i < (kSortThreads / 32) * 256; i += blockDim.x) (&wcnt[0][0])[i] = 0;
+        __syncthreads();
+        uint32_t i = tile + threadIdx.x;
+        bool valid = i < end;
+        uint64_t key = valid ? kin[i] : 0ull;
+        uint32_t val = valid ? vin[i] : 0u;
+        uint32_t digit = valid ? ((uint32_t)(key >> shift) & 0xFFu) : 256u + lane;   // invalid lanes never match
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0) wcnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t before = 0;
+            for (uint32_t w = 0; w < warp; w++) before += wcnt[w][digit];
+            uint32_t pos = base[digit] + before + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+            uint32_t tot = 0;
+            for (int w = 0; w < kSortThreads / 32; w++) tot += wcnt[w][d];
+            base[d] += tot;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- Karras radix tree ----
+__device__ __forceinline__ int delta(const uint64_t* keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = keys[i], b = keys[j];
+    if (a == b) return 64 + __clz((uint32_t)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+__global__ void k_karras(const uint64_t* __restrict__ keys, int n, uint32_t* __restrict__ left, uint32_t* __restrict__ right,
+                         uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf, uint2* __restrict__ range) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    uint32_t lc = (lo == gamma) ? ((uint32_t)gamma | kLeafBit) : (uint32_t)gamma;
+    uint32_t rc = (hi == gamma + 1) ? ((uint32_t)(gamma + 1) | kLeafBit) : (uint32_t)(gamma + 1);
+    left[i] = lc;
+    right[i] = rc;
+    range[i] = make_uint2((uint32_t)lo, (uint32_t)hi);
+    if (lc & kLeafBit) parent_leaf[lc & ~kLeafBit] = (uint32_t)i; else parent_int[lc] = (uint32_t)i;
+    if (rc & kLeafBit) parent_leaf[rc & ~kLeafBit] = (uint32_t)i; else parent_int[rc] = (uint32_t)i;
+}
+
+__device__ __forceinline__ void ref_box(uint32_t ref, const float4* nlo, const float4* nhi, const float4* tlo,
+                                        const float4* thi, const uint32_t* sorted, float4* lo, float4* hi) {
+    if (ref & kLeafBit) {
+        uint32_t p = sorted[ref & ~kLeafBit];
+        *lo = tlo[p]; *hi = thi[p];
+    } else {
+        *lo = __ldcg(nlo + ref); *hi = __ldcg(nhi + ref);
+    }
+}
+
+__global__ void k_bounds(int n, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                         const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ parent_leaf,
+                         const uint32_t* __restrict__ sorted, const float4* __restrict__ tlo, const float4* __restrict__ thi,
+                         float4* nlo, float4* nhi, uint32_t* flags) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t node = parent_leaf[j];
+    while (node != kInvalid) {
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0u) return;
+        __threadfence();
+        float4 al, ah, bl, bh;
+        ref_box(left[node], nlo, nhi, tlo, thi, sorted, &al, &ah);
+        ref_box(right[node], nlo, nhi, tlo, thi, sorted, &bl, &bh);
+        __stcg(nlo + node, make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.0f));
+        __stcg(nhi + node, make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f));
+        node = parent_int[node];
+    }
+}
+
+struct CollapseArgs {
+    const uint32_t* left; const uint32_t* right; const uint2* range;
+    const float4* nlo; const float4* nhi; const float4* tlo; const float4* thi;
+    const uint32_t* sorted;           // sorted primitive ids
+    const uint4* tri_idx; const float4* vpos;
+    const uint32_t* task_in; const uint32_t* task_wide_in; uint32_t n_tasks;
+    uint32_t* task_out; uint32_t* task_wide_out;
+    uint32_t* counters;               // [0] wide nodes, [1] tri slots, [2] next task count
+    WideNode* nodes; float4* tris;
+    int emin;                         // smallest exponent of the quantisation grid
+};
+
+__device__ __forceinline__ uint32_t ref_count(uint32_t ref, const uint2* range) {
+    if (ref & kLeafBit) return 1u;
+    uint2 r = range[ref];
+    return r.y - r.x + 1u;
+}
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+__device__ __forceinline__ int ceil_log2f(float v) {   // smallest e with 2^e >= v (v > 0)
+    int e;
+    float m = frexpf(v, &e);                           // v = m 2^e, m in [0.5, 1)
+    return (m == 0.5f) ? e - 1 : e;
+}
+
+__global__ void k_collapse(CollapseArgs a) {
+    uint32_t task = blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= a.n_tasks) return;
+    const uint32_t bref = a.task_in[task];
+    const uint32_t widx = a.task_wide_in[task];
+    uint32_t refs[8];
+    int nc = 0;
+    if (bref & kLeafBit) {
+        refs[nc++] = bref;
+    } else {
+        refs[nc++] = a.left[bref];
+        refs[nc++] = a.right[bref];
+        while (nc < 8) {
+            int best = -1;
+            float best_area = -1.0f;
+            for (int phase = 0; phase < 2 && best < 0; phase++) {
+                for (int c = 0; c < nc; c++) {
+                    uint32_t r = refs[c];
+                    if (r & kLeafBit) continue;
+                    uint32_t cnt = ref_count(r, a.range);
+                    if (phase == 0 ? cnt <= 3u : cnt > 3u) continue;
+                    float ar = half_area(a.nlo[r], a.nhi[r]);
+                    if (ar > best_area) { best_area = ar; best = c; }
+                }
+            }
+            if (best < 0) break;
+            uint32_t r = refs[best];
+            refs[best] = a.left[r];
+            refs[nc++] = a.right[r];
+        }
+    }
+    // boxes, parent box
+    float4 clo[8], chi[8];
+    float4 plo = make_float4(INFINITY, INFINITY, INFINITY, 0), phi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
+    for (int c = 0; c < nc; c++) {
+        ref_box(refs[c], a.nlo, a.nhi, a.tlo, a.thi, a.sorted, &clo[c], &chi[c]);
+        plo = make_float4(fminf(plo.x, clo[c].x), fminf(plo.y, clo[c].y), fminf(plo.z, clo[c].z), 0);
+        phi = make_float4(fmaxf(phi.x, chi[c].x), fmaxf(phi.y, chi[c].y), fmaxf(phi.z, chi[c].z), 0);
+    }
+    // slot assignment by octant of the child centre relative to the parent centre
+    int slot_of[8];
+    uint32_t used = 0;
+    float pcx = (plo.x + phi.x) * 0.5f, pcy = (plo.y + phi.y) * 0.5f, pcz = (plo.z + phi.z) * 0.5f;
+    uint32_t oct[8];
+    for (int c = 0; c < nc; c++) {
+        float cx = (clo[c].x + chi[c].x) * 0.5f, cy = (clo[c].y + chi[c].y) * 0.5f, cz = (clo[c].z + chi[c].z) * 0.5f;
+        oct[c] = (cx >= pcx ? 1u : 0u) | (cy >= pcy ? 2u : 0u) | (cz >= pcz ? 4u : 0u);
+        slot_of[c] = -1;
+        if (!(used & (1u << oct[c]))) { slot_of[c] = (int)oct[c]; used |= 1u << oct[c]; }
+    }
+    for (int c = 0; c < nc; c++) {
+        if (slot_of[c] >= 0) continue;
+        int best = -1, bd = 99;
+        for (int s = 0; s < 8; s++) {
+            if (used & (1u << s)) continue;
+            int dd = __popc((uint32_t)s ^ oct[c]);
+            if (dd < bd) { bd = dd; best = s; }
+        }
+        slot_of[c] = best;
+        used |= 1u << best;
+    }
+    // internal children and leaf triangle counts
+    uint32_t imask = 0, n_int = 0, n_tris = 0;
+    uint32_t cnt_of[8];
+    for (int c = 0; c < nc; c++) {
+        uint32_t cnt = ref_count(refs[c], a.range);
+        cnt_of[c] = cnt;
+        if (!(refs[c] & kLeafBit) && cnt > 3u) { imask |= 1u << slot_of[c]; n_int++; }
+        else n_tris += cnt;
+    }
+    uint32_t child_base = n_int ? atomicAdd(&a.counters[0], n_int) : 0u;
+    uint32_t tri_base = n_tris ? atomicAdd(&a.counters[1], n_tris) : 0u;
+    // quantisation grid: p = lo - one cell, cells of 2^e with extent / 2^e <= 250
+    WideNode nd;
+    int e[3];
+    float lo3[3] = {plo.x, plo.y, plo.z}, hi3[3] = {phi.x, phi.y, phi.z}, p3[3];
+    for (int k = 0; k < 3; k++) {
+        float ext = hi3[k] - lo3[k];
+        int ek = ext > 0.0f ? ceil_log2f(ext / 250.0f) : a.emin;
+        ek = max(ek, a.emin);
+        e[k] = ek;
+        p3[k] = lo3[k] - ldexpf(1.0f, ek);
+    }
+    nd.px = p3[0]; nd.py = p3[1]; nd.pz = p3[2];
+    nd.exyz_imask = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
+    nd.child_base = child_base;
+    nd.tri_base = tri_base;
+    uint8_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint8_t ql[3][8], qh[3][8];
+    for (int s = 0; s < 8; s++) for (int k = 0; k < 3; k++) { ql[k][s] = 0; qh[k][s] = 0; }
+    // leaf triangle offsets in slot order
+    uint32_t off = 0;
+    for (int s = 0; s < 8; s++) {
+        int c = -1;
+        for (int cc = 0; cc < nc; cc++) if (slot_of[cc] == s) c = cc;
+        if (c < 0) continue;
+        float cl[3] = {clo[c].x, clo[c].y, clo[c].z}, ch[3] = {chi[c].x, chi[c].y, chi[c].z};
+        for (int k = 0; k < 3; k++) {
+            float inv = ldexpf(1.0f, -e[k]);
+            float l = floorf((cl[k] - p3[k]) * inv) - 1.0f;
+            float h = ceilf((ch[k] - p3[k]) * inv) + 1.0f;
+            ql[k][s] = (uint8_t)fminf(fmaxf(l, 0.0f), 255.0f);
+            qh[k][s] = (uint8_t)fminf(fmaxf(h, 0.0f), 255.0f);
+        }
+        uint32_t r = refs[c];
+        if (imask & (1u << s)) {
+            meta[s] = 0x80;
+            uint32_t rank = __popc(imask & ((1u << s) - 1u));
+            uint32_t slot = atomicAdd(&a.counters[2], 1u);
+            a.task_out[slot] = r;
+            a.task_wide_out[slot] = child_base + rank;
+        } else {
+            uint32_t first = (r & kLeafBit) ? (r & ~kLeafBit) : a.range[r].x;
+            uint32_t cnt = cnt_of[c];
+            meta[s] = (uint8_t)((cnt << 5) | off);
+            for (uint32_t j = 0; j < cnt; j++) {
+                uint32_t prim = a.sorted[first + j];
+                uint4 id = a.tri_idx[prim];
+                float4 v0 = a.vpos[id.x], v1 = a.vpos[id.y], v2 = a.vpos[id.z];
+                float4* dst = a.tris + 3u * (tri_base + off + j);
+                dst[0] = make_float4(v0.x, v0.y, v0.z, __uint_as_float(prim));
+                dst[1] = make_float4(v1.x, v1.y, v1.z, 0.0f);
+                dst[2] = make_float4(v2.x, v2.y, v2.z, 0.0f);
+            }
+            off += cnt;
+        }
+    }
+    nd.meta[0] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | ((uint32_t)meta[3] << 24);
+    nd.meta[1] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | ((uint32_t)meta[7] << 24);
+    auto pack = [&](const uint8_t* q8, uint32_t* w) {
+        w[0] = q8[0] | (q8[1] << 8) | (q8[2] << 16) | ((uint32_t)q8[3] << 24);
+        w[1] = q8[4] | (q8[5] << 8) | (q8[6] << 16) | ((uint32_t)q8[7] << 24);
+    };
+    pack(ql[0], &nd.q[0]); pack(ql[1], &nd.q[2]); pack(ql[2], &nd.q[4]);
+    pack(qh[0], &nd.q[6]); pack(qh[1], &nd.q[8]); pack(qh[2], &nd.q[10]);
+    a.nodes[widx] = nd;
+}
+
+template <typename T>
+xr_status dalloc(Context* ctx, T** p, size_t count) {
+    return cuda_check(ctx, cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)), "cudaMalloc (bvh)");
+}
+
+}  // namespace
+
+xr_status build_bvh(Context* ctx) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t n = ctx->ntri;
+    if (ctx->d_nodes) { cudaFree(ctx->d_nodes); ctx->d_nodes = nullptr; }
+    if (ctx->d_tris) { cudaFree(ctx->d_tris); ctx->d_tris = nullptr; }
+    ctx->n_nodes = 0; ctx->n_tri_slots = 0; ctx->bvh_depth = 0;
+    if (n == 0) { ctx->bvh_ready = true; return XR_OK; }
+
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+
+    float4 *tlo = nullptr, *thi = nullptr, *nlo = nullptr, *nhi = nullptr;
+    uint64_t *k0 = nullptr, *k1 = nullptr;
+    uint32_t *v0 = nullptr, *v1 = nullptr, *bounds = nullptr, *hist = nullptr;
+    uint32_t *left = nullptr, *right = nullptr, *pint = nullptr, *pleaf = nullptr, *flags = nullptr;
+    uint2* range = nullptr;
+    uint32_t *ta = nullptr, *tb = nullptr, *wa = nullptr, *wb = nullptr, *counters = nullptr;
+    WideNode* nodes_tmp = nullptr;
+    xr_status s = XR_OK;
+    const uint32_t nint = n > 1 ? n - 1 : 1;
+    const uint32_t chunk = 4096;
+    const uint32_t nblk = (n + chunk - 1) / chunk;
+    if ((s = dalloc(ctx, &tlo, n)) || (s = dalloc(ctx, &thi, n)) || (s = dalloc(ctx, &k0, n)) ||
+        (s = dalloc(ctx, &k1, n)) || (s = dalloc(ctx, &v0, n)) || (s = dalloc(ctx, &v1, n)) ||
+        (s = dalloc(ctx, &bounds, 8)) || (s = dalloc(ctx, &hist, 256 * nblk)) || (s = dalloc(ctx, &left, nint)) ||
+        (s = dalloc(ctx, &right, nint)) || (s = dalloc(ctx, &pint, nint)) || (s = dalloc(ctx, &pleaf, n)) ||
+        (s = dalloc(ctx, &flags, nint)) || (s = dalloc(ctx, &range, nint)) || (s = dalloc(ctx, &nlo, nint)) ||
+        (s = dalloc(ctx, &nhi, nint)) || (s = dalloc(ctx, &ta, n)) || (s = dalloc(ctx, &tb, n)) ||
+        (s = dalloc(ctx, &wa, n)) || (s = dalloc(ctx, &wb, n)) || (s = dalloc(ctx, &counters, 4)) ||
+        (s = dalloc(ctx, &nodes_tmp, nint)) || (s = dalloc(ctx, &ctx->d_tris, 3 * (size_t)n)))
+        goto done;
+    {
+        uint32_t binit[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
+        cudaMemcpyAsync(bounds, binit, sizeof(binit), cudaMemcpyHostToDevice, st);
+        uint32_t blocks = (n + 255) / 256;
+        k_tri_prep<<<blocks, 256, 0, st>>>(ctx->d_tri_idx, ctx->d_vpos, n, tlo, thi, bounds);
+        k_morton<<<blocks, 256, 0, st>>>(tlo, thi, n, bounds, k0, v0);
+        for (int pass = 0; pass < 8; pass++) {
+            int shift = pass * 8;
+            k_sort_hist<<<nblk, 256, 0, st>>>(k0, n, chunk, shift, hist, nblk);
+            k_sort_scan<<<1, 1024, 0, st>>>(hist, 256 * nblk);
+            k_sort_scatter<<<nblk, kSortThreads, 0, st>>>(k0, v0, k1, v1, n, chunk, shift, hist, nblk);
+            std::swap(k0, k1);
+            std::swap(v0, v1);
+        }
+        uint32_t bh[8];
+        cudaMemcpyAsync(bh, bounds, sizeof(bh), cudaMemcpyDeviceToHost, st);
+        if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: sort"))) goto done;
+        float amax;
+        memcpy(&amax, &bh[6], 4);
+        int emin;
+        frexpf(fmaxf(amax, 1e-20f), &emin);
+        emin -= 17;   // cells of at least 2^-17 of the largest coordinate
+        cudaMemsetAsync(pint, 0xFF, nint * 4, st);
+        cudaMemsetAsync(pleaf, 0xFF, (size_t)n * 4, st);
+        cudaMemsetAsync(flags, 0, nint * 4, st);
+        uint32_t root_ref = 0u;
+        if (n > 1) {
+            k_karras<<<(n - 1 + 255) / 256, 256, 0, st>>>(k0, (int)n, left, right, pint, pleaf, range);
+            k_bounds<<<(n + 255) / 256, 256, 0, st>>>((int)n, left, right, pint, pleaf, v0, tlo, thi, nlo, nhi, flags);
+        } else {
+            root_ref = 0u | kLeafBit;
+        }
+        uint32_t cinit[4] = {1u, 0u, 0u, 0u};
+        cudaMemcpyAsync(counters, cinit, sizeof(cinit), cudaMemcpyHostToDevice, st);
+        uint32_t zero = 0u;
+        cudaMemcpyAsync(ta, &root_ref, 4, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(wa, &zero, 4, cudaMemcpyHostToDevice, st);
+        uint32_t ntask = 1, depth = 0;
+        while (ntask > 0) {
+            CollapseArgs ca;
+            ca.left = left; ca.right = right; ca.range = range; ca.nlo = nlo; ca.nhi = nhi; ca.tlo = tlo; ca.thi = thi;
+            ca.sorted = v0; ca.tri_idx = ctx->d_tri_idx; ca.vpos = ctx->d_vpos;
+            ca.task_in = ta; ca.task_wide_in = wa; ca.n_tasks = ntask; ca.task_out = tb; ca.task_wide_out = wb;
+            ca.counters = counters; ca.nodes = nodes_tmp; ca.tris = ctx->d_tris; ca.emin = emin;
+            cudaMemsetAsync(counters + 2, 0, 4, st);
+            k_collapse<<<(ntask + 127) / 128, 128, 0, st>>>(ca);
+            cudaMemcpyAsync(&ntask, counters + 2, 4, cudaMemcpyDeviceToHost, st);
+            if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: collapse"))) goto done;
+            std::swap(ta, tb);
+            std::swap(wa, wb);
+            depth++;
+            if (depth > 200) { s = fail(ctx, XR_ERR_OVERFLOW, "bvh: collapse did not terminate"); goto done; }
+        }
+        uint32_t ch[4];
+        cudaMemcpy(ch, counters, sizeof(ch), cudaMemcpyDeviceToHost);
+        if (ch[1] != n) { s = fail(ctx, XR_ERR_STATE, "bvh: triangle slots do not match the primitive count"); goto done; }
+        if ((s = dalloc(ctx, &ctx->d_nodes, ch[0]))) goto done;
+        cudaMemcpyAsync(ctx->d_nodes, nodes_tmp, (size_t)ch[0] * sizeof(WideNode), cudaMemcpyDeviceToDevice, st);
+        cudaEventRecord(e1, st);
+        if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: finish"))) goto done;
+        ctx->n_nodes = ch[0];
+        ctx->n_tri_slots = ch[1];
+        ctx->bvh_depth = depth;
+        cudaEventElapsedTime(&ctx->ms_bvh, e0, e1);
+        ctx->bvh_ready = true;
+    }
+done:
+    cudaFree(tlo); cudaFree(thi); cudaFree(k0); cudaFree(k1); cudaFree(v0); cudaFree(v1); cudaFree(bounds);
+    cudaFree(hist); cudaFree(left); cudaFree(right); cudaFree(pint); cudaFree(pleaf); cudaFree(flags);
+    cudaFree(range); cudaFree(nlo); cudaFree(nhi); cudaFree(ta); cudaFree(tb); cudaFree(wa); cudaFree(wb);
+    cudaFree(counters); cudaFree(nodes_tmp);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    if (s != XR_OK && ctx->d_tris) { cudaFree(ctx->d_tris); ctx->d_tris = nullptr; }
+    return s;
+}
+
+}  // namespace xr

@@ -1,0 +1,813 @@
+// restir.cu -- the ReSTIR GI frame: initial sample (wavefront), temporal reuse,
+// spatial reuse with fused shading.
+//
+//   initial sample  ReSTIRGIInitialSample.rgen.hlsl:35-214
+//   temporal reuse  ReSTIRGITemporalReuse.rgen.hlsl:33-151
+//   spatial reuse   ReSTIRGISpatialReuse.rgen.hlsl:35-183
+//   reservoirs      ReSTIRGICommon.hlsl:43-121
+//
+// The reference runs one ray-generation thread per pixel that loops over the
+// bounces.  Here each bounce is one launch over a compacted queue of live
+// paths: the first launch generates camera rays per 16x8 pixel tile, every
+// launch traces, shades and samples the next direction, and survivors are
+// appended to the next queue with one atomic per warp (ballot + popc).  Later
+// bounces run on a persistent grid that reads the queue length from device
+// memory, so the whole frame is launched without a host round trip.
+//
+// Per-pixel data is written in the layouts documented in xr_internal.h.
+#include <utility>
+
+#include "bsdf.cuh"
+#include "traverse.cuh"
+
+namespace xr {
+namespace {
+
+constexpr int kBlock = 128;
+
+struct HitPayload {
+    float3 pos, normal, geo;
+    int32_t mat;
+    float t;
+};
+
+// Ray.rchit.hlsl:26-60 with identity instance transforms; miss = material -1
+// (Ray.rmiss.hlsl:3-8).
+__device__ __forceinline__ HitPayload closest_hit(const DeviceScene& sc, const HitRec& h) {
+    HitPayload pl;
+    uint4 id = __ldg(sc.tri_idx + h.prim);
+    float bx = 1.0f - h.b1 - h.b2, by = h.b1, bz = h.b2;
+    float3 n0 = xyz(__ldg(sc.vnrm + id.x)), n1 = xyz(__ldg(sc.vnrm + id.y)), n2 = xyz(__ldg(sc.vnrm + id.z));
+    float3 nm = n0 * bx + n1 * by + n2 * bz;
+    float3 normal = normalize(nm);
+    float3 v0 = xyz(__ldg(sc.vpos + id.x)), v1 = xyz(__ldg(sc.vpos + id.y)), v2 = xyz(__ldg(sc.vpos + id.z));
+    pl.pos = v0 * bx + v1 * by + v2 * bz;
+    float3 e0 = v2 - v0, e1 = v1 - v0;
+    pl.geo = normalize(cross(e0, e1));
+    pl.normal = normalize(normal);
+    pl.mat = (int32_t)id.w;
+    pl.t = h.t;
+    return pl;
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ void flag_error(const FrameArgs& fa, uint32_t bits) { atomicOr(&fa.counters[63], bits); }
+
+// ---------------------------------------------------------------------------
+// one bounce of one path
+// ---------------------------------------------------------------------------
+struct PathState {
+    float3 o, d, thr;
+    uint32_t pixel, rng;
+    float pq;
+};
+
+template <bool COMPAT>
+__device__ __forceinline__ void write_invalid(const FrameArgs& fa, uint32_t p, float3 x_view, float3 n_view, float3 le0) {
+    if (COMPAT) {
+        fa.s_xv[p] = f4(x_view, __uint_as_float(kInvalid));
+        fa.s_nv[p] = f4(n_view, __uint_as_float(0u));
+        fa.s_xs[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        fa.s_ns[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        fa.s_L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (fa.write_pt) fa.le0[p] = f4(le0, 0.0f);
+    } else {
+        fa.gb_pos_cur[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        fa.gb_mat_cur[p] = kInvalid;
+        fa.cand_a[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        fa.cand_b[p] = f4(le0, __uint_as_float(0u));
+    }
+}
+
+template <bool COMPAT>
+__device__ __forceinline__ void write_sample(const FrameArgs& fa, uint32_t p, float3 x_s, float3 n_s, float3 L, float pq) {
+    if (COMPAT) {
+        fa.s_xs[p] = f4(x_s, pq);
+        fa.s_ns[p] = f4(n_s, 0.0f);
+        fa.s_L[p] = f4(L, 0.0f);
+    } else {
+        fa.cand_a[p] = f4(x_s, pq);
+        fa.cand_b[p] = f4(L, __uint_as_float(oct_encode(n_s, 12) | 0x80000000u));
+    }
+}
+
+template <bool COMPAT>
+__device__ __forceinline__ void add_radiance(const FrameArgs& fa, uint32_t p, float3 add) {
+    float4* dst = COMPAT ? fa.s_L : fa.cand_b;
+    float4 v = dst[p];
+    float3 L = xyz(v) + add;
+    dst[p] = f4(L, v.w);
+}
+
+// Returns true when the path continues to bounce + 1 (state updated in place).
+template <bool COMPAT>
+__device__ __forceinline__ bool bounce_step(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
+                                            uint32_t bounce, uint32_t nb, PathState& s) {
+    const uint32_t p = s.pixel;
+    HitRec h;
+    if (!traverse<false>(fa.sc, s.o, s.d, 0.0001f, 10000.0f, h)) flag_error(fa, XR_DEVFLAG_STACK_OVERFLOW);
+    HitPayload pl;
+    pl.mat = -1;
+    if (h.prim >= 0) pl = closest_hit(fa.sc, h);
+    const bool sky = u->has_sky_box != 0u;
+    const float3 sky_c = f3(1.0f, 1.0f, 1.0f);
+    if (pl.mat == -1) {
+        if (bounce == 0) {
+            write_invalid<COMPAT>(fa, p, f3(0.0f, 0.0f, 0.0f), f3(0.0f, 0.0f, 0.0f), sky ? sky_c : f3(0.0f, 0.0f, 0.0f));
+        } else if (bounce == 1) {
+            float3 L = f3(0.0f, 0.0f, 0.0f);
+            if (sky) L = L + s.thr * sky_c;
+            write_sample<COMPAT>(fa, p, s.o + s.d * 1000.0f, -s.d, L, s.pq);
+        } else if (sky) {
+            add_radiance<COMPAT>(fa, p, s.thr * sky_c);
+        }
+        return false;
+    }
+    if ((uint32_t)pl.mat >= fa.sc.n_mats) {
+        flag_error(fa, XR_DEVFLAG_BAD_INDEX);
+        if (bounce == 0) write_invalid<COMPAT>(fa, p, f3(0.0f, 0.0f, 0.0f), f3(0.0f, 0.0f, 0.0f), f3(0.0f, 0.0f, 0.0f));
+        else if (bounce == 1) write_sample<COMPAT>(fa, p, f3(0, 0, 0), f3(0, 0, 1), f3(0, 0, 0), s.pq);
+        return false;
+    }
+    const XrMaterial mat = fa.sc.mats[pl.mat];
+    if (!COMPAT) {
+        float3 wo = -s.d;
+        if (dot(pl.geo, wo) < 0.0f) pl.geo = -pl.geo;
+        if (dot(pl.normal, pl.geo) < 0.0f) pl.normal = -pl.normal;
+    }
+    if (mat.material_model == XR_MAT_DIFFUSE_LIGHT) {
+        float3 base = f3(mat.base_color[0], mat.base_color[1], mat.base_color[2]);
+        float3 term = s.thr * base * 4.0f;
+        if (bounce == 0) {
+            write_invalid<COMPAT>(fa, p, pl.pos, pl.normal, base * 4.0f);
+        } else if (bounce == 1) {
+            float3 L = f3(0.0f, 0.0f, 0.0f) + term;
+            write_sample<COMPAT>(fa, p, pl.pos, pl.normal, L, s.pq);
+        } else {
+            add_radiance<COMPAT>(fa, p, term);
+        }
+        return false;
+    }
+    float pdf = 0.0f, cos_theta = 0.0f;
+    float3 wi;
+    const float3 wo = -s.d;
+    const float3 x_s = pl.pos, n_s = pl.normal;
+    const uint32_t seed_this = s.rng;
+    float3 f = sample_bsdf<COMPAT>(pl.normal, mat, wo, &wi, &pdf, &cos_theta, s.rng);
+    float3 factor = div3(f * cos_theta, pdf);
+    if (!COMPAT && !(pdf > 0.0f)) factor = f3(0.0f, 0.0f, 0.0f);
+    bool alive = COMPAT ? true : (pdf > 0.0f);
+    if (bounce == 0) {
+        if (COMPAT) {
+            fa.s_xv[p] = f4(pl.pos, __uint_as_float((uint32_t)pl.mat));
+            fa.s_nv[p] = f4(pl.normal, __uint_as_float(seed_this));
+        } else {
+            fa.gb_pos_cur[p] = f4(pl.pos, __uint_as_float(oct_encode(pl.normal, 16)));
+            fa.gb_mat_cur[p] = (uint32_t)pl.mat;
+        }
+        if (fa.write_pt) fa.thr0[p] = f4(factor, 0.0f);
+        s.pq = pdf;
+    } else {
+        s.thr = s.thr * factor;
+    }
+    if (alive && bounce > 3) {
+        float pr = fmaxf(s.thr.x, fmaxf(s.thr.y, s.thr.z));
+        if (random_float(s.rng) > pr) alive = false;
+        else s.thr = s.thr * (1.0f / pr);
+    }
+    if (bounce + 1 >= nb) alive = false;   // the next iteration would hit the depth limit
+    if (bounce == 1) write_sample<COMPAT>(fa, p, x_s, n_s, f3(0.0f, 0.0f, 0.0f), s.pq);
+    if (bounce == 0 && !alive) {
+        if (COMPAT) {
+            fa.s_xs[p] = make_float4(0.0f, 0.0f, 0.0f, pdf);
+            fa.s_ns[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            fa.s_L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            fa.cand_a[p] = make_float4(0.0f, 0.0f, 0.0f, pdf);
+            fa.cand_b[p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0u));
+        }
+    }
+    if (alive) {
+        float3 hit_pos = s.o + s.d * pl.t;
+        float3 off = dot(wi, pl.geo) > 0.0f ? pl.geo : -pl.geo;
+        s.o = hit_pos + off * 0.01f;
+        s.d = wi;
+        if (bounce == 0) s.thr = f3(1.0f, 1.0f, 1.0f);
+    }
+    return alive;
+}
+
+__device__ __forceinline__ void push_path(const FrameArgs& fa, bool alive, const PathState& s, uint32_t qslot) {
+    uint32_t mask = __ballot_sync(0xFFFFFFFFu, alive);
+    if (mask == 0u) return;
+    uint32_t lane = lane_id();
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(&fa.counters[qslot], (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (alive) {
+        uint32_t i = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+        fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
+        fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
+        fa.q_out[2][i] = f4(s.thr, s.pq);
+    }
+}
+
+__device__ __forceinline__ void count_rays(const FrameArgs& fa, bool active) {
+    uint32_t mask = __ballot_sync(0xFFFFFFFFu, active);
+    if (lane_id() == 0 && mask) atomicAdd(&fa.counters[33], (uint32_t)__popc(mask));
+}
+
+// bounce 0: camera rays for a 16 x 8 pixel tile per block
+template <bool COMPAT>
+__global__ void __launch_bounds__(kBlock) k_bounce0(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t nb) {
+    const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 4);
+    const bool inside = x < fa.W && y < fa.H;
+    PathState s;
+    bool alive = false;
+    if (inside) {
+        s.pixel = y * fa.W + x;
+        s.rng = pass_rng(COMPAT, x, y, fa.W, u->current_frame, kPassInitial, fa.seed);
+        float ox = random_float(s.rng);
+        float oy = random_float(s.rng);
+        float px = (float)x + ox, py = (float)y + oy;
+        float uvx = (px / (float)fa.W) * 2.0f - 1.0f, uvy = (py / (float)fa.H) * 2.0f - 1.0f;
+        float4 origin = mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f));
+        float4 target = mat_mul(u->projection_inverse, make_float4(uvx, uvy, 1.0f, 1.0f));
+        float3 tn = normalize(xyz(target));
+        s.d = normalize(xyz(mat_mul(u->view_inverse, make_float4(tn.x, tn.y, tn.z, 0.0f))));
+        s.o = xyz(origin);
+        s.thr = f3(1.0f, 1.0f, 1.0f);
+        s.pq = 0.0f;
+        if (nb == 0u) {
+            write_invalid<COMPAT>(fa, s.pixel, f3(0, 0, 0), f3(0, 0, 0), f3(0, 0, 0));
+        } else {
+            alive = bounce_step<COMPAT>(fa, u, 0u, nb, s);
+        }
+    }
+    count_rays(fa, inside && nb != 0u);
+    push_path(fa, alive, s, 1u);
+}
+
+// bounce >= 1: persistent grid over the queue written by the previous bounce
+template <bool COMPAT>
+__global__ void __launch_bounds__(kBlock) k_bounce(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t bounce,
+                                                   uint32_t nb) {
+    const uint32_t count = *(volatile const uint32_t*)&fa.counters[bounce];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
+        uint32_t i = base + threadIdx.x;
+        bool active = i < count;
+        PathState s;
+        bool alive = false;
+        if (active) {
+            float4 a = fa.q_in[0][i], b = fa.q_in[1][i], c = fa.q_in[2][i];
+            s.o = xyz(a); s.pixel = __float_as_uint(a.w);
+            s.d = xyz(b); s.rng = __float_as_uint(b.w);
+            s.thr = xyz(c); s.pq = c.w;
+            alive = bounce_step<COMPAT>(fa, u, bounce, nb, s);
+        }
+        count_rays(fa, active);
+        push_path(fa, alive, s, bounce + 1u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reservoir passes
+// ---------------------------------------------------------------------------
+struct Res {            // one reservoir in registers (selected sample + weights)
+    float3 xs, L, ns, f;
+    uint32_t code;      // corrected layout: oct12 code of ns
+    float w_sum, W;
+    uint32_t m;
+};
+__device__ __forceinline__ void res_init(Res& r) {
+    r.xs = f3(0, 0, 0); r.L = f3(0, 0, 0); r.ns = f3(0, 0, 0); r.f = f3(0, 0, 0);
+    r.code = 0u; r.w_sum = 0.0f; r.W = 0.0f; r.m = 0u;
+}
+// UpdateReservoir (ReSTIRGICommon.hlsl:52-61): candidate fields passed by value
+__device__ __forceinline__ void res_update(Res& r, const Res& cand, float w_new, uint32_t& seed) {
+    r.w_sum += w_new;
+    r.m++;
+    if (random_float(seed) < w_new / fmaxf(1e-10f, r.w_sum)) {
+        r.xs = cand.xs; r.L = cand.L; r.ns = cand.ns; r.f = cand.f; r.code = cand.code;
+    }
+}
+// MergeReservoir (ReSTIRGICommon.hlsl:63-73)
+__device__ __forceinline__ void res_merge(Res& t, const Res& src, float p_hat, uint32_t& seed) {
+    uint32_t M0 = t.m;
+    float w_new = p_hat * src.W * (float)src.m;
+    res_update(t, src, w_new, seed);
+    t.m = M0 + src.m;
+}
+// ReSTIRGITemporalReuse.rgen.hlsl:33-40
+__device__ __forceinline__ float eval_target(float3 xs, float3 L, float3 x_curr, float3 n_curr) {
+    float3 wi = normalize(xs - x_curr);
+    float c = dot(n_curr, wi);
+    if (c <= 0.0f) return 0.0f;
+    return length(L);
+}
+
+__device__ __forceinline__ void load_wide(const FrameArgs& fa, float4* const* planes, uint32_t i, Res& r) {
+    float4 a = planes[0][i], b = planes[1][i], c = planes[2][i], d = planes[3][i];
+    r.xs = xyz(a); r.W = a.w;
+    r.L = xyz(b); r.w_sum = b.w;
+    r.ns = xyz(c); r.m = __float_as_uint(c.w);
+    r.f = xyz(d); r.code = 0u;
+}
+__device__ __forceinline__ void store_wide(float4* const* planes, uint32_t i, const Res& r) {
+    planes[0][i] = f4(r.xs, r.W);
+    planes[1][i] = f4(r.L, r.w_sum);
+    planes[2][i] = f4(r.ns, __uint_as_float(r.m));
+    planes[3][i] = f4(r.f, 0.0f);
+}
+__device__ __forceinline__ void load_packed(const float4* p0, const float4* p1, uint32_t i, Res& r) {
+    float4 a = p0[i], b = p1[i];
+    uint32_t w = __float_as_uint(b.w);
+    r.xs = xyz(a); r.W = a.w;
+    r.L = xyz(b);
+    r.code = w & 0x00FFFFFFu;
+    r.m = w >> 24;
+    r.ns = oct_decode(r.code, 12);
+    r.f = f3(0, 0, 0);
+    r.w_sum = 0.0f;
+}
+__device__ __forceinline__ void store_packed(float4* p0, float4* p1, uint32_t i, const Res& r) {
+    p0[i] = f4(r.xs, r.W);
+    p1[i] = f4(r.L, __uint_as_float((r.code & 0x00FFFFFFu) | (r.m << 24)));
+}
+
+__device__ __forceinline__ void write_out(const FrameArgs& fa, uint32_t p, float3 c, bool tonemap) {
+    if (fa.out_hdr) fa.out_hdr[p] = f4(c, 1.0f);
+    if (tonemap) {
+        fa.out_ldr[p] = tonemap_ldr(c);
+    } else {
+        fa.out_ldr[p] = make_uchar4(unorm8(c.x), unorm8(c.y), unorm8(c.z), 255);
+    }
+}
+
+__device__ __forceinline__ float3 mat_albedo_over_pi(const FrameArgs& fa, uint32_t m) {
+    const XrMaterial& mm = fa.sc.mats[m];
+    return f3(mm.base_color[0], mm.base_color[1], mm.base_color[2]) * XR_INV_PI_F;
+}
+
+// ---- temporal, compat layout (the reference's fields and quirks) ----
+__global__ void __launch_bounds__(256) k_temporal_compat(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    const uint32_t x = p % fa.W, y = p / fa.W, N = fa.N;
+    uint32_t rng = pass_rng(true, x, y, fa.W, u->current_frame, kPassTemporal, fa.seed);
+    const uint32_t pp = u->current_frame % 2u;
+    const uint32_t cur = pp * N, prev = (1u - pp) * N;
+    float4 xv = fa.s_xv[p], nv = fa.s_nv[p], xs = fa.s_xs[p], ns = fa.s_ns[p], Lv = fa.s_L[p];
+    const uint32_t mat = __float_as_uint(xv.w);
+    if (fa.write_pt) {
+        float3 v = mat != kInvalid ? xyz(fa.thr0[p]) * xyz(Lv) : xyz(fa.le0[p]);
+        fa.out_pt[p] = f4(v, 1.0f);
+    }
+    if (length(xyz(ns)) == 0.0f) {
+        Res e; res_init(e);
+        store_wide(fa.rw, cur + p, e);
+        store_wide(fa.rsw, cur + p, e);
+        return;
+    }
+    bool found = false;
+    Res r_prev; res_init(r_prev);
+    {
+        float2 cuv = make_float2(((float)x + 0.5f) / (float)fa.W, ((float)y + 0.5f) / (float)fa.H);
+        float2 puv0 = world_to_screen_uv(xyz(xv), u->view_prev, u->projection_prev);
+        float mvx = half_round(cuv.x - puv0.x), mvy = half_round(cuv.y - puv0.y);
+        float fx = (cuv.x - mvx) * (float)fa.W, fy = (cuv.y - mvy) * (float)fa.H;
+        if (fx > -1.0f && fx < (float)fa.W && fy > -1.0f && fy < (float)fa.H) {
+            uint32_t q = (uint32_t)(int)fy * fa.W + (uint32_t)(int)fx;
+            // previous G-buffer aliases the current one: validity of this frame at q
+            if (__float_as_uint(fa.s_xv[q].w) != kInvalid) {
+                load_wide(fa, fa.rw, prev + q, r_prev);
+                found = true;
+            } else {
+                Res e; res_init(e);
+                store_wide(fa.rsw, cur + p, e);
+            }
+        }
+    }
+    if (!fa.temporal_on) found = false;
+    Res s_new;
+    s_new.xs = xyz(xs); s_new.L = xyz(Lv); s_new.ns = xyz(ns); s_new.f = mat_albedo_over_pi(fa, mat); s_new.code = 0u;
+    const float3 x_curr = xyz(xv);
+    const float3 n_curr = normalize(xyz(nv));
+    Res r; res_init(r);
+    r.code = 0u;
+    float tp_new = eval_target(s_new.xs, s_new.L, x_curr, n_curr);
+    float w_new = (xs.w > 1e-6f) ? (tp_new / xs.w) : 0.0f;
+    res_update(r, s_new, w_new, rng);
+    if (found) {
+        float tp_prev = eval_target(r_prev.xs, r_prev.L, x_curr, n_curr);
+        res_merge(r, r_prev, tp_prev, rng);
+    } else {
+        r.m = 1u;
+    }
+    if (r.m > 30u) {
+        r.w_sum *= (float)30u / (float)r.m;
+        r.m = 30u;
+    }
+    float tpf = eval_target(r.xs, r.L, x_curr, n_curr);
+    r.W = (tpf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * tpf) : 0.0f;
+    store_wide(fa.rw, cur + p, r);
+    if (out_here) {
+        float3 c = f3(0, 0, 0);
+        if (r.W > 0.0f) {
+            float3 wi = normalize(r.xs - x_curr);
+            float ct = fmaxf(0.0f, dot(xyz(nv), wi));
+            c = r.L * r.W * r.f * ct;
+        }
+        write_out(fa, p, c, true);
+    }
+}
+
+__device__ __forceinline__ uint32_t neighbor_index(uint32_t x, uint32_t y, uint32_t W, uint32_t H, float max_r, uint32_t& seed) {
+    float randa = random_float(seed) * 2.0f * XR_PI_F;
+    float randr = sqrtf(random_float(seed)) * max_r;
+    float s, c;
+    sincos_xr(randa, &s, &c);
+    int32_t ox = (int32_t)floorf(c * randr), oy = (int32_t)floorf(s * randr);
+    int32_t cx = min(max((int32_t)x + ox, 0), (int32_t)W - 1);
+    int32_t cy = min(max((int32_t)y + oy, 0), (int32_t)H - 1);
+    return (uint32_t)cy * W + (uint32_t)cx;
+}
+
+__device__ __forceinline__ float jacobian_of(float3 x_nb_view, float3 x_view, float3 xs, float3 ns) {
+    float3 v_orig = x_nb_view - xs;
+    float d2o = dot(v_orig, v_orig);
+    float3 v_curr = x_view - xs;
+    float d2c = dot(v_curr, v_curr);
+    float jac = 1.0f;
+    if (d2o > 1e-6f && d2c > 1e-6f) {
+        float3 dir_o = v_orig * (1.0f / sqrtf(d2o));
+        float3 dir_c = v_curr * (1.0f / sqrtf(d2c));
+        float cpo = fmaxf(0.0f, dot(ns, dir_o));
+        float cpc = fmaxf(0.0f, dot(ns, dir_c));
+        if (cpo > 1e-6f) jac = (cpc * d2o) / (cpo * d2c);
+    }
+    return fminf(fmaxf(jac, 0.1f), 10.0f);
+}
+
+// ---- spatial, compat layout ----
+__global__ void __launch_bounds__(256) k_spatial_compat(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    const uint32_t x = p % fa.W, y = p / fa.W, N = fa.N;
+    uint32_t rng = pass_rng(true, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
+    const uint32_t pp = u->current_frame % 2u;
+    const uint32_t read_off = pp * N, write_off = (1u - pp) * N;
+    const bool reuse = u->reuse != 0u;
+    float4 xv = fa.s_xv[p], nv = fa.s_nv[p], ns = fa.s_ns[p];
+    if (length(xyz(nv)) == 0.0f) { if (reuse) write_out(fa, p, f3(0, 0, 0), false); return; }
+    if (length(xyz(ns)) == 0.0f) { if (reuse) write_out(fa, p, f3(1, 1, 1), false); return; }
+    const uint32_t mat = __float_as_uint(xv.w);
+    Res center; load_wide(fa, fa.rw, read_off + p, center);
+    Res r; res_init(r);
+    res_merge(r, center, length(center.L), rng);
+    for (int i = 0; i < 6; i++) {
+        uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, 5.0f, rng);
+        float4 nxv = fa.s_xv[nbi], nnv = fa.s_nv[nbi];
+        if (length(xyz(nnv)) == 0.0f) continue;
+        float3 dd = xyz(xv) - xyz(nxv);
+        if (dot(dd, dd) > 0.1f) continue;
+        if (dot(xyz(nv), xyz(nnv)) < 0.8f) continue;
+        if (mat != __float_as_uint(nxv.w)) continue;
+        Res rn; load_wide(fa, fa.rw, read_off + nbi, rn);
+        float jac = jacobian_of(xyz(nxv), xyz(xv), rn.xs, rn.ns);
+        float ph = length(rn.L) * jac;
+        res_merge(r, rn, ph, rng);
+        if (ph == 0.0f) r.m -= rn.m;
+    }
+    r.m = min(r.m, 300u);
+    float phf = length(r.L);
+    r.W = (phf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * phf) : 0.0f;
+    store_wide(fa.rsw, write_off + p, r);
+    if (reuse) {
+        float3 c = f3(0, 0, 0);
+        if (r.W > 0.0f) {
+            float3 wi = normalize(r.xs - xyz(xv));
+            float ct = fmaxf(0.0f, dot(xyz(nv), wi));
+            c = r.L * r.W * r.f * ct;
+        }
+        write_out(fa, p, c, true);
+    }
+}
+
+// ---- corrected mode ----
+__device__ __forceinline__ float3 shade_corrected(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
+                                                  const Res& r, float3 x_view, float3 n_view, uint32_t mat) {
+    float3 c = f3(0, 0, 0);
+    if (r.W > 0.0f) {
+        float3 wi = normalize(r.xs - x_view);
+        float ct = fmaxf(0.0f, dot(n_view, wi));
+        float3 cam = xyz(mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));
+        float3 wo = normalize(cam - x_view);
+        float3 f = eval_world(fa.sc.mats[mat], n_view, wo, wi);
+        c = r.L * r.W * f * ct;
+    }
+    return c;
+}
+
+__global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    const uint32_t x = p % fa.W, y = p / fa.W;
+    float4 g = fa.gb_pos_cur[p];
+    uint32_t mat = fa.gb_mat_cur[p];
+    float4 a = fa.cand_a[p], b = fa.cand_b[p];
+    const uint32_t bw = __float_as_uint(b.w);
+    const bool valid = mat != kInvalid, has = (bw >> 31) != 0u;
+    if (fa.write_pt) {
+        float3 v = valid ? xyz(fa.thr0[p]) * (has ? xyz(b) : f3(0, 0, 0)) : xyz(b);
+        fa.out_pt[p] = f4(v, 1.0f);
+    }
+    if (!valid || !has) {
+        Res e; res_init(e);
+        store_packed(fa.rt_cur0, fa.rt_cur1, p, e);
+        if (out_here) write_out(fa, p, valid ? f3(0, 0, 0) : xyz(b), true);
+        return;
+    }
+    uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassTemporal, fa.seed);
+    const float3 x_view = xyz(g);
+    const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
+    Res s_new;
+    s_new.xs = xyz(a); s_new.L = xyz(b); s_new.code = bw & 0x00FFFFFFu; s_new.ns = oct_decode(s_new.code, 12);
+    s_new.f = f3(0, 0, 0);
+    bool found = false;
+    Res r_prev; res_init(r_prev);
+    if (fa.temporal_on) {
+        float2 puv = world_to_screen_uv(x_view, u->view_prev, u->projection_prev);
+        float fx = floorf(puv.x * (float)fa.W), fy = floorf(puv.y * (float)fa.H);
+        if (fx >= 0.0f && fx < (float)fa.W && fy >= 0.0f && fy < (float)fa.H) {
+            uint32_t q = (uint32_t)fy * fa.W + (uint32_t)fx;
+            if (fa.gb_mat_prev[q] == mat) {
+                float4 pg = fa.gb_pos_prev[q];
+                float3 pn = oct_decode(__float_as_uint(pg.w), 16);
+                float3 dd = x_view - xyz(pg);
+                if (!(dot(n_view, pn) < 0.8f) && !(dot(dd, dd) > 0.1f)) {
+                    load_packed(fa.rt_prev0, fa.rt_prev1, q, r_prev);
+                    found = true;
+                }
+            }
+        }
+    }
+    const float3 x_curr = x_view;
+    const float3 n_curr = normalize(n_view);
+    Res r; res_init(r);
+    float tp_new = eval_target(s_new.xs, s_new.L, x_curr, n_curr);
+    float w_new = (a.w > 1e-6f) ? (tp_new / a.w) : 0.0f;
+    res_update(r, s_new, w_new, rng);
+    if (found) {
+        float tp_prev = eval_target(r_prev.xs, r_prev.L, x_curr, n_curr);
+        res_merge(r, r_prev, tp_prev, rng);
+    } else {
+        r.m = 1u;
+    }
+    if (r.m > fa.m_cap_t) {
+        r.w_sum *= (float)fa.m_cap_t / (float)r.m;
+        r.m = fa.m_cap_t;
+    }
+    float tpf = eval_target(r.xs, r.L, x_curr, n_curr);
+    r.W = (tpf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * tpf) : 0.0f;
+    store_packed(fa.rt_cur0, fa.rt_cur1, p, r);
+    if (out_here) write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);
+}
+
+__global__ void __launch_bounds__(256) k_spatial(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    const uint32_t x = p % fa.W, y = p / fa.W;
+    float4 g = fa.gb_pos_cur[p];
+    uint32_t mat = fa.gb_mat_cur[p];
+    float4 b = fa.cand_b[p];
+    const bool valid = mat != kInvalid, has = (__float_as_uint(b.w) >> 31) != 0u;
+    if (!valid || !has) {
+        Res e; res_init(e);
+        store_packed(fa.rs0, fa.rs1, p, e);
+        write_out(fa, p, valid ? f3(0, 0, 0) : xyz(b), true);
+        return;
+    }
+    uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
+    const float3 x_view = xyz(g);
+    const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
+    Res center; load_packed(fa.rt_cur0, fa.rt_cur1, p, center);
+    Res r; res_init(r);
+    res_merge(r, center, length(center.L), rng);
+    uint32_t shadow = 0;
+    for (uint32_t i = 0; i < fa.n_nb; i++) {
+        uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, fa.radius, rng);
+        uint32_t nmat = fa.gb_mat_cur[nbi];
+        if (nmat == kInvalid) continue;
+        float4 ng = fa.gb_pos_cur[nbi];
+        float3 dd = x_view - xyz(ng);
+        if (dot(dd, dd) > 0.1f) continue;
+        if (dot(n_view, oct_decode(__float_as_uint(ng.w), 16)) < 0.8f) continue;
+        if (mat != nmat) continue;
+        Res rn; load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
+        float jac = jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
+        float ph = length(rn.L) * jac;
+        if (fa.visibility && ph > 0.0f) {
+            float3 dir = rn.xs - x_view;
+            float dist = length(dir);
+            float3 ro = x_view + n_view * 0.01f;
+            HitRec hh;
+            if (!traverse<true>(fa.sc, ro, normalize(dir), 0.0f, dist - 0.01f, hh)) flag_error(fa, XR_DEVFLAG_STACK_OVERFLOW);
+            shadow++;
+            if (hh.prim >= 0) ph = 0.0f;
+        }
+        res_merge(r, rn, ph, rng);
+        if (ph == 0.0f) r.m -= rn.m;
+    }
+    if (r.m > fa.m_cap_s) {
+        r.w_sum *= (float)fa.m_cap_s / (float)r.m;
+        r.m = fa.m_cap_s;
+    }
+    float phf = length(r.L);
+    r.W = (phf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * phf) : 0.0f;
+    store_packed(fa.rs0, fa.rs1, p, r);
+    write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);
+    if (shadow) atomicAdd(&fa.counters[32], shadow);
+}
+
+// ---------------------------------------------------------------------------
+// conversion to and from the reference layouts (ReSTIRGICommon.hlsl:6-30)
+// ---------------------------------------------------------------------------
+__global__ void k_export_samples(FrameArgs fa, uint32_t* __restrict__ out) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    uint32_t w[24];
+    for (int i = 0; i < 24; i++) w[i] = 0u;
+    auto put3 = [&](int at, float3 v) { w[at] = __float_as_uint(v.x); w[at + 1] = __float_as_uint(v.y); w[at + 2] = __float_as_uint(v.z); };
+    if (fa.compat) {
+        float4 xv = fa.s_xv[p], nv = fa.s_nv[p], xs = fa.s_xs[p], ns = fa.s_ns[p], L = fa.s_L[p];
+        uint32_t mat = __float_as_uint(xv.w);
+        put3(0, xyz(xv)); w[3] = mat;
+        put3(4, xyz(nv)); w[7] = __float_as_uint(nv.w);
+        put3(8, xyz(xs)); w[11] = __float_as_uint(xs.w);
+        put3(12, xyz(ns));
+        put3(16, xyz(L));
+        if (mat != kInvalid && mat < fa.sc.n_mats) put3(20, mat_albedo_over_pi(fa, mat));
+    } else {
+        float4 g = fa.gb_pos_cur[p], a = fa.cand_a[p], b = fa.cand_b[p];
+        uint32_t mat = fa.gb_mat_cur[p], bw = __float_as_uint(b.w);
+        bool valid = mat != kInvalid, has = (bw >> 31) != 0u;
+        w[3] = mat;
+        if (valid) {
+            uint32_t c16 = __float_as_uint(g.w);
+            put3(0, xyz(g));
+            put3(4, oct_decode(c16, 16));
+            w[7] = c16;
+            w[11] = __float_as_uint(a.w);
+        }
+        if (has) {
+            put3(8, xyz(a));
+            put3(12, oct_decode(bw & 0x00FFFFFFu, 12));
+            w[15] = bw;
+            put3(16, xyz(b));
+        }
+    }
+    uint4* o = reinterpret_cast<uint4*>(out + 24u * p);
+    for (int i = 0; i < 6; i++) o[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+}
+
+struct Planes4 { float4* p[4]; };
+
+__global__ void k_export_res_wide(Planes4 pl, uint32_t n, uint32_t* __restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = pl.p[0][i], b = pl.p[1][i], c = pl.p[2][i], d = pl.p[3][i];
+    uint32_t w[28];
+    for (int k = 0; k < 28; k++) w[k] = 0u;
+    w[0] = __float_as_uint(b.w); w[1] = __float_as_uint(a.w); w[2] = __float_as_uint(c.w);
+    w[12] = __float_as_uint(a.x); w[13] = __float_as_uint(a.y); w[14] = __float_as_uint(a.z);
+    w[16] = __float_as_uint(c.x); w[17] = __float_as_uint(c.y); w[18] = __float_as_uint(c.z);
+    w[20] = __float_as_uint(b.x); w[21] = __float_as_uint(b.y); w[22] = __float_as_uint(b.z);
+    w[24] = __float_as_uint(d.x); w[25] = __float_as_uint(d.y); w[26] = __float_as_uint(d.z);
+    uint4* o = reinterpret_cast<uint4*>(out + 28u * i);
+    for (int k = 0; k < 7; k++) o[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+}
+
+__global__ void k_export_res_packed(const float4* __restrict__ p0, const float4* __restrict__ p1, uint32_t n,
+                                    uint32_t* __restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Res r;
+    load_packed(p0, p1, i, r);
+    uint32_t w[28];
+    for (int k = 0; k < 28; k++) w[k] = 0u;
+    w[1] = __float_as_uint(r.W); w[2] = r.m;
+    w[12] = __float_as_uint(r.xs.x); w[13] = __float_as_uint(r.xs.y); w[14] = __float_as_uint(r.xs.z);
+    w[16] = __float_as_uint(r.ns.x); w[17] = __float_as_uint(r.ns.y); w[18] = __float_as_uint(r.ns.z);
+    w[19] = r.code;
+    w[20] = __float_as_uint(r.L.x); w[21] = __float_as_uint(r.L.y); w[22] = __float_as_uint(r.L.z);
+    uint4* o = reinterpret_cast<uint4*>(out + 28u * i);
+    for (int k = 0; k < 7; k++) o[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+}
+
+__global__ void k_import_samples(FrameArgs fa, const uint32_t* __restrict__ in) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    const uint32_t* w = in + 24u * p;
+    auto get3 = [&](int at) { return f3(__uint_as_float(w[at]), __uint_as_float(w[at + 1]), __uint_as_float(w[at + 2])); };
+    if (fa.compat) {
+        fa.s_xv[p] = f4(get3(0), __uint_as_float(w[3]));
+        fa.s_nv[p] = f4(get3(4), __uint_as_float(w[7]));
+        fa.s_xs[p] = f4(get3(8), __uint_as_float(w[11]));
+        fa.s_ns[p] = f4(get3(12), 0.0f);
+        fa.s_L[p] = f4(get3(16), 0.0f);
+    } else {
+        uint32_t mat = w[3];
+        bool valid = mat != kInvalid, has = (w[15] >> 31) != 0u;
+        fa.gb_pos_cur[p] = valid ? f4(get3(0), __uint_as_float(w[7])) : make_float4(0, 0, 0, 0);
+        fa.gb_mat_cur[p] = mat;
+        fa.cand_a[p] = valid ? f4(has ? get3(8) : f3(0, 0, 0), __uint_as_float(w[11])) : make_float4(0, 0, 0, 0);
+        fa.cand_b[p] = has ? f4(get3(16), __uint_as_float(w[15])) : make_float4(0, 0, 0, 0);
+    }
+}
+
+__global__ void k_import_res_wide(Planes4 pl, uint32_t n, const uint32_t* __restrict__ in) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t* w = in + 28u * i;
+    auto g = [&](int k) { return __uint_as_float(w[k]); };
+    pl.p[0][i] = make_float4(g(12), g(13), g(14), g(1));
+    pl.p[1][i] = make_float4(g(20), g(21), g(22), g(0));
+    pl.p[2][i] = make_float4(g(16), g(17), g(18), __uint_as_float(w[2]));
+    pl.p[3][i] = make_float4(g(24), g(25), g(26), 0.0f);
+}
+
+__global__ void k_import_res_packed(float4* __restrict__ p0, float4* __restrict__ p1, uint32_t n, const uint32_t* __restrict__ in) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t* w = in + 28u * i;
+    auto g = [&](int k) { return __uint_as_float(w[k]); };
+    p0[i] = make_float4(g(12), g(13), g(14), g(1));
+    p1[i] = make_float4(g(20), g(21), g(22), __uint_as_float((w[19] & 0x00FFFFFFu) | (min(w[2], 255u) << 24)));
+}
+
+}  // namespace
+
+uint32_t persistent_grid(int sm_count, bool compat) {
+    static int occ[2] = {0, 0};
+    int& o = occ[compat ? 1 : 0];
+    if (o == 0) {
+        int v = 0;
+        if (compat) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_bounce<true>, kBlock, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_bounce<false>, kBlock, 0);
+        o = v > 0 ? v : 4;
+    }
+    return (uint32_t)(o * sm_count);
+}
+
+void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
+    dim3 grid0((fa.W + 15u) / 16u, (fa.H + 7u) / 8u);
+    FrameArgs a = fa;
+    if (fa.compat) k_bounce0<true><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
+    else k_bounce0<false><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
+    for (uint32_t b = 1; b < nb; b++) {
+        // queues alternate: bounce b reads what bounce b-1 wrote
+        for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
+        if (fa.compat) k_bounce<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
+        else k_bounce<false><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
+    }
+}
+
+void launch_temporal(const FrameArgs& fa, bool write_image, cudaStream_t st) {
+    uint32_t blocks = (fa.N + 255u) / 256u;
+    if (fa.compat) k_temporal_compat<<<blocks, 256, 0, st>>>(fa, fa.ubo, write_image);
+    else k_temporal<<<blocks, 256, 0, st>>>(fa, fa.ubo, write_image);
+}
+
+void launch_export_samples(const FrameArgs& fa, uint32_t* out, cudaStream_t st) {
+    k_export_samples<<<(fa.N + 255u) / 256u, 256, 0, st>>>(fa, out);
+}
+void launch_import_samples(const FrameArgs& fa, const uint32_t* in, cudaStream_t st) {
+    k_import_samples<<<(fa.N + 255u) / 256u, 256, 0, st>>>(fa, in);
+}
+void launch_export_res_wide(float4* const planes[4], uint32_t n, uint32_t* out, cudaStream_t st) {
+    Planes4 pl{{planes[0], planes[1], planes[2], planes[3]}};
+    k_export_res_wide<<<(n + 255u) / 256u, 256, 0, st>>>(pl, n, out);
+}
+void launch_export_res_packed(const float4* p0, const float4* p1, uint32_t n, uint32_t* out, cudaStream_t st) {
+    k_export_res_packed<<<(n + 255u) / 256u, 256, 0, st>>>(p0, p1, n, out);
+}
+void launch_import_res_wide(float4* const planes[4], uint32_t n, const uint32_t* in, cudaStream_t st) {
+    Planes4 pl{{planes[0], planes[1], planes[2], planes[3]}};
+    k_import_res_wide<<<(n + 255u) / 256u, 256, 0, st>>>(pl, n, in);
+}
+void launch_import_res_packed(float4* p0, float4* p1, uint32_t n, const uint32_t* in, cudaStream_t st) {
+    k_import_res_packed<<<(n + 255u) / 256u, 256, 0, st>>>(p0, p1, n, in);
+}
+
+void launch_spatial(const FrameArgs& fa, cudaStream_t st) {
+    uint32_t blocks = (fa.N + 255u) / 256u;
+    if (fa.compat) k_spatial_compat<<<blocks, 256, 0, st>>>(fa, fa.ubo);
+    else k_spatial<<<blocks, 256, 0, st>>>(fa, fa.ubo);
+}
+
+}  // namespace xr

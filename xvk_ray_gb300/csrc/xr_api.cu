@@ -1,0 +1,585 @@
+// xr_api.cu -- the C ABI of libxr.so (include/xr.h).
+//
+// Host orchestration of the reference's render pass (ApplicationReSTIRGI.cpp:150-275):
+// upload the frame's UBO, then initial sample -> temporal reuse -> spatial reuse
+// in stream order on the context's own stream.  No exception leaves this file;
+// every failure returns a status and records a message for xr_last_error().
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "xr_internal.h"
+
+namespace xr {
+
+namespace {
+std::mutex g_err_mu;
+std::string g_last_error;
+thread_local std::string t_err_copy;
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+size_t align256(size_t v) { return (v + 255u) & ~size_t(255u); }
+}  // namespace
+
+xr_status fail(const Context* ctx, xr_status code, const std::string& msg) {
+    {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        g_last_error = msg;
+    }
+    if (ctx) const_cast<Context*>(ctx)->last_error = msg;
+    return code;
+}
+
+xr_status cuda_check(Context* ctx, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return XR_OK;
+    (void)cudaGetLastError();
+    xr_status code = (e == cudaErrorMemoryAllocation) ? XR_ERR_OUT_OF_MEMORY : XR_ERR_CUDA;
+    return fail(ctx, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+uint32_t persistent_grid(int sm_count, bool compat);
+
+namespace {
+
+void free_pixels(Context* c) {
+    if (c->pix_mem) cudaFree(c->pix_mem);
+    c->pix_mem = nullptr;
+    c->pix_bytes = 0;
+    FrameArgs z{};
+    z.sc = c->fa.sc;
+    c->fa = z;
+    for (int i = 0; i < 2; i++) { c->gb_pos[i] = nullptr; c->gb_mat[i] = nullptr; c->rt0[i] = nullptr; c->rt1[i] = nullptr; }
+}
+
+// One allocation holds every per-pixel buffer of the selected layout.
+xr_status alloc_pixels(Context* c) {
+    free_pixels(c);
+    const XrParams& P = c->params;
+    const size_t N = (size_t)P.width * P.height;
+    const bool compat = P.compat_reference != 0;
+    struct Item { void** dst; size_t bytes; };
+    std::vector<Item> items;
+    FrameArgs& fa = c->fa;
+    auto add = [&](void** dst, size_t bytes) { items.push_back({dst, bytes}); };
+    if (compat) {
+        add((void**)&fa.s_xv, N * 16); add((void**)&fa.s_nv, N * 16); add((void**)&fa.s_xs, N * 16);
+        add((void**)&fa.s_ns, N * 16); add((void**)&fa.s_L, N * 16);
+        for (int k = 0; k < 4; k++) add((void**)&fa.rw[k], 2 * N * 16);
+        for (int k = 0; k < 4; k++) add((void**)&fa.rsw[k], 2 * N * 16);
+        if (P.write_pt) add((void**)&fa.le0, N * 16);
+    } else {
+        for (int i = 0; i < 2; i++) { add((void**)&c->gb_pos[i], N * 16); add((void**)&c->gb_mat[i], N * 4); }
+        add((void**)&fa.cand_a, N * 16); add((void**)&fa.cand_b, N * 16);
+        for (int i = 0; i < 2; i++) { add((void**)&c->rt0[i], N * 16); add((void**)&c->rt1[i], N * 16); }
+        add((void**)&fa.rs0, N * 16); add((void**)&fa.rs1, N * 16);
+    }
+    if (P.write_pt) { add((void**)&fa.thr0, N * 16); add((void**)&fa.out_pt, N * 16); }
+    add((void**)&fa.out_ldr, N * 4);
+    if (P.write_hdr) add((void**)&fa.out_hdr, N * 16);
+    for (int i = 0; i < 2; i++)
+        for (int k = 0; k < 3; k++) add((void**)&c->q[i][k], N * 16);
+    size_t total = 0;
+    for (auto& it : items) total += align256(it.bytes);
+    void* mem = nullptr;
+    xr_status s = cuda_check(c, cudaMalloc(&mem, total), "cudaMalloc (per-pixel buffers)");
+    if (s) return s;
+    s = cuda_check(c, cudaMemsetAsync(mem, 0, total, c->stream), "memset (per-pixel buffers)");
+    if (s) { cudaFree(mem); return s; }
+    size_t off = 0;
+    for (auto& it : items) { *it.dst = (char*)mem + off; off += align256(it.bytes); }
+    c->pix_mem = mem;
+    c->pix_bytes = total;
+    if (!compat)
+        for (int i = 0; i < 2; i++) cudaMemsetAsync(c->gb_mat[i], 0xFF, N * 4, c->stream);
+    c->W = P.width; c->H = P.height; c->N = (uint32_t)N;
+    fa.W = c->W; fa.H = c->H; fa.N = c->N;
+    fa.counters = c->d_counters;
+    fa.ubo = c->d_ubo;
+    for (int k = 0; k < 3; k++) { fa.q_out[k] = c->q[0][k]; fa.q_in[k] = c->q[1][k]; }
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "per-pixel buffer init");
+}
+
+void set_frame_pointers(Context* c, uint32_t parity) {
+    FrameArgs& fa = c->fa;
+    const XrParams& P = c->params;
+    fa.parity = parity;
+    fa.compat = P.compat_reference; fa.temporal_on = P.temporal_on; fa.spatial_on = P.spatial_on;
+    fa.visibility = P.visibility; fa.write_pt = P.write_pt; fa.seed = P.seed;
+    fa.m_cap_t = P.m_cap_temporal; fa.m_cap_s = P.m_cap_spatial; fa.n_nb = P.n_neighbours; fa.radius = P.radius_px;
+    if (!P.compat_reference) {
+        fa.gb_pos_cur = c->gb_pos[parity]; fa.gb_pos_prev = c->gb_pos[1 - parity];
+        fa.gb_mat_cur = c->gb_mat[parity]; fa.gb_mat_prev = c->gb_mat[1 - parity];
+        fa.rt_cur0 = c->rt0[parity]; fa.rt_cur1 = c->rt1[parity];
+        fa.rt_prev0 = c->rt0[1 - parity]; fa.rt_prev1 = c->rt1[1 - parity];
+    }
+    fa.grid_persistent = persistent_grid(c->sm_count, P.compat_reference != 0);
+}
+
+xr_status upload_ubo(Context* c, const XrUniformBufferObject* ubo) {
+    // the pinned staging copy may still be read by the previous frame's transfer
+    xr_status s = cuda_check(c, cudaEventSynchronize(c->ev[5]), "ubo staging");
+    if (s) return s;
+    *c->h_ubo = *ubo;
+    s = cuda_check(c, cudaMemcpyAsync(c->d_ubo, c->h_ubo, sizeof(XrUniformBufferObject), cudaMemcpyHostToDevice, c->stream),
+                   "ubo upload");
+    if (s) return s;
+    return cuda_check(c, cudaEventRecord(c->ev[5], c->stream), "ubo event");
+}
+
+xr_status check_flags(Context* c) {
+    uint32_t flags = 0;
+    xr_status s = cuda_check(c, cudaMemcpy(&flags, c->d_counters + 63, 4, cudaMemcpyDeviceToHost), "read device flags");
+    if (s) return s;
+    if (flags & ~c->error_flags) {
+        c->error_flags |= flags;
+        std::string m = "device-side check failed:";
+        if (flags & XR_DEVFLAG_STACK_OVERFLOW) m += " traversal stack overflow;";
+        if (flags & XR_DEVFLAG_QUEUE_OVERFLOW) m += " path queue overflow;";
+        if (flags & XR_DEVFLAG_BAD_INDEX) m += " material index out of range;";
+        return fail(c, XR_ERR_OVERFLOW, m);
+    }
+    return XR_OK;
+}
+
+xr_status validate_params(const Context* c, const XrParams* p) {
+    if (!p) return fail(c, XR_ERR_INVALID_ARGUMENT, "params: null");
+    if (p->width == 0 || p->height == 0 || p->width > 16384 || p->height > 16384)
+        return fail(c, XR_ERR_INVALID_ARGUMENT, "params: width/height must be in [1, 16384]");
+    if (!p->compat_reference) {
+        if (p->m_cap_temporal == 0 || p->m_cap_temporal > 255 || p->m_cap_spatial == 0 || p->m_cap_spatial > 255)
+            return fail(c, XR_ERR_INVALID_ARGUMENT, "params: M caps must be in [1, 255] (8-bit M in the 32 B reservoir)");
+        if (p->n_neighbours > 32) return fail(c, XR_ERR_INVALID_ARGUMENT, "params: n_neighbours must be <= 32");
+        if (!(p->radius_px >= 0.0f) || !(p->radius_px <= 4096.0f))
+            return fail(c, XR_ERR_INVALID_ARGUMENT, "params: radius_px must be in [0, 4096]");
+    }
+    return XR_OK;
+}
+
+}  // namespace
+}  // namespace xr
+
+using namespace xr;
+
+extern "C" {
+
+uint32_t xr_api_version(void) { return XR_API_VERSION; }
+
+const char* xr_last_error(const XrContext* ctx) {
+    if (ctx) return ctx->last_error.c_str();
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    t_err_copy = g_last_error;
+    return t_err_copy.c_str();
+}
+
+void xr_params_default(XrParams* p, uint32_t width, uint32_t height) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->width = width; p->height = height;
+    p->compat_reference = 0;
+    p->temporal_on = 1; p->spatial_on = 1;
+    p->m_cap_temporal = 20; p->m_cap_spatial = 120;
+    p->n_neighbours = 5; p->radius_px = 30.0f;
+    p->visibility = 1; p->seed = 1;
+}
+
+void xr_params_reference(XrParams* p, uint32_t width, uint32_t height) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->width = width; p->height = height;
+    p->compat_reference = 1;
+    p->temporal_on = 1; p->spatial_on = 1;
+    p->m_cap_temporal = 30; p->m_cap_spatial = 300;   // ReSTIRGITemporalReuse.rgen.hlsl:3, ReSTIRGISpatialReuse.rgen.hlsl:6
+    p->n_neighbours = 6; p->radius_px = 5.0f;         // ReSTIRGISpatialReuse.rgen.hlsl:4-5
+    p->visibility = 0; p->seed = 0;
+}
+
+xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
+    if (!desc || !out) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "create: null argument");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, XR_ERR_CUDA, std::string("create: no CUDA device (") + cudaGetErrorString(e) + ")");
+    if (desc->device < 0 || desc->device >= ndev) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "create: bad device ordinal");
+    XrContext* c = new XrContext();
+    c->device = desc->device;
+    DeviceGuard g(c->device);
+    xr_status s = XR_OK;
+    cudaDeviceProp prop;
+    if ((s = cuda_check(c, cudaGetDeviceProperties(&prop, c->device), "device properties"))) goto bad;
+    if (prop.major < 10) { s = fail(c, XR_ERR_UNSUPPORTED, "create: this library is built for sm_103a (GB300)"); goto bad; }
+    c->sm_count = prop.multiProcessorCount;
+    if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) goto bad;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_counters, 64 * 4), "counters"))) goto bad;
+    if ((s = cuda_check(c, cudaMemset(c->d_counters, 0, 64 * 4), "counters"))) goto bad;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_ubo, sizeof(XrUniformBufferObject)), "ubo"))) goto bad;
+    if ((s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, sizeof(XrUniformBufferObject)), "ubo staging"))) goto bad;
+    for (int i = 0; i < 6; i++)
+        if ((s = cuda_check(c, cudaEventCreate(&c->ev[i]), "event"))) goto bad;
+    for (int i = 0; i < 8; i++)
+        if ((s = cuda_check(c, cudaEventCreate(&c->user_ev[i]), "event"))) goto bad;
+    cudaEventRecord(c->ev[5], c->stream);
+    {
+        XrParams p;
+        xr_params_default(&p, desc->width ? desc->width : 1, desc->height ? desc->height : 1);
+        c->params = p;
+        if ((s = alloc_pixels(c))) goto bad;
+        c->params_set = desc->width != 0 && desc->height != 0;
+    }
+    *out = c;
+    return XR_OK;
+bad:
+    xr_destroy(c);
+    return s;
+}
+
+void xr_destroy(XrContext* c) {
+    if (!c) return;
+    DeviceGuard g(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_pixels(c);
+    cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
+    cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo);
+    if (c->h_ubo) cudaFreeHost(c->h_ubo);
+    for (int i = 0; i < 6; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const uint32_t* idx, uint32_t ni,
+                          const XrMaterial* m, uint32_t nm, const XrMeshRange* ranges, uint32_t nranges) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "upload: null context");
+    if ((nv && !v) || (ni && !idx) || (nm && !m) || (nranges && !ranges))
+        return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: null array with non-zero count");
+    if (ni % 3 != 0) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: index count must be a multiple of 3");
+    DeviceGuard g(c->device);
+    std::vector<XrMeshRange> rg;
+    if (nranges == 0) rg.push_back({0u, 0u});
+    else rg.assign(ranges, ranges + nranges);
+    const uint32_t ntri = ni / 3;
+    std::vector<uint4> tri(ntri);
+    for (size_t r = 0; r < rg.size(); r++) {
+        uint32_t b = rg[r].index_offset, e = (r + 1 < rg.size()) ? rg[r + 1].index_offset : ni;
+        if (b % 3 || e % 3 || b > e || e > ni) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: bad mesh range index offsets");
+        for (uint32_t i = b; i < e; i += 3) {
+            uint32_t g0 = rg[r].vertex_offset + idx[i], g1 = rg[r].vertex_offset + idx[i + 1], g2 = rg[r].vertex_offset + idx[i + 2];
+            if (g0 >= nv || g1 >= nv || g2 >= nv) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: vertex index out of range");
+            int32_t mi = v[g0].material_index;
+            if (mi < -1 || mi >= (int32_t)nm) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: material index out of range");
+            tri[i / 3] = make_uint4(g0, g1, g2, (uint32_t)mi);
+        }
+    }
+    bool non_lambert = false;
+    for (uint32_t i = 0; i < nm; i++) {
+        if (m[i].base_color_texture_index >= 0)
+            return fail(c, XR_ERR_UNSUPPORTED, "upload: base-colour textures are not supported by this build");
+        uint32_t mm = m[i].material_model;
+        if (mm != XR_MAT_LAMBERTIAN && mm != XR_MAT_DIFFUSE_LIGHT) non_lambert = true;
+        if (mm > XR_MAT_PLASTIC) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: unknown material model");
+    }
+    std::vector<float4> pos(nv), nrm(nv);
+    for (uint32_t i = 0; i < nv; i++) {
+        pos[i] = make_float4(v[i].pos[0], v[i].pos[1], v[i].pos[2], 0.0f);
+        nrm[i] = make_float4(v[i].normal[0], v[i].normal[1], v[i].normal[2], 0.0f);
+        if (!std::isfinite(v[i].pos[0]) || !std::isfinite(v[i].pos[1]) || !std::isfinite(v[i].pos[2]))
+            return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: non-finite vertex position");
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
+    c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr;
+    c->scene_ready = false; c->bvh_ready = false;
+    xr_status s;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_tri_idx, std::max<size_t>(ntri, 1) * 16), "scene alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_vpos, std::max<size_t>(nv, 1) * 16), "scene alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_vnrm, std::max<size_t>(nv, 1) * 16), "scene alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_mats, std::max<size_t>(nm, 1) * sizeof(XrMaterial)), "scene alloc")))
+        return s;
+    if (ntri) cudaMemcpy(c->d_tri_idx, tri.data(), (size_t)ntri * 16, cudaMemcpyHostToDevice);
+    if (nv) { cudaMemcpy(c->d_vpos, pos.data(), (size_t)nv * 16, cudaMemcpyHostToDevice);
+              cudaMemcpy(c->d_vnrm, nrm.data(), (size_t)nv * 16, cudaMemcpyHostToDevice); }
+    if (nm) cudaMemcpy(c->d_mats, m, (size_t)nm * sizeof(XrMaterial), cudaMemcpyHostToDevice);
+    if ((s = cuda_check(c, cudaGetLastError(), "scene upload"))) return s;
+    c->nv = nv; c->ntri = ntri; c->nm = nm;
+    c->scene_has_non_lambert = non_lambert;
+    c->scene_ready = true;
+    return XR_OK;
+}
+
+xr_status xr_build_bvh(XrContext* c) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "build_bvh: null context");
+    if (!c->scene_ready) return fail(c, XR_ERR_STATE, "build_bvh: upload a scene first");
+    DeviceGuard g(c->device);
+    xr_status s = build_bvh(c);
+    if (s) return s;
+    DeviceScene& sc = c->fa.sc;
+    sc.tri = c->d_tris; sc.nodes = c->d_nodes; sc.n_nodes = c->n_nodes;
+    sc.tri_idx = c->d_tri_idx; sc.vpos = c->d_vpos; sc.vnrm = c->d_vnrm;
+    sc.mats = c->d_mats; sc.n_mats = c->nm; sc.ntri = c->ntri;
+    return XR_OK;
+}
+
+xr_status xr_set_params(XrContext* c, const XrParams* p) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "set_params: null context");
+    xr_status s = validate_params(c, p);
+    if (s) return s;
+    DeviceGuard g(c->device);
+    const XrParams& o = c->params;
+    bool realloc = !c->pix_mem || o.width != p->width || o.height != p->height || o.compat_reference != p->compat_reference ||
+                   o.write_pt != p->write_pt || o.write_hdr != p->write_hdr;
+    c->params = *p;
+    c->params_set = true;
+    if (realloc) {
+        cudaStreamSynchronize(c->stream);
+        if ((s = alloc_pixels(c))) return s;
+    }
+    return XR_OK;
+}
+
+xr_status xr_get_params(XrContext* c, XrParams* p) {
+    if (!c || !p) return fail(c, XR_ERR_INVALID_ARGUMENT, "get_params: null argument");
+    *p = c->params;
+    return XR_OK;
+}
+
+xr_status xr_render_frame(XrContext* c, const XrUniformBufferObject* ubo) {
+    if (!c || !ubo) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_frame: null argument");
+    if (!c->params_set) return fail(c, XR_ERR_STATE, "render_frame: set the parameters (extent) first");
+    if (!c->bvh_ready) return fail(c, XR_ERR_STATE, "render_frame: build the BVH first");
+    if (ubo->number_of_bounces > 31) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_frame: number_of_bounces must be <= 31");
+    if (c->params.compat_reference && c->scene_has_non_lambert)
+        return fail(c, XR_ERR_UNSUPPORTED, "render_frame: reference mode renders only Lambertian and DiffuseLight materials");
+    DeviceGuard g(c->device);
+    xr_status s = upload_ubo(c, ubo);
+    if (s) return s;
+    set_frame_pointers(c, ubo->current_frame % 2u);
+    cudaMemsetAsync(c->d_counters, 0, 63 * 4, c->stream);   // keep the sticky error word [63]
+    const bool compat = c->params.compat_reference != 0;
+    cudaEventRecord(c->ev[0], c->stream);
+    launch_initial(c->fa, ubo->number_of_bounces, c->stream);
+    cudaEventRecord(c->ev[1], c->stream);
+    bool temporal_writes_image = compat ? (ubo->reuse == 0u) : (c->params.spatial_on == 0u);
+    launch_temporal(c->fa, temporal_writes_image, c->stream);
+    cudaEventRecord(c->ev[2], c->stream);
+    if (compat || c->params.spatial_on) launch_spatial(c->fa, c->stream);
+    cudaEventRecord(c->ev[3], c->stream);
+    c->frames++;
+    return cuda_check(c, cudaGetLastError(), "render_frame launch");
+}
+
+xr_status xr_sync(XrContext* c) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "sync: null context");
+    DeviceGuard g(c->device);
+    xr_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+    if (s) return s;
+    return check_flags(c);
+}
+
+static void* output_ptr(XrContext* c, uint32_t which, size_t* bytes) {
+    const size_t N = c->N;
+    switch (which) {
+        case XR_OUT_LDR8: *bytes = N * 4; return c->fa.out_ldr;
+        case XR_OUT_HDR: *bytes = N * 16; return c->fa.out_hdr;
+        case XR_OUT_PT: *bytes = N * 16; return c->fa.out_pt;
+        default: *bytes = 0; return nullptr;
+    }
+}
+
+xr_status xr_read_output(XrContext* c, uint32_t which, void* host, size_t bytes) {
+    if (!c || !host) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_output: null argument");
+    size_t need;
+    void* src = output_ptr(c, which, &need);
+    if (!src) return fail(c, XR_ERR_STATE, "read_output: that image is not enabled (write_hdr / write_pt)");
+    if (bytes < need) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_output: host buffer too small");
+    DeviceGuard g(c->device);
+    xr_status s = cuda_check(c, cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, c->stream), "read_output copy");
+    if (s) return s;
+    return xr_sync(c);
+}
+
+xr_status xr_output_device_ptr(XrContext* c, uint32_t which, void** dptr) {
+    if (!c || !dptr) return fail(c, XR_ERR_INVALID_ARGUMENT, "output_device_ptr: null argument");
+    size_t need;
+    *dptr = output_ptr(c, which, &need);
+    if (!*dptr) return fail(c, XR_ERR_STATE, "output_device_ptr: that image is not enabled");
+    return XR_OK;
+}
+
+xr_status xr_get_stats(XrContext* c, XrStats* st) {
+    if (!c || !st) return fail(c, XR_ERR_INVALID_ARGUMENT, "get_stats: null argument");
+    DeviceGuard g(c->device);
+    xr_status s = xr_sync(c);
+    XrStats o;
+    memset(&o, 0, sizeof(o));
+    o.frames = c->frames;
+    o.error_flags = c->error_flags;
+    if (c->frames) {
+        cudaEventElapsedTime(&o.ms_initial, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&o.ms_temporal, c->ev[1], c->ev[2]);
+        cudaEventElapsedTime(&o.ms_spatial, c->ev[2], c->ev[3]);
+        cudaEventElapsedTime(&o.ms_frame, c->ev[0], c->ev[3]);
+        uint32_t cnt[64];
+        cudaMemcpy(cnt, c->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost);
+        o.rays_traced = cnt[33];
+        o.shadow_rays = cnt[32];
+    }
+    o.bvh_nodes = c->n_nodes; o.bvh_triangles = c->n_tri_slots; o.bvh_depth = c->bvh_depth;
+    o.ms_bvh_build = c->ms_bvh;
+    *st = o;
+    return s;
+}
+
+xr_status xr_read_buffer(XrContext* c, uint32_t which, void* host, size_t bytes, size_t* bytes_out) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "read_buffer: null context");
+    const size_t N = c->N;
+    const bool compat = c->params.compat_reference != 0;
+    size_t need;
+    switch (which) {
+        case XR_BUF_SAMPLES: need = N * 96; break;
+        case XR_BUF_TEMPORAL: need = 2 * N * 112; break;
+        case XR_BUF_SPATIAL: need = (compat ? 2 * N : N) * 112; break;
+        default: return fail(c, XR_ERR_INVALID_ARGUMENT, "read_buffer: unknown buffer");
+    }
+    if (bytes_out) *bytes_out = need;
+    if (!host) return XR_OK;
+    if (bytes < need) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_buffer: host buffer too small");
+    DeviceGuard g(c->device);
+    uint32_t* tmp = nullptr;
+    xr_status s = cuda_check(c, cudaMalloc((void**)&tmp, need), "read_buffer alloc");
+    if (s) return s;
+    set_frame_pointers(c, c->fa.parity);
+    if (which == XR_BUF_SAMPLES) {
+        launch_export_samples(c->fa, tmp, c->stream);
+    } else if (compat) {
+        launch_export_res_wide(which == XR_BUF_TEMPORAL ? c->fa.rw : c->fa.rsw, (uint32_t)(2 * N), tmp, c->stream);
+    } else if (which == XR_BUF_TEMPORAL) {
+        launch_export_res_packed(c->rt0[0], c->rt1[0], (uint32_t)N, tmp, c->stream);
+        launch_export_res_packed(c->rt0[1], c->rt1[1], (uint32_t)N, tmp + 28 * N, c->stream);
+    } else {
+        launch_export_res_packed(c->fa.rs0, c->fa.rs1, (uint32_t)N, tmp, c->stream);
+    }
+    s = cuda_check(c, cudaMemcpyAsync(host, tmp, need, cudaMemcpyDeviceToHost, c->stream), "read_buffer copy");
+    if (!s) s = cuda_check(c, cudaStreamSynchronize(c->stream), "read_buffer sync");
+    cudaFree(tmp);
+    return s;
+}
+
+xr_status xr_write_buffer(XrContext* c, uint32_t which, const void* host, size_t bytes) {
+    if (!c || !host) return fail(c, XR_ERR_INVALID_ARGUMENT, "write_buffer: null argument");
+    const size_t N = c->N;
+    const bool compat = c->params.compat_reference != 0;
+    size_t need;
+    switch (which) {
+        case XR_BUF_SAMPLES: need = N * 96; break;
+        case XR_BUF_TEMPORAL: need = 2 * N * 112; break;
+        default: return fail(c, XR_ERR_INVALID_ARGUMENT, "write_buffer: only samples and temporal reservoirs can be written");
+    }
+    if (bytes != need) return fail(c, XR_ERR_INVALID_ARGUMENT, "write_buffer: size mismatch");
+    DeviceGuard g(c->device);
+    uint32_t* tmp = nullptr;
+    xr_status s = cuda_check(c, cudaMalloc((void**)&tmp, need), "write_buffer alloc");
+    if (s) return s;
+    s = cuda_check(c, cudaMemcpyAsync(tmp, host, need, cudaMemcpyHostToDevice, c->stream), "write_buffer copy");
+    if (!s) {
+        set_frame_pointers(c, c->fa.parity);
+        if (which == XR_BUF_SAMPLES) {
+            launch_import_samples(c->fa, tmp, c->stream);
+        } else if (compat) {
+            launch_import_res_wide(c->fa.rw, (uint32_t)(2 * N), tmp, c->stream);
+        } else {
+            launch_import_res_packed(c->rt0[0], c->rt1[0], (uint32_t)N, tmp, c->stream);
+            launch_import_res_packed(c->rt0[1], c->rt1[1], (uint32_t)N, tmp + 28 * N, c->stream);
+        }
+        s = cuda_check(c, cudaStreamSynchronize(c->stream), "write_buffer sync");
+    }
+    cudaFree(tmp);
+    return s;
+}
+
+xr_status xr_run_pass(XrContext* c, const XrUniformBufferObject* ubo, uint32_t pass) {
+    if (!c || !ubo) return fail(c, XR_ERR_INVALID_ARGUMENT, "run_pass: null argument");
+    if (pass != 1 && pass != 2) return fail(c, XR_ERR_INVALID_ARGUMENT, "run_pass: pass must be 1 (temporal) or 2 (spatial)");
+    if (!c->params_set || !c->bvh_ready) return fail(c, XR_ERR_STATE, "run_pass: parameters and BVH required");
+    DeviceGuard g(c->device);
+    xr_status s = upload_ubo(c, ubo);
+    if (s) return s;
+    set_frame_pointers(c, ubo->current_frame % 2u);
+    const bool compat = c->params.compat_reference != 0;
+    if (pass == 1) launch_temporal(c->fa, compat ? (ubo->reuse == 0u) : (c->params.spatial_on == 0u), c->stream);
+    else launch_spatial(c->fa, c->stream);
+    s = cuda_check(c, cudaGetLastError(), "run_pass launch");
+    if (s) return s;
+    return xr_sync(c);
+}
+
+xr_status xr_trace_rays_device(XrContext* c, const float* d_rays, uint32_t n, int32_t any_hit, int32_t* d_prim,
+                               float* d_t, float* d_bary) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "trace: null context");
+    if (!c->bvh_ready) return fail(c, XR_ERR_STATE, "trace: build the BVH first");
+    if (n && (!d_rays || !d_prim || !d_t || !d_bary)) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null array");
+    DeviceGuard g(c->device);
+    launch_trace(c->fa.sc, d_rays, n, any_hit, d_prim, d_t, d_bary, c->d_counters + 63, c->sm_count, c->stream);
+    return cuda_check(c, cudaGetLastError(), "trace launch");
+}
+
+xr_status xr_trace_rays(XrContext* c, const float* rays, uint32_t n, int32_t any_hit, int32_t* prim, float* t,
+                        float* bary) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "trace: null context");
+    if (n == 0) return XR_OK;
+    if (!rays || !prim || !t || !bary) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null array");
+    DeviceGuard g(c->device);
+    float* dr = nullptr; int32_t* dp = nullptr; float* dt = nullptr; float* db = nullptr;
+    xr_status s = XR_OK;
+    if ((s = cuda_check(c, cudaMalloc((void**)&dr, (size_t)n * 32), "trace alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&dp, (size_t)n * 4), "trace alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&dt, (size_t)n * 4), "trace alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&db, (size_t)n * 8), "trace alloc")))
+        goto out;
+    cudaMemcpyAsync(dr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream);
+    if ((s = xr_trace_rays_device(c, dr, n, any_hit, dp, dt, db))) goto out;
+    cudaMemcpyAsync(prim, dp, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(t, dt, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(bary, db, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream);
+    s = xr_sync(c);
+out:
+    cudaFree(dr); cudaFree(dp); cudaFree(dt); cudaFree(db);
+    return s;
+}
+
+xr_status xr_event_record(XrContext* c, uint32_t slot) {
+    if (!c || slot >= 8) return fail(c, XR_ERR_INVALID_ARGUMENT, "event_record: bad argument");
+    DeviceGuard g(c->device);
+    return cuda_check(c, cudaEventRecord(c->user_ev[slot], c->stream), "event_record");
+}
+
+xr_status xr_event_elapsed(XrContext* c, uint32_t a, uint32_t b, float* ms) {
+    if (!c || a >= 8 || b >= 8 || !ms) return fail(c, XR_ERR_INVALID_ARGUMENT, "event_elapsed: bad argument");
+    DeviceGuard g(c->device);
+    xr_status s = cuda_check(c, cudaEventSynchronize(c->user_ev[b]), "event_elapsed sync");
+    if (s) return s;
+    return cuda_check(c, cudaEventElapsedTime(ms, c->user_ev[a], c->user_ev[b]), "event_elapsed");
+}
+
+xr_status xr_alloc_host(size_t bytes, void** ptr) {
+    if (!ptr) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "alloc_host: null argument");
+    return cuda_check(nullptr, cudaMallocHost(ptr, bytes), "cudaMallocHost");
+}
+
+void xr_free_host(void* ptr) {
+    if (ptr) cudaFreeHost(ptr);
+}
+
+}  // extern "C"

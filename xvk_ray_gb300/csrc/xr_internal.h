@@ -1,0 +1,162 @@
+// xr_internal.h -- context, device data layout and launch wrappers of libxr.so.
+//
+// Device layout (structure of arrays, every per-pixel access one 128-bit or
+// 64-bit load/store):
+//   corrected mode ("packed"):
+//     gb_pos[2]  float4 {x_view.xyz, oct16(n_view)}      ping-pong by frame parity
+//     gb_mat[2]  u32 material id of the visible point (0xFFFFFFFF = invalid)
+//     cand_a     float4 {x_sample.xyz, p_q}
+//     cand_b     float4 {L_out.rgb, oct12(n_sample) | has_sample << 31}
+//                (for invalid pixels .rgb holds the directly seen emission)
+//     res_t[2]   2 planes float4: {x_s.xyz, W}, {L.rgb, oct12(n_s) | M << 24}  (32 B/pixel)
+//     res_s      same, single buffer
+//   compat mode ("wide", the reference's fields at full precision):
+//     s_xv {x_view, matID} s_nv {n_view, randSeed} s_xs {x_sample, p_q}
+//     s_ns {n_sample, 0}   s_L {L_out, 0}
+//     res_t / res_s: 4 planes {x_s, W} {L, w_sum} {n_s, m} {f, 0}, 2N entries each
+//   path queues (wavefront): 3 float4 per path {o, pixel} {d, rng} {throughput, p_q}
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <string>
+
+#include "../../include/xr.h"
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#else
+#include <cuda_runtime_api.h>
+#endif
+
+namespace xr {
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr int kStackSize = 40;
+
+// 8-wide compressed BVH node, 80 B (five 16-byte words).
+//  w0: origin p.xyz, byte-packed {e.x, e.y, e.z (biased by 127), internal mask}
+//  w1: child_base, tri_base, meta[0..3], meta[4..7]
+//  w2..w4: q_lo.x[8], q_lo.y[8], q_lo.z[8], q_hi.x[8], q_hi.y[8], q_hi.z[8]
+// meta: 0 empty, 0x80 internal child, (count << 5) | offset for a leaf of 1..3
+// triangles at tri_base + offset.  Internal child in slot s is node
+// child_base + popc(imask & ((1 << s) - 1)).
+struct alignas(16) WideNode {
+    float px, py, pz;
+    uint32_t exyz_imask;
+    uint32_t child_base, tri_base;
+    uint32_t meta[2];
+    uint32_t q[12];
+};
+static_assert(sizeof(WideNode) == 80, "wide node is 80 B");
+
+struct DeviceScene {
+    const float4* tri;        // 3 float4 per BVH triangle slot: v0 {xyz, prim id}, v1, v2
+    const WideNode* nodes;
+    uint32_t n_nodes;
+    const uint4* tri_idx;     // per primitive {i0, i1, i2, material of v0}
+    const float4* vpos;       // per vertex {pos, 0}
+    const float4* vnrm;       // per vertex {normal, 0}
+    const XrMaterial* mats;
+    uint32_t n_mats;
+    uint32_t ntri;
+};
+
+struct FrameArgs {
+    DeviceScene sc;
+    const XrUniformBufferObject* ubo;   // device copy of this frame's UBO
+    uint32_t W, H, N;
+    uint32_t compat, temporal_on, spatial_on, visibility, write_pt, seed;
+    uint32_t m_cap_t, m_cap_s, n_nb;
+    float radius;
+    uint32_t parity;                    // current_frame % 2 (host copy for pointer selection)
+    // corrected layout
+    float4* gb_pos_cur; const float4* gb_pos_prev;
+    uint32_t* gb_mat_cur; const uint32_t* gb_mat_prev;
+    float4* cand_a; float4* cand_b;
+    float4* rt_cur0; float4* rt_cur1; const float4* rt_prev0; const float4* rt_prev1;
+    float4* rs0; float4* rs1;
+    // compat layout
+    float4* s_xv; float4* s_nv; float4* s_xs; float4* s_ns; float4* s_L;
+    float4* rw[4];            // temporal reservoirs, 2N entries per plane
+    float4* rsw[4];           // spatial reservoirs, 2N entries per plane
+    // shared
+    float4* thr0;             // bounce-0 throughput (write_pt)
+    float4* le0;              // directly seen emission (write_pt, compat)
+    uchar4* out_ldr; float4* out_hdr; float4* out_pt;
+    // wavefront
+    float4* q_in[3]; float4* q_out[3];
+    uint32_t* counters;       // [0..7] queue counts, [8] shadow rays, [9] rays, [15] error flags
+    uint32_t grid_persistent;
+};
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    XrParams params{};
+    bool params_set = false;
+    std::string last_error;
+
+    // scene
+    uint32_t nv = 0, ntri = 0, nm = 0;
+    uint4* d_tri_idx = nullptr;
+    float4* d_vpos = nullptr;
+    float4* d_vnrm = nullptr;
+    XrMaterial* d_mats = nullptr;
+    bool scene_ready = false;
+    bool scene_has_non_lambert = false;
+
+    // BVH
+    WideNode* d_nodes = nullptr;
+    float4* d_tris = nullptr;
+    uint32_t n_nodes = 0, n_tri_slots = 0, bvh_depth = 0;
+    bool bvh_ready = false;
+    float ms_bvh = 0.0f;
+
+    // per-pixel buffers
+    uint32_t W = 0, H = 0, N = 0;
+    void* pix_mem = nullptr;       // one allocation for all per-pixel buffers
+    size_t pix_bytes = 0;
+    FrameArgs fa{};                // pointers of the current allocation
+    float4* gb_pos[2] = {nullptr, nullptr};
+    uint32_t* gb_mat[2] = {nullptr, nullptr};
+    float4* rt0[2] = {nullptr, nullptr};
+    float4* rt1[2] = {nullptr, nullptr};
+    float4* q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    uint32_t* d_counters = nullptr;
+    XrUniformBufferObject* d_ubo = nullptr;
+    XrUniformBufferObject* h_ubo = nullptr;   // pinned staging
+
+    // statistics
+    uint32_t frames = 0;
+    uint32_t error_flags = 0;
+    cudaEvent_t ev[6] = {};
+    cudaEvent_t user_ev[8] = {};
+    XrStats stats{};
+};
+
+xr_status fail(const Context* ctx, xr_status code, const std::string& msg);
+xr_status cuda_check(Context* ctx, cudaError_t e, const char* what);
+
+// ---- launch wrappers (bvh_build.cu) ----
+xr_status build_bvh(Context* ctx);
+
+// ---- launch wrappers (trace.cu) ----
+void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_hit, int32_t* prim, float* t,
+                  float* bary, uint32_t* flags, int sm_count, cudaStream_t st);
+
+// ---- launch wrappers (restir.cu) ----
+void launch_initial(const FrameArgs& fa, uint32_t number_of_bounces, cudaStream_t st);
+void launch_temporal(const FrameArgs& fa, bool write_image, cudaStream_t st);
+void launch_spatial(const FrameArgs& fa, cudaStream_t st);
+void launch_export_samples(const FrameArgs& fa, uint32_t* out, cudaStream_t st);
+void launch_import_samples(const FrameArgs& fa, const uint32_t* in, cudaStream_t st);
+void launch_export_res_wide(float4* const planes[4], uint32_t n, uint32_t* out, cudaStream_t st);
+void launch_export_res_packed(const float4* p0, const float4* p1, uint32_t n, uint32_t* out, cudaStream_t st);
+void launch_import_res_wide(float4* const planes[4], uint32_t n, const uint32_t* in, cudaStream_t st);
+void launch_import_res_packed(float4* p0, float4* p1, uint32_t n, const uint32_t* in, cudaStream_t st);
+
+}  // namespace xr
+
+struct XrContext : public xr::Context {};
