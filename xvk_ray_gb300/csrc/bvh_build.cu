@@ -228,7 +228,9 @@ __global__ void k_bounds(int n, const uint32_t* __restrict__ left, const uint32_
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     uint32_t node = parent_leaf[j];
-    while (node != kInvalid) {
+    // the radix tree of 64-bit keys split by 32-bit index is at most 96 levels deep
+    for (int guard = 0; node != kInvalid; guard++) {
+        if (guard > 128 || node >= (uint32_t)(n - 1)) { atomicOr(&flags[n - 1], 1u); return; }
         __threadfence();
         if (atomicAdd(&flags[node], 1u) == 0u) return;
         __threadfence();
@@ -251,6 +253,7 @@ struct CollapseArgs {
     uint32_t* counters;               // [0] wide nodes, [1] tri slots, [2] next task count
     WideNode* nodes; float4* tris;
     int emin;                         // smallest exponent of the quantisation grid
+    uint32_t max_nodes, n_prims;      // allocation bounds
 };
 
 __device__ __forceinline__ uint32_t ref_count(uint32_t ref, const uint2* range) {
@@ -340,6 +343,10 @@ __global__ void k_collapse(CollapseArgs a) {
     }
     uint32_t child_base = n_int ? atomicAdd(&a.counters[0], n_int) : 0u;
     uint32_t tri_base = n_tris ? atomicAdd(&a.counters[1], n_tris) : 0u;
+    if (child_base + n_int > a.max_nodes || tri_base + n_tris > a.n_prims) {
+        atomicOr(&a.counters[3], 1u);   // inconsistent tree: reported by the host, nothing written
+        return;
+    }
     // quantisation grid: p = lo - one cell, cells of 2^e with extent / 2^e <= 250
     WideNode nd;
     int e[3];
@@ -440,7 +447,7 @@ xr_status build_bvh(Context* ctx) {
         (s = dalloc(ctx, &k1, n)) || (s = dalloc(ctx, &v0, n)) || (s = dalloc(ctx, &v1, n)) ||
         (s = dalloc(ctx, &bounds, 8)) || (s = dalloc(ctx, &hist, 256 * nblk)) || (s = dalloc(ctx, &left, nint)) ||
         (s = dalloc(ctx, &right, nint)) || (s = dalloc(ctx, &pint, nint)) || (s = dalloc(ctx, &pleaf, n)) ||
-        (s = dalloc(ctx, &flags, nint)) || (s = dalloc(ctx, &range, nint)) || (s = dalloc(ctx, &nlo, nint)) ||
+        (s = dalloc(ctx, &flags, nint + 1)) || (s = dalloc(ctx, &range, nint)) || (s = dalloc(ctx, &nlo, nint)) ||
         (s = dalloc(ctx, &nhi, nint)) || (s = dalloc(ctx, &ta, n)) || (s = dalloc(ctx, &tb, n)) ||
         (s = dalloc(ctx, &wa, n)) || (s = dalloc(ctx, &wb, n)) || (s = dalloc(ctx, &counters, 4)) ||
         (s = dalloc(ctx, &nodes_tmp, nint)) || (s = dalloc(ctx, &ctx->d_tris, 3 * (size_t)n)))
@@ -469,7 +476,7 @@ xr_status build_bvh(Context* ctx) {
         emin -= 17;   // cells of at least 2^-17 of the largest coordinate
         cudaMemsetAsync(pint, 0xFF, nint * 4, st);
         cudaMemsetAsync(pleaf, 0xFF, (size_t)n * 4, st);
-        cudaMemsetAsync(flags, 0, nint * 4, st);
+        cudaMemsetAsync(flags, 0, (nint + 1) * 4, st);
         uint32_t root_ref = 0u;
         if (n > 1) {
             k_karras<<<(n - 1 + 255) / 256, 256, 0, st>>>(k0, (int)n, left, right, pint, pleaf, range);
@@ -489,6 +496,7 @@ xr_status build_bvh(Context* ctx) {
             ca.sorted = v0; ca.tri_idx = ctx->d_tri_idx; ca.vpos = ctx->d_vpos;
             ca.task_in = ta; ca.task_wide_in = wa; ca.n_tasks = ntask; ca.task_out = tb; ca.task_wide_out = wb;
             ca.counters = counters; ca.nodes = nodes_tmp; ca.tris = ctx->d_tris; ca.emin = emin;
+            ca.max_nodes = nint; ca.n_prims = n;
             cudaMemsetAsync(counters + 2, 0, 4, st);
             k_collapse<<<(ntask + 127) / 128, 128, 0, st>>>(ca);
             cudaMemcpyAsync(&ntask, counters + 2, 4, cudaMemcpyDeviceToHost, st);
@@ -498,8 +506,10 @@ xr_status build_bvh(Context* ctx) {
             depth++;
             if (depth > 200) { s = fail(ctx, XR_ERR_OVERFLOW, "bvh: collapse did not terminate"); goto done; }
         }
-        uint32_t ch[4];
+        uint32_t ch[4], bflag = 0;
         cudaMemcpy(ch, counters, sizeof(ch), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&bflag, flags + nint, 4, cudaMemcpyDeviceToHost);
+        if (ch[3] || bflag) { s = fail(ctx, XR_ERR_STATE, "bvh: inconsistent radix tree"); goto done; }
         if (ch[1] != n) { s = fail(ctx, XR_ERR_STATE, "bvh: triangle slots do not match the primitive count"); goto done; }
         if ((s = dalloc(ctx, &ctx->d_nodes, ch[0]))) goto done;
         cudaMemcpyAsync(ctx->d_nodes, nodes_tmp, (size_t)ch[0] * sizeof(WideNode), cudaMemcpyDeviceToDevice, st);

@@ -349,6 +349,7 @@ __device__ __forceinline__ void write_out(const FrameArgs& fa, uint32_t p, float
 }
 
 __device__ __forceinline__ float3 mat_albedo_over_pi(const FrameArgs& fa, uint32_t m) {
+    if (m >= fa.sc.n_mats) return f3(0.0f, 0.0f, 0.0f);
     const XrMaterial& mm = fa.sc.mats[m];
     return f3(mm.base_color[0], mm.base_color[1], mm.base_color[2]) * XR_INV_PI_F;
 }
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(256) k_spatial_compat(FrameArgs fa, const XrUn
 __device__ __forceinline__ float3 shade_corrected(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
                                                   const Res& r, float3 x_view, float3 n_view, uint32_t mat) {
     float3 c = f3(0, 0, 0);
-    if (r.W > 0.0f) {
+    if (r.W > 0.0f && mat < fa.sc.n_mats) {
         float3 wi = normalize(r.xs - x_view);
         float ct = fmaxf(0.0f, dot(n_view, wi));
         float3 cam = xyz(mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));

@@ -96,7 +96,8 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t w0, uint32_t w1, uint32_t i
 }
 
 // One ray through the wide BVH.  ANY: stop at the first accepted hit.
-// Returns false when the traversal stack would overflow (the caller flags it).
+// Returns false when the traversal stack would overflow or the tree is malformed
+// (the caller flags it).
 template <bool ANY>
 __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 o, float3 d, float tmin, float tmax,
                                          HitRec& h) {
@@ -112,10 +113,15 @@ __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 o, float3
     int sp = 0;
     uint32_t node = 0;
     bool ok = true;
+    // a well-formed tree visits each node at most once; the limit only stops a
+    // corrupted one from looping
+    uint32_t visits_left = sc.n_nodes;
     // group = children of the last visited node still to visit
     uint32_t g_base = 0, g_hits = 0, g_imask = 0;
     while (true) {
         // ---- visit `node`: test its 8 child boxes, then its leaf triangles ----
+        if (node >= sc.n_nodes || visits_left == 0u) { ok = false; break; }
+        visits_left--;
         {
             const uint4* np = reinterpret_cast<const uint4*>(sc.nodes + node);
             uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
@@ -153,6 +159,7 @@ __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 o, float3
             while (trimask) {
                 uint32_t bit = __ffs(trimask) - 1u;
                 trimask &= trimask - 1u;
+                if (tri_base + bit >= sc.ntri) { ok = false; continue; }
                 const float4* tp = sc.tri + 3u * (tri_base + bit);
                 float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 int32_t prim = (int32_t)__float_as_uint(a.w);
