@@ -194,6 +194,17 @@ xr_status xr_trace_rays(XrContext* ctx, const float* rays, uint32_t n, int32_t a
 /* Same on device pointers, asynchronous on the context stream. */
 xr_status xr_trace_rays_device(XrContext* ctx, const float* d_rays, uint32_t n, int32_t any_hit,
                                int32_t* d_prim, float* d_t, float* d_bary);
+/* No counterpart in the reference.  xr_trace_rays for callers that cannot
+   allocate device memory where they query rays (an engine that owns all device
+   memory through its own allocator, a real-time loop where allocation's implicit
+   synchronisation is not allowed): the staging lives in one fixed device array
+   of this library (65536 rays, about 3 MiB, held on each GPU until exit), so at
+   most 65536 rays per call; larger batches fail with XR_ERR_INVALID_ARGUMENT.
+   Allocates nothing.  The first call on a device looks the array's address up
+   and should come before any stream capture.  Calls share the array: calls that
+   overlap on the GPU race, so serialise them.  Same results as xr_trace_rays. */
+xr_status xr_trace_rays_noalloc(XrContext* ctx, const float* rays, uint32_t n, int32_t any_hit,
+                                int32_t* prim, float* t, float* bary);
 
 /* ---- host helpers (no GPU work) ---- */
 /* Camera for one frame: replaces PathTracer::GetUniformBufferObject

@@ -121,6 +121,7 @@ _SIGS = {
     "xr_run_pass": (_i32, [_P, C.POINTER(XrUniformBufferObject), _u32]),
     "xr_trace_rays": (_i32, [_P, _P, _u32, _i32, _P, _P, _P]),
     "xr_trace_rays_device": (_i32, [_P, _P, _u32, _i32, _P, _P, _P]),
+    "xr_trace_rays_noalloc": (_i32, [_P, _P, _u32, _i32, _P, _P, _P]),
     "xr_camera_ubo": (_i32, [C.POINTER(XrCamera), _u32, _u32, C.POINTER(XrUniformBufferObject), _u32, _u32, _u32,
                              _u32, C.POINTER(XrUniformBufferObject)]),
     "xr_scene_cornell": (_i32, [C.POINTER(XrSceneData)]),
