@@ -33,7 +33,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-W, H = 1920, 1080
+W, H = 1920, 1080          # overridden by --width/--height (profiling of smaller cases)
 BOUNCES = 4
 SCENE_KW = dict(seed=1, n_objects=4096, n_lights=16, extent=40.0, sphere_subdiv=2)
 METRIC = "ms/frame 1080p & relMSE vs FP64 ref: plain ReSTIR GI vs ReSTIR GI+MLP cache"
@@ -319,7 +319,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--width", type=int, default=1920, help="smaller extents are for profiling only")
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--objects", type=int, default=4096, help="scene objects (4096 -> 998,442 triangles)")
     args = ap.parse_args()
+    global W, H
+    W, H = args.width, args.height
+    SCENE_KW["n_objects"] = args.objects
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

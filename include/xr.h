@@ -125,6 +125,9 @@ typedef struct XrStats {
     uint64_t shadow_rays;        /* any-hit rays of the last frame */
     uint32_t bvh_nodes, bvh_triangles, bvh_depth;
     float ms_bvh_build;
+    uint64_t query_rays;         /* rays of the last xr_trace_rays call */
+    uint64_t query_node_visits;  /* BVH nodes visited by those rays */
+    uint64_t query_tri_tests;    /* triangle tests of those rays */
 } XrStats;
 enum { XR_DEVFLAG_STACK_OVERFLOW = 1u, XR_DEVFLAG_QUEUE_OVERFLOW = 2u, XR_DEVFLAG_BAD_INDEX = 4u };
 

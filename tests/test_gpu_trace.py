@@ -68,8 +68,10 @@ def test_axis_aligned_and_edge_rays():
     assert np.array_equal(gt[op >= 0].view(np.uint32), ot[op >= 0].view(np.uint32))
 
 
+@pytest.mark.parametrize("builder", ["ploc", "lbvh"])
 @pytest.mark.parametrize("n_objects", [64, 2048])
-def test_procedural_hits_bit_exact(n_objects):
+def test_procedural_hits_bit_exact(n_objects, builder, monkeypatch):
+    monkeypatch.setenv("XR_BVH_BUILDER", builder)
     scene = xr.Scene.procedural(seed=5, n_objects=n_objects, extent=10.0)
     rng = np.random.default_rng(11)
     rays = random_rays(rng, 100000, [-12, 0.0, -12], [12, 4.0, 12])

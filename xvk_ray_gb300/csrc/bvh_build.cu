@@ -16,6 +16,8 @@
 //      become leaves, slots are assigned by octant of the child centre so that a
 //      ray visits near children first, boxes are quantised to 8 bits.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "device_math.cuh"
@@ -183,7 +185,8 @@ __device__ __forceinline__ int delta(const uint64_t* keys, int n, int i, int j) 
 }
 
 __global__ void k_karras(const uint64_t* __restrict__ keys, int n, uint32_t* __restrict__ left, uint32_t* __restrict__ right,
-                         uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf, uint2* __restrict__ range) {
+                         uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf,
+                         uint32_t* __restrict__ count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -206,7 +209,7 @@ __global__ void k_karras(const uint64_t* __restrict__ keys, int n, uint32_t* __r
     uint32_t rc = (hi == gamma + 1) ? ((uint32_t)(gamma + 1) | kLeafBit) : (uint32_t)(gamma + 1);
     left[i] = lc;
     right[i] = rc;
-    range[i] = make_uint2((uint32_t)lo, (uint32_t)hi);
+    count[i] = (uint32_t)(hi - lo + 1);
     if (lc & kLeafBit) parent_leaf[lc & ~kLeafBit] = (uint32_t)i; else parent_int[lc] = (uint32_t)i;
     if (rc & kLeafBit) parent_leaf[rc & ~kLeafBit] = (uint32_t)i; else parent_int[rc] = (uint32_t)i;
 }
@@ -244,7 +247,7 @@ __global__ void k_bounds(int n, const uint32_t* __restrict__ left, const uint32_
 }
 
 struct CollapseArgs {
-    const uint32_t* left; const uint32_t* right; const uint2* range;
+    const uint32_t* left; const uint32_t* right; const uint32_t* count;   // binary tree, primitives per node
     const float4* nlo; const float4* nhi; const float4* tlo; const float4* thi;
     const uint32_t* sorted;           // sorted primitive ids
     const uint4* tri_idx; const float4* vpos;
@@ -256,10 +259,8 @@ struct CollapseArgs {
     uint32_t max_nodes, n_prims;      // allocation bounds
 };
 
-__device__ __forceinline__ uint32_t ref_count(uint32_t ref, const uint2* range) {
-    if (ref & kLeafBit) return 1u;
-    uint2 r = range[ref];
-    return r.y - r.x + 1u;
+__device__ __forceinline__ uint32_t ref_count(uint32_t ref, const uint32_t* count) {
+    return (ref & kLeafBit) ? 1u : count[ref];
 }
 __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
     float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
@@ -290,7 +291,7 @@ __global__ void k_collapse(CollapseArgs a) {
                 for (int c = 0; c < nc; c++) {
                     uint32_t r = refs[c];
                     if (r & kLeafBit) continue;
-                    uint32_t cnt = ref_count(r, a.range);
+                    uint32_t cnt = ref_count(r, a.count);
                     if (phase == 0 ? cnt <= 3u : cnt > 3u) continue;
                     float ar = half_area(a.nlo[r], a.nhi[r]);
                     if (ar > best_area) { best_area = ar; best = c; }
@@ -336,7 +337,7 @@ __global__ void k_collapse(CollapseArgs a) {
     uint32_t imask = 0, n_int = 0, n_tris = 0;
     uint32_t cnt_of[8];
     for (int c = 0; c < nc; c++) {
-        uint32_t cnt = ref_count(refs[c], a.range);
+        uint32_t cnt = ref_count(refs[c], a.count);
         cnt_of[c] = cnt;
         if (!(refs[c] & kLeafBit) && cnt > 3u) { imask |= 1u << slot_of[c]; n_int++; }
         else n_tris += cnt;
@@ -387,11 +388,24 @@ __global__ void k_collapse(CollapseArgs a) {
             a.task_out[slot] = r;
             a.task_wide_out[slot] = child_base + rank;
         } else {
-            uint32_t first = (r & kLeafBit) ? (r & ~kLeafBit) : a.range[r].x;
+            // the (at most 3) primitives of the subtree, left to right
+            uint32_t prims[3], np = 0, dfs[4], dsp = 0;
+            dfs[dsp++] = r;
+            while (dsp) {
+                uint32_t x = dfs[--dsp];
+                if (x & kLeafBit) {
+                    if (np < 3u) prims[np] = a.sorted[x & ~kLeafBit];
+                    np++;
+                } else if (dsp + 2u <= 4u) {
+                    dfs[dsp++] = a.right[x];
+                    dfs[dsp++] = a.left[x];
+                }
+            }
             uint32_t cnt = cnt_of[c];
+            if (np != cnt) { atomicOr(&a.counters[3], 2u); cnt = min(np, 3u); }
             meta[s] = (uint8_t)((cnt << 5) | off);
             for (uint32_t j = 0; j < cnt; j++) {
-                uint32_t prim = a.sorted[first + j];
+                uint32_t prim = prims[j];
                 uint4 id = a.tri_idx[prim];
                 float4 v0 = a.vpos[id.x], v1 = a.vpos[id.y], v2 = a.vpos[id.z];
                 float4* dst = a.tris + 3u * (tri_base + off + j);
@@ -411,6 +425,136 @@ __global__ void k_collapse(CollapseArgs a) {
     pack(ql[0], &nd.q[0]); pack(ql[1], &nd.q[2]); pack(ql[2], &nd.q[4]);
     pack(qh[0], &nd.q[6]); pack(qh[1], &nd.q[8]); pack(qh[2], &nd.q[10]);
     a.nodes[widx] = nd;
+}
+
+// ---- PLOC: Meister and Bittner, "Parallel Locally-Ordered Clustering for
+// Bounding Volume Hierarchy Construction" (TVCG 2018).  Clusters stay in
+// Morton order; each finds the cluster within +-kPlocRadius positions whose
+// merged box has the smallest surface area (ties by the pair's indices, so the
+// globally best pair is always mutual and every round merges), mutual pairs
+// merge into a new internal node at the lower position, the array is
+// compacted, and rounds repeat until one cluster is left.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+
+__global__ void k_ploc_init(uint32_t n, const uint32_t* __restrict__ sorted, const float4* __restrict__ tlo,
+                            const float4* __restrict__ thi, uint32_t* __restrict__ cref, float4* __restrict__ clo,
+                            float4* __restrict__ chi) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t p = sorted[i];
+    cref[i] = i | kLeafBit;
+    clo[i] = tlo[p];
+    chi[i] = thi[p];
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(uint32_t n, const float4* __restrict__ clo,
+                                                        const float4* __restrict__ chi, uint32_t* __restrict__ nn) {
+    __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+    const int base = (int)(blockIdx.x * kPlocBlock) - kPlocRadius;
+    for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += kPlocBlock) {
+        int j = base + k;
+        if (j >= 0 && j < (int)n) { slo[k] = clo[j]; shi[k] = chi[j]; }
+    }
+    __syncthreads();
+    const int i = (int)(blockIdx.x * kPlocBlock + threadIdx.x);
+    if (i >= (int)n) return;
+    const float4 alo = slo[threadIdx.x + kPlocRadius], ahi = shi[threadIdx.x + kPlocRadius];
+    float best = INFINITY;
+    int bj = -1;
+    for (int o = -kPlocRadius; o <= kPlocRadius; o++) {
+        int j = i + o;
+        if (o == 0 || j < 0 || j >= (int)n) continue;
+        float4 blo = slo[threadIdx.x + kPlocRadius + o], bhi = shi[threadIdx.x + kPlocRadius + o];
+        float dx = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);
+        float dy = fmaxf(ahi.y, bhi.y) - fminf(alo.y, blo.y);
+        float dz = fmaxf(ahi.z, bhi.z) - fminf(alo.z, blo.z);
+        float a = dx * dy + dy * dz + dz * dx;
+        // total order on pairs: area, then the pair's lower index, then its upper index
+        bool better = a < best;
+        if (a == best && bj >= 0) {
+            int lo_new = min(i, j), hi_new = max(i, j), lo_old = min(i, bj), hi_old = max(i, bj);
+            better = lo_new < lo_old || (lo_new == lo_old && hi_new < hi_old);
+        }
+        if (better) { best = a; bj = j; }
+    }
+    nn[i] = bj < 0 ? (uint32_t)i : (uint32_t)bj;
+}
+
+__global__ void k_ploc_merge(uint32_t n, const uint32_t* __restrict__ nn, const uint32_t* __restrict__ cref,
+                             const float4* __restrict__ clo, const float4* __restrict__ chi, uint32_t* __restrict__ tref,
+                             float4* __restrict__ tlo, float4* __restrict__ thi, uint32_t* __restrict__ keep,
+                             uint32_t* __restrict__ left, uint32_t* __restrict__ right, uint32_t* __restrict__ count,
+                             float4* __restrict__ nlo, float4* __restrict__ nhi, uint32_t* node_counter, uint32_t max_nodes) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = nn[i];
+    const bool mutual = j != i && nn[j] == i;
+    if (mutual && i > j) { keep[i] = 0u; return; }   // merged into position j
+    keep[i] = 1u;
+    if (!mutual) { tref[i] = cref[i]; tlo[i] = clo[i]; thi[i] = chi[i]; return; }
+    const uint32_t k = atomicAdd(node_counter, 1u);
+    const float4 al = clo[i], ah = chi[i], bl = clo[j], bh = chi[j];
+    const float4 ml = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.0f);
+    const float4 mh = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f);
+    const uint32_t ra = cref[i], rb = cref[j];
+    if (k < max_nodes) {
+        left[k] = ra;
+        right[k] = rb;
+        count[k] = ((ra & kLeafBit) ? 1u : count[ra]) + ((rb & kLeafBit) ? 1u : count[rb]);
+        nlo[k] = ml;
+        nhi[k] = mh;
+    }
+    tref[i] = k;
+    tlo[i] = ml;
+    thi[i] = mh;
+}
+
+// exclusive scan of keep[] in blocks of 1024 (block sums to `sums`)
+__global__ void __launch_bounds__(1024) k_scan_local(const uint32_t* __restrict__ in, uint32_t n,
+                                                     uint32_t* __restrict__ out, uint32_t* __restrict__ sums) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t i = blockIdx.x * 1024u + threadIdx.x, lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t v = i < n ? in[i] : 0u;
+    uint32_t x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+        if ((int)lane >= off) x += y;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = warp_sums[lane];
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, off);
+            if ((int)lane >= off) s += y;
+        }
+        warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t before = (w ? warp_sums[w - 1] : 0u) + x - v;
+    if (i < n) out[i] = before;
+    if (threadIdx.x == 1023) sums[blockIdx.x] = warp_sums[31];
+}
+
+// exclusive scan of the block sums (one block); sums[nb] receives the total
+__global__ void k_scan_top(uint32_t* sums, uint32_t nb) {
+    if (threadIdx.x != 0) return;
+    uint32_t acc = 0;
+    for (uint32_t b = 0; b < nb; b++) { uint32_t v = sums[b]; sums[b] = acc; acc += v; }
+    sums[nb] = acc;
+}
+
+__global__ void k_ploc_compact(uint32_t n, const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos,
+                               const uint32_t* __restrict__ sums, const uint32_t* __restrict__ tref,
+                               const float4* __restrict__ tlo, const float4* __restrict__ thi,
+                               uint32_t* __restrict__ cref, float4* __restrict__ clo, float4* __restrict__ chi) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !keep[i]) return;
+    uint32_t d = pos[i] + sums[i / 1024u];
+    cref[d] = tref[i];
+    clo[d] = tlo[i];
+    chi[d] = thi[i];
 }
 
 template <typename T>
@@ -436,7 +580,7 @@ xr_status build_bvh(Context* ctx) {
     uint64_t *k0 = nullptr, *k1 = nullptr;
     uint32_t *v0 = nullptr, *v1 = nullptr, *bounds = nullptr, *hist = nullptr;
     uint32_t *left = nullptr, *right = nullptr, *pint = nullptr, *pleaf = nullptr, *flags = nullptr;
-    uint2* range = nullptr;
+    uint32_t* range = nullptr;   // primitives below each binary internal node
     uint32_t *ta = nullptr, *tb = nullptr, *wa = nullptr, *wb = nullptr, *counters = nullptr;
     WideNode* nodes_tmp = nullptr;
     xr_status s = XR_OK;
@@ -478,11 +622,52 @@ xr_status build_bvh(Context* ctx) {
         cudaMemsetAsync(pleaf, 0xFF, (size_t)n * 4, st);
         cudaMemsetAsync(flags, 0, (nint + 1) * 4, st);
         uint32_t root_ref = 0u;
-        if (n > 1) {
+        const char* builder = getenv("XR_BVH_BUILDER");
+        const bool use_lbvh = builder && strcmp(builder, "lbvh") == 0;
+        if (n == 1) {
+            root_ref = 0u | kLeafBit;
+        } else if (use_lbvh) {
             k_karras<<<(n - 1 + 255) / 256, 256, 0, st>>>(k0, (int)n, left, right, pint, pleaf, range);
             k_bounds<<<(n + 255) / 256, 256, 0, st>>>((int)n, left, right, pint, pleaf, v0, tlo, thi, nlo, nhi, flags);
         } else {
-            root_ref = 0u | kLeafBit;
+            // PLOC rounds; the ping-pong cluster arrays reuse the Morton key buffers' space
+            uint32_t *cref0 = nullptr, *cref1 = nullptr, *nnb = nullptr, *keep = nullptr, *pos = nullptr, *sums = nullptr;
+            float4 *clo0 = nullptr, *chi0 = nullptr, *clo1 = nullptr, *chi1 = nullptr;
+            const uint32_t nbmax = (n + 1023) / 1024;
+            if ((s = dalloc(ctx, &cref0, n)) || (s = dalloc(ctx, &cref1, n)) || (s = dalloc(ctx, &nnb, n)) ||
+                (s = dalloc(ctx, &keep, n)) || (s = dalloc(ctx, &pos, n)) || (s = dalloc(ctx, &sums, nbmax + 1)) ||
+                (s = dalloc(ctx, &clo0, n)) || (s = dalloc(ctx, &chi0, n)) || (s = dalloc(ctx, &clo1, n)) ||
+                (s = dalloc(ctx, &chi1, n))) {
+                cudaFree(cref0); cudaFree(cref1); cudaFree(nnb); cudaFree(keep); cudaFree(pos); cudaFree(sums);
+                cudaFree(clo0); cudaFree(chi0); cudaFree(clo1); cudaFree(chi1);
+                goto done;
+            }
+            cudaMemsetAsync(counters + 3, 0, 4, st);
+            k_ploc_init<<<(n + 255) / 256, 256, 0, st>>>(n, v0, tlo, thi, cref0, clo0, chi0);
+            uint32_t cnt = n, rounds = 0;
+            while (cnt > 1 && !s) {
+                const uint32_t nb = (cnt + 1023) / 1024;
+                k_ploc_nn<<<(cnt + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, st>>>(cnt, clo0, chi0, nnb);
+                k_ploc_merge<<<(cnt + 255) / 256, 256, 0, st>>>(cnt, nnb, cref0, clo0, chi0, cref1, clo1, chi1, keep,
+                                                                 left, right, range, nlo, nhi, counters + 3, nint);
+                k_scan_local<<<nb, 1024, 0, st>>>(keep, cnt, pos, sums);
+                k_scan_top<<<1, 32, 0, st>>>(sums, nb);
+                k_ploc_compact<<<(cnt + 255) / 256, 256, 0, st>>>(cnt, keep, pos, sums, cref1, clo1, chi1, cref0, clo0, chi0);
+                uint32_t next = 0;
+                cudaMemcpyAsync(&next, sums + nb, 4, cudaMemcpyDeviceToHost, st);
+                if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: ploc"))) break;
+                if (next >= cnt || ++rounds > 100000) { s = fail(ctx, XR_ERR_STATE, "bvh: clustering made no progress"); break; }
+                cnt = next;
+            }
+            uint32_t made = 0;
+            if (!s) {
+                cudaMemcpy(&root_ref, cref0, 4, cudaMemcpyDeviceToHost);
+                cudaMemcpy(&made, counters + 3, 4, cudaMemcpyDeviceToHost);
+                if (made != n - 1) s = fail(ctx, XR_ERR_STATE, "bvh: clustering built the wrong number of nodes");
+            }
+            cudaFree(cref0); cudaFree(cref1); cudaFree(nnb); cudaFree(keep); cudaFree(pos); cudaFree(sums);
+            cudaFree(clo0); cudaFree(chi0); cudaFree(clo1); cudaFree(chi1);
+            if (s) goto done;
         }
         uint32_t cinit[4] = {1u, 0u, 0u, 0u};
         cudaMemcpyAsync(counters, cinit, sizeof(cinit), cudaMemcpyHostToDevice, st);
@@ -492,7 +677,7 @@ xr_status build_bvh(Context* ctx) {
         uint32_t ntask = 1, depth = 0;
         while (ntask > 0) {
             CollapseArgs ca;
-            ca.left = left; ca.right = right; ca.range = range; ca.nlo = nlo; ca.nhi = nhi; ca.tlo = tlo; ca.thi = thi;
+            ca.left = left; ca.right = right; ca.count = range; ca.nlo = nlo; ca.nhi = nhi; ca.tlo = tlo; ca.thi = thi;
             ca.sorted = v0; ca.tri_idx = ctx->d_tri_idx; ca.vpos = ctx->d_vpos;
             ca.task_in = ta; ca.task_wide_in = wa; ca.n_tasks = ntask; ca.task_out = tb; ca.task_wide_out = wb;
             ca.counters = counters; ca.nodes = nodes_tmp; ca.tris = ctx->d_tris; ca.emin = emin;

@@ -18,7 +18,7 @@
 #include <utility>
 
 #include "bsdf.cuh"
-#include "traverse.cuh"
+#include "wavefront_trace.cuh"
 
 namespace xr {
 namespace {
@@ -52,7 +52,7 @@ __device__ __forceinline__ HitPayload closest_hit(const DeviceScene& sc, const H
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
-__device__ __forceinline__ void flag_error(const FrameArgs& fa, uint32_t bits) { atomicOr(&fa.counters[63], bits); }
+__device__ __forceinline__ void flag_error(const FrameArgs& fa, uint32_t bits) { atomicOr(&fa.counters[kCntError], bits); }
 
 // ---------------------------------------------------------------------------
 // one bounce of one path
@@ -100,13 +100,13 @@ __device__ __forceinline__ void add_radiance(const FrameArgs& fa, uint32_t p, fl
     dst[p] = f4(L, v.w);
 }
 
-// Returns true when the path continues to bounce + 1 (state updated in place).
+// Shades the traced hit `h` of one path: records the bounce's sample fields,
+// samples the BSDF and returns true when the path continues to bounce + 1
+// (state updated in place).
 template <bool COMPAT>
-__device__ __forceinline__ bool bounce_step(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
-                                            uint32_t bounce, uint32_t nb, PathState& s) {
+__device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
+                                           uint32_t bounce, uint32_t nb, PathState& s, const HitRec& h) {
     const uint32_t p = s.pixel;
-    HitRec h;
-    if (!traverse<false>(fa.sc, s.o, s.d, 0.0001f, 10000.0f, h)) flag_error(fa, XR_DEVFLAG_STACK_OVERFLOW);
     HitPayload pl;
     pl.mat = -1;
     if (h.prim >= 0) pl = closest_hit(fa.sc, h);
@@ -214,14 +214,10 @@ __device__ __forceinline__ void push_path(const FrameArgs& fa, bool alive, const
     }
 }
 
-__device__ __forceinline__ void count_rays(const FrameArgs& fa, bool active) {
-    uint32_t mask = __ballot_sync(0xFFFFFFFFu, active);
-    if (lane_id() == 0 && mask) atomicAdd(&fa.counters[33], (uint32_t)__popc(mask));
-}
-
-// bounce 0: camera rays for a 16 x 8 pixel tile per block
+// Camera rays (ReSTIRGIInitialSample.rgen.hlsl:41-52) for a 16 x 8 pixel tile per
+// block, appended to the queue of bounce 0 in tile order.
 template <bool COMPAT>
-__global__ void __launch_bounds__(kBlock) k_bounce0(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t nb) {
+__global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t nb) {
     const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
     const uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 4);
     const bool inside = x < fa.W && y < fa.H;
@@ -241,35 +237,53 @@ __global__ void __launch_bounds__(kBlock) k_bounce0(FrameArgs fa, const XrUnifor
         s.o = xyz(origin);
         s.thr = f3(1.0f, 1.0f, 1.0f);
         s.pq = 0.0f;
-        if (nb == 0u) {
-            write_invalid<COMPAT>(fa, s.pixel, f3(0, 0, 0), f3(0, 0, 0), f3(0, 0, 0));
-        } else {
-            alive = bounce_step<COMPAT>(fa, u, 0u, nb, s);
-        }
+        if (nb == 0u) write_invalid<COMPAT>(fa, s.pixel, f3(0, 0, 0), f3(0, 0, 0), f3(0, 0, 0));
+        else alive = true;
     }
-    count_rays(fa, inside && nb != 0u);
-    push_path(fa, alive, s, 1u);
+    push_path(fa, alive, s, 0u);
 }
 
-// bounce >= 1: persistent grid over the queue written by the previous bounce
+// Closest hits of the paths of one bounce (TMin 1e-4, TMax 1e4,
+// ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
+__global__ void __launch_bounds__(kBlock) k_trace_paths(DeviceScene sc, const float4* __restrict__ q0,
+                                                        const float4* __restrict__ q1, uint4* __restrict__ hits,
+                                                        const uint32_t* count_ptr, uint32_t* next, uint32_t* err) {
+    const uint32_t count = *(volatile const uint32_t*)count_ptr;
+    trace_persistent<false>(
+        sc, count, next,
+        [&](uint32_t i) {
+            float4 a = q0[i], b = q1[i];
+            RayIn r;
+            r.o = xyz(a); r.d = xyz(b); r.tmin = 0.0001f; r.tmax = 10000.0f;
+            return r;
+        },
+        [&](uint32_t i, const HitRec& h) {
+            hits[i] = make_uint4((uint32_t)h.prim, __float_as_uint(h.t), __float_as_uint(h.b1), __float_as_uint(h.b2));
+        },
+        err);
+}
+
+// Shading of one bounce over the queue (persistent grid): coherent per-path
+// work after the divergent traversal.
 template <bool COMPAT>
-__global__ void __launch_bounds__(kBlock) k_bounce(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t bounce,
-                                                   uint32_t nb) {
+__global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t bounce,
+                                                  uint32_t nb) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[bounce];
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
         uint32_t i = base + threadIdx.x;
-        bool active = i < count;
         PathState s;
         bool alive = false;
-        if (active) {
+        if (i < count) {
             float4 a = fa.q_in[0][i], b = fa.q_in[1][i], c = fa.q_in[2][i];
+            uint4 hr = fa.hits[i];
             s.o = xyz(a); s.pixel = __float_as_uint(a.w);
             s.d = xyz(b); s.rng = __float_as_uint(b.w);
             s.thr = xyz(c); s.pq = c.w;
-            alive = bounce_step<COMPAT>(fa, u, bounce, nb, s);
+            HitRec h;
+            h.prim = (int32_t)hr.x; h.t = __uint_as_float(hr.y); h.b1 = __uint_as_float(hr.z); h.b2 = __uint_as_float(hr.w);
+            alive = shade_step<COMPAT>(fa, u, bounce, nb, s, h);
         }
-        count_rays(fa, active);
         push_path(fa, alive, s, bounce + 1u);
     }
 }
@@ -579,7 +593,96 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     if (out_here) write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);
 }
 
-__global__ void __launch_bounds__(256) k_spatial(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+// Spatial reuse, step 1 of 3 (corrected mode with shadow rays): replays the
+// neighbour picks of the resolve step (same RNG stream: one draw for the centre
+// merge, two per pick, one per accepted neighbour's merge) and queues one
+// shadow ray {pixel << 5 | slot, neighbour} per neighbour whose sample would
+// get a non-zero weight.  Every pixel clears its occlusion bits.
+__global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = lane_id();
+    uint32_t emit_mask = 0u;
+    uint32_t nb_of[32];
+    if (p < fa.N) {
+        fa.occ[p] = 0u;
+        const uint32_t x = p % fa.W, y = p / fa.W;
+        const float4 g = fa.gb_pos_cur[p];
+        const uint32_t mat = fa.gb_mat_cur[p];
+        const float4 b = fa.cand_b[p];
+        if (mat != kInvalid && (__float_as_uint(b.w) >> 31) != 0u) {
+            uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
+            const float3 x_view = xyz(g);
+            const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
+            (void)random_float(rng);   // the centre merge's draw
+            for (uint32_t i = 0; i < fa.n_nb; i++) {
+                const uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, fa.radius, rng);
+                const uint32_t nmat = fa.gb_mat_cur[nbi];
+                if (nmat == kInvalid) continue;
+                const float4 ng = fa.gb_pos_cur[nbi];
+                const float3 dd = x_view - xyz(ng);
+                if (dot(dd, dd) > 0.1f) continue;
+                if (dot(n_view, oct_decode(__float_as_uint(ng.w), 16)) < 0.8f) continue;
+                if (mat != nmat) continue;
+                Res rn;
+                load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
+                const float ph = length(rn.L) * jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
+                (void)random_float(rng);   // the merge's draw
+                if (ph > 0.0f) { emit_mask |= 1u << i; nb_of[i] = nbi; }
+            }
+        }
+    }
+    // one atomic per warp: exclusive scan of the per-lane ray counts
+    const uint32_t cnt = __popc(emit_mask);
+    uint32_t incl = cnt;
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if ((int)lane >= off) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(&fa.counters[32], total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31);
+    uint32_t pos = base + incl - cnt;
+    while (emit_mask) {
+        const uint32_t i = __ffs(emit_mask) - 1u;
+        emit_mask &= emit_mask - 1u;
+        fa.shadow_q[pos++] = make_uint2((p << 5) | i, nb_of[i]);
+    }
+}
+
+// Spatial reuse, step 2 of 3: any-hit traversal of the queued shadow rays
+// (ReSTIRGISpatialReuse.rgen.hlsl:44-62 with the centre pixel's visible point as
+// origin); an occluded ray sets its slot's bit in the pixel's occlusion word.
+__global__ void __launch_bounds__(kBlock) k_trace_shadow(FrameArgs fa) {
+    const uint32_t count = *(volatile const uint32_t*)&fa.counters[32];
+    trace_persistent<true>(
+        fa.sc, count, &fa.counters[kCntFetchShadow],
+        [&](uint32_t i) {
+            const uint2 e = fa.shadow_q[i];
+            const float4 g = fa.gb_pos_cur[e.x >> 5];
+            const float3 from = xyz(g);
+            const float3 n = oct_decode(__float_as_uint(g.w), 16);
+            const float3 to = xyz(fa.rt_cur0[e.y]);
+            const float3 dir = to - from;
+            RayIn r;
+            r.o = from + n * 0.01f;
+            r.d = normalize(dir);
+            r.tmin = 0.0f;
+            r.tmax = length(dir) - 0.01f;
+            return r;
+        },
+        [&](uint32_t i, const HitRec& h) {
+            if (h.prim >= 0) {
+                const uint32_t owner = fa.shadow_q[i].x;
+                atomicOr(&fa.occ[owner >> 5], 1u << (owner & 31u));
+            }
+        },
+        &fa.counters[kCntError]);
+}
+
+// Spatial reuse, step 3 of 3: the merge of ReSTIRGISpatialReuse.rgen.hlsl:91-176
+// with the visibility of step 2, M cap, W, shading and tone mapping.
+__global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
     const uint32_t x = p % fa.W, y = p / fa.W;
@@ -596,10 +699,10 @@ __global__ void __launch_bounds__(256) k_spatial(FrameArgs fa, const XrUniformBu
     uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
     const float3 x_view = xyz(g);
     const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
+    const uint32_t occ = fa.visibility ? fa.occ[p] : 0u;
     Res center; load_packed(fa.rt_cur0, fa.rt_cur1, p, center);
     Res r; res_init(r);
     res_merge(r, center, length(center.L), rng);
-    uint32_t shadow = 0;
     for (uint32_t i = 0; i < fa.n_nb; i++) {
         uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, fa.radius, rng);
         uint32_t nmat = fa.gb_mat_cur[nbi];
@@ -612,15 +715,7 @@ __global__ void __launch_bounds__(256) k_spatial(FrameArgs fa, const XrUniformBu
         Res rn; load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
         float jac = jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
         float ph = length(rn.L) * jac;
-        if (fa.visibility && ph > 0.0f) {
-            float3 dir = rn.xs - x_view;
-            float dist = length(dir);
-            float3 ro = x_view + n_view * 0.01f;
-            HitRec hh;
-            if (!traverse<true>(fa.sc, ro, normalize(dir), 0.0f, dist - 0.01f, hh)) flag_error(fa, XR_DEVFLAG_STACK_OVERFLOW);
-            shadow++;
-            if (hh.prim >= 0) ph = 0.0f;
-        }
+        if (ph > 0.0f && ((occ >> i) & 1u)) ph = 0.0f;
         res_merge(r, rn, ph, rng);
         if (ph == 0.0f) r.m -= rn.m;
     }
@@ -632,7 +727,6 @@ __global__ void __launch_bounds__(256) k_spatial(FrameArgs fa, const XrUniformBu
     r.W = (phf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * phf) : 0.0f;
     store_packed(fa.rs0, fa.rs1, p, r);
     write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);
-    if (shadow) atomicAdd(&fa.counters[32], shadow);
 }
 
 // ---------------------------------------------------------------------------
@@ -753,28 +847,41 @@ __global__ void k_import_res_packed(float4* __restrict__ p0, float4* __restrict_
 
 }  // namespace
 
+// Resident blocks per SM of the persistent kernels (queried once per process).
 uint32_t persistent_grid(int sm_count, bool compat) {
     static int occ[2] = {0, 0};
     int& o = occ[compat ? 1 : 0];
     if (o == 0) {
         int v = 0;
-        if (compat) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_bounce<true>, kBlock, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_bounce<false>, kBlock, 0);
+        if (compat) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_shade<true>, kBlock, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_shade<false>, kBlock, 0);
         o = v > 0 ? v : 4;
     }
     return (uint32_t)(o * sm_count);
 }
 
+uint32_t trace_grid(int sm_count) {
+    static int occ = 0;
+    if (occ == 0) {
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths, kBlock, 0);
+        occ = v > 0 ? v : 4;
+    }
+    return (uint32_t)(occ * sm_count);
+}
+
 void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
     dim3 grid0((fa.W + 15u) / 16u, (fa.H + 7u) / 8u);
     FrameArgs a = fa;
-    if (fa.compat) k_bounce0<true><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
-    else k_bounce0<false><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
-    for (uint32_t b = 1; b < nb; b++) {
-        // queues alternate: bounce b reads what bounce b-1 wrote
+    if (fa.compat) k_raygen<true><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
+    else k_raygen<false><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
+    for (uint32_t b = 0; b < nb; b++) {
+        // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
-        if (fa.compat) k_bounce<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
-        else k_bounce<false><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
+        k_trace_paths<<<fa.grid_trace, kBlock, 0, st>>>(fa.sc, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+                                                        fa.counters + kCntFetchPath + b, fa.counters + kCntError);
+        if (fa.compat) k_shade<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
+        else k_shade<false><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
     }
 }
 
@@ -807,8 +914,15 @@ void launch_import_res_packed(float4* p0, float4* p1, uint32_t n, const uint32_t
 
 void launch_spatial(const FrameArgs& fa, cudaStream_t st) {
     uint32_t blocks = (fa.N + 255u) / 256u;
-    if (fa.compat) k_spatial_compat<<<blocks, 256, 0, st>>>(fa, fa.ubo);
-    else k_spatial<<<blocks, 256, 0, st>>>(fa, fa.ubo);
+    if (fa.compat) {
+        k_spatial_compat<<<blocks, 256, 0, st>>>(fa, fa.ubo);
+        return;
+    }
+    if (fa.visibility) {
+        k_spatial_select<<<blocks, 256, 0, st>>>(fa, fa.ubo);
+        k_trace_shadow<<<fa.grid_trace, kBlock, 0, st>>>(fa);
+    }
+    k_spatial_resolve<<<blocks, 256, 0, st>>>(fa, fa.ubo);
 }
 
 }  // namespace xr

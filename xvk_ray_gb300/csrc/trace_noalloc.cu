@@ -16,7 +16,8 @@
 // shares the array and it keeps the last call's contents; the error word is
 // cleared at the start of each call.  Calls that overlap on the GPU (several
 // host threads, or contexts on different streams of one device) race on the
-// array: serialise them.
+// array: serialise them.  The error word and the kernel's ray-fetch counter
+// must start at zero and are cleared at the start of every call.
 #include <mutex>
 #include <string>
 
@@ -34,6 +35,7 @@ struct TraceScratch {
     int32_t prim[kMaxRays];
     float t[kMaxRays];
     uint32_t flags;               // device-side error word, cleared per call
+    uint32_t fetch;               // the kernel's ray-fetch counter, cleared per call
 };
 
 }  // namespace
@@ -85,10 +87,10 @@ extern "C" xr_status xr_trace_rays_noalloc(XrContext* c, const float* rays, uint
     xr_status st = scratch_for(c, &s);
     if (!st) {
         cudaStream_t sm = c->stream;
-        cudaMemsetAsync(&s->flags, 0, sizeof(uint32_t), sm);
+        cudaMemsetAsync(&s->flags, 0, 2 * sizeof(uint32_t), sm);   // flags and fetch
         cudaMemcpyAsync(s->rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, sm);
         launch_trace(c->fa.sc, reinterpret_cast<const float*>(s->rays), n, any_hit, s->prim, s->t,
-                     reinterpret_cast<float*>(s->bary), &s->flags, c->sm_count, sm);
+                     reinterpret_cast<float*>(s->bary), &s->fetch, &s->flags, nullptr, c->sm_count, sm);
         cudaMemcpyAsync(prim, s->prim, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);
         cudaMemcpyAsync(t, s->t, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);
         cudaMemcpyAsync(bary, s->bary, (size_t)n * 8, cudaMemcpyDeviceToHost, sm);

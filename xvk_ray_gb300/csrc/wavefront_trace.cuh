@@ -1,0 +1,212 @@
+// wavefront_trace.cuh -- persistent CWBVH traversal with dynamic ray fetching.
+//
+// Software replacement of the hardware TraceRay (opaque triangles, no culling,
+// closest hit with ties to the lowest primitive id, or first hit for shadow
+// rays).  Each warp keeps 32 rays in flight; whenever lanes finish, the warp
+// refills them from the ray queue with one atomic (Aila and Laine, "Understanding
+// the Efficiency of Ray Traversal on GPUs", HPG 2009).  The loop follows Ylitie,
+// Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+// Compressed Wide BVHs" (HPG 2017): a lane holds one group of internal children
+// still to visit (base index, hit bits in near-to-far order, internal-child
+// mask) and one group of triangles; each iteration visits at most one node,
+// then tests triangles while enough lanes of the warp have some, and postpones
+// the rest onto the lane's stack otherwise.
+//
+// The triangle test and the box test are those of traverse.cuh (same arithmetic
+// as the CPU oracle); only the order of the work differs, which the closest-hit
+// rule makes irrelevant for the result.
+#pragma once
+#include "traverse.cuh"
+
+namespace xr {
+
+constexpr uint32_t kTriGroupBit = 0x80000000u;   // stack entry holds a triangle group
+constexpr int kPostponeBelow = 12;                // lanes; fewer testing triangles -> postpone
+
+struct RayIn {
+    float3 o, d;
+    float tmin, tmax;
+};
+
+// Byte k of `word` as an exact float: the byte becomes the low mantissa bits of
+// 2^23 (one byte permute), then 2^23 is subtracted -- no integer-to-float
+// conversion unit involved.
+__device__ __forceinline__ float qbyte(uint32_t word, uint32_t k) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7650u | k)) - 8388608.0f;
+}
+
+// LoadRay(i) -> RayIn; StoreHit(i, const HitRec&).  `next` is the fetch counter
+// (zeroed before the launch), `count` the number of rays, `err` the error word.
+// With `work` non-null (query kernels only) the node visits and triangle tests
+// are summed into work[0] and work[1].
+template <bool ANY, typename LoadRay, typename StoreHit>
+__device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t count, uint32_t* next,
+                                                 LoadRay load, StoreHit store, uint32_t* err,
+                                                 unsigned long long* work = nullptr) {
+    const uint32_t FULL = 0xFFFFFFFFu;
+    uint32_t n_visits = 0, n_tests = 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    bool active = false, drained = false;
+    uint32_t ray_id = 0;
+    float3 o = f3(0, 0, 0);
+    float idx = 0, idy = 0, idz = 0, tmin = 0, tmin_box = 0;
+    RayTri rt;
+    uint32_t flip = 0;
+    HitRec h;
+    h.prim = -1; h.t = 0; h.b1 = 0; h.b2 = 0;
+    uint2 stack[kStackSize];
+    int sp = 0;
+    uint32_t ng_base = 0, ng_bits = 0;   // bits 0..7 hits (near-to-far), 8..15 internal-child mask
+    uint32_t tg_base = 0, tg_mask = 0;
+    uint32_t visits_left = 0;
+    bool bad = false;
+
+    while (true) {
+        // ---- refill idle lanes ----
+        const uint32_t idle = __ballot_sync(FULL, !active);
+        if (idle && !drained) {
+            const uint32_t n_idle = __popc(idle);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(next, n_idle);
+            base = __shfl_sync(FULL, base, 0);
+            if (base + n_idle >= count) drained = true;
+            if (!active) {
+                const uint32_t my = base + __popc(idle & lt_mask);
+                if (my < count) {
+                    RayIn r = load(my);
+                    ray_id = my;
+                    active = true;
+                    o = r.o;
+                    tmin = r.tmin;
+                    tmin_box = r.tmin * (1.0f - 1e-6f) - 1e-30f;
+                    idx = 1.0f / r.d.x; idy = 1.0f / r.d.y; idz = 1.0f / r.d.z;
+                    rt = prep_ray(r.o, r.d);
+                    // sign bits (so that -0 selects the same planes as its infinite reciprocal)
+                    flip = (__float_as_uint(r.d.x) >> 31) | ((__float_as_uint(r.d.y) >> 31) << 1) |
+                           ((__float_as_uint(r.d.z) >> 31) << 2);
+                    h.prim = -1; h.t = r.tmax; h.b1 = 0.0f; h.b2 = 0.0f;
+                    sp = 0;
+                    tg_mask = 0;
+                    visits_left = sc.n_nodes;
+                    // a virtual group whose only child is the root (node 0)
+                    ng_base = 0;
+                    ng_bits = sc.n_nodes ? (1u | ((1u << flip) << 8)) : 0u;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) break;
+
+        // ---- node phase: visit the nearest remaining child of the current group ----
+        if (active && tg_mask == 0u && (ng_bits & 0xFFu)) {
+            const uint32_t k = __ffs(ng_bits & 0xFFu) - 1u;
+            ng_bits &= ~(1u << k);
+            const uint32_t slot = k ^ flip;
+            const uint32_t node = ng_base + __popc((ng_bits >> 8) & ((1u << slot) - 1u));
+            if (ng_bits & 0xFFu) {
+                if (sp < kStackSize) stack[sp++] = make_uint2(ng_base, ng_bits);
+                else bad = true;
+            }
+            if (node >= sc.n_nodes || visits_left == 0u) {
+                bad = true;
+                ng_bits = 0;
+            } else {
+                visits_left--;
+                n_visits++;
+                const uint4* np = reinterpret_cast<const uint4*>(sc.nodes + node);
+                const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
+                            w4 = __ldg(np + 4);
+                const float sx = __uint_as_float((w0.w & 0xFFu) << 23) * idx;
+                const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * idy;
+                const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * idz;
+                const float ax = (__uint_as_float(w0.x) - o.x) * idx;
+                const float ay = (__uint_as_float(w0.y) - o.y) * idy;
+                const float az = (__uint_as_float(w0.z) - o.z) * idz;
+                const float tlimit = h.t * (1.0f + 1e-6f) + 1e-30f;
+                // near and far quantised planes per axis, chosen once per node from the
+                // sign bits of the direction (a negative axis enters through the high plane)
+                const bool nx = (flip & 1u) != 0u, ny = (flip & 2u) != 0u, nz = (flip & 4u) != 0u;
+                const uint32_t xn0 = nx ? w3.z : w2.x, xn1 = nx ? w3.w : w2.y;
+                const uint32_t xf0 = nx ? w2.x : w3.z, xf1 = nx ? w2.y : w3.w;
+                const uint32_t yn0 = ny ? w4.x : w2.z, yn1 = ny ? w4.y : w2.w;
+                const uint32_t yf0 = ny ? w2.z : w4.x, yf1 = ny ? w2.w : w4.y;
+                const uint32_t zn0 = nz ? w4.z : w3.x, zn1 = nz ? w4.w : w3.y;
+                const uint32_t zf0 = nz ? w3.x : w4.z, zf1 = nz ? w3.y : w4.w;
+                uint32_t hits = 0, trimask = 0;
+#pragma unroll
+                for (uint32_t i = 0; i < 8; i++) {
+                    const uint32_t meta = byte_of(w1.z, w1.w, i);
+                    const float txn = __fmaf_rn(qbyte(i < 4 ? xn0 : xn1, i & 3u), sx, ax);
+                    const float txf = __fmaf_rn(qbyte(i < 4 ? xf0 : xf1, i & 3u), sx, ax);
+                    const float tyn = __fmaf_rn(qbyte(i < 4 ? yn0 : yn1, i & 3u), sy, ay);
+                    const float tyf = __fmaf_rn(qbyte(i < 4 ? yf0 : yf1, i & 3u), sy, ay);
+                    const float tzn = __fmaf_rn(qbyte(i < 4 ? zn0 : zn1, i & 3u), sz, az);
+                    const float tzf = __fmaf_rn(qbyte(i < 4 ? zf0 : zf1, i & 3u), sz, az);
+                    const float tn = fmaxf(fmaxf(txn, tyn), fmaxf(tzn, tmin_box));
+                    const float tf = fminf(fminf(txf, tyf), fminf(tzf, tlimit));
+                    if (meta != 0u && tn <= __fmaf_rn(tf, 1.0f + 2e-6f, 1e-30f)) {
+                        if (meta == 0x80u) hits |= 1u << (i ^ flip);
+                        else trimask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+                    }
+                }
+                ng_base = w1.x;
+                ng_bits = hits | ((w0.w >> 24) << 8);
+                tg_base = w1.y;
+                tg_mask = trimask;
+            }
+        }
+
+        // ---- triangle phase: test while enough lanes have triangles ----
+        bool first = true;
+        while (true) {
+            const bool want = active && tg_mask != 0u;
+            const uint32_t m = __ballot_sync(FULL, want);
+            if (!m) break;
+            if (!first && (int)__popc(m) < kPostponeBelow) {
+                if (want && sp < kStackSize) {
+                    stack[sp++] = make_uint2(tg_base, tg_mask | kTriGroupBit);
+                    tg_mask = 0u;
+                }
+                break;
+            }
+            first = false;
+            if (want) {
+                const uint32_t bit = __ffs(tg_mask) - 1u;
+                n_tests++;
+                tg_mask &= tg_mask - 1u;
+                if (tg_base + bit >= sc.ntri) {
+                    bad = true;
+                } else {
+                    const float4* tp = sc.tri + 3u * (tg_base + bit);
+                    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                    const int32_t prim = (int32_t)__float_as_uint(a.w);
+                    float tt, b1, b2;
+                    if (hit_triangle(rt, xyz(a), xyz(b), xyz(c), tmin, h.t, &tt, &b1, &b2) &&
+                        (h.prim < 0 || tt < h.t || (tt == h.t && prim < h.prim))) {
+                        h.prim = prim; h.t = tt; h.b1 = b1; h.b2 = b2;
+                        if (ANY) { tg_mask = 0u; ng_bits = 0u; sp = 0; }
+                    }
+                }
+            }
+        }
+
+        // ---- pop or finish ----
+        if (active && tg_mask == 0u && !(ng_bits & 0xFFu)) {
+            if (sp == 0) {
+                store(ray_id, h);
+                active = false;
+            } else {
+                const uint2 e = stack[--sp];
+                if (e.y & kTriGroupBit) { tg_base = e.x; tg_mask = e.y & 0x00FFFFFFu; ng_bits = 0u; }
+                else { ng_base = e.x; ng_bits = e.y; }
+            }
+        }
+    }
+    if (__any_sync(FULL, bad) && bad) atomicOr(err, (uint32_t)XR_DEVFLAG_STACK_OVERFLOW);
+    if (work) {
+        atomicAdd(&work[0], (unsigned long long)n_visits);
+        atomicAdd(&work[1], (unsigned long long)n_tests);
+    }
+}
+
+}  // namespace xr

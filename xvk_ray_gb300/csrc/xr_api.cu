@@ -4,6 +4,7 @@
 // upload the frame's UBO, then initial sample -> temporal reuse -> spatial reuse
 // in stream order on the context's own stream.  No exception leaves this file;
 // every failure returns a status and records a message for xr_last_error().
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -51,6 +52,7 @@ xr_status cuda_check(Context* ctx, cudaError_t e, const char* what) {
 }
 
 uint32_t persistent_grid(int sm_count, bool compat);
+uint32_t trace_grid(int sm_count);
 
 namespace {
 
@@ -87,6 +89,11 @@ xr_status alloc_pixels(Context* c) {
         add((void**)&fa.rs0, N * 16); add((void**)&fa.rs1, N * 16);
     }
     if (P.write_pt) { add((void**)&fa.thr0, N * 16); add((void**)&fa.out_pt, N * 16); }
+    if (!compat) {
+        add((void**)&fa.occ, N * 4);
+        add((void**)&fa.shadow_q, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
+    }
+    add((void**)&fa.hits, N * 16);
     add((void**)&fa.out_ldr, N * 4);
     if (P.write_hdr) add((void**)&fa.out_hdr, N * 16);
     for (int i = 0; i < 2; i++)
@@ -126,6 +133,7 @@ void set_frame_pointers(Context* c, uint32_t parity) {
         fa.rt_prev0 = c->rt0[1 - parity]; fa.rt_prev1 = c->rt1[1 - parity];
     }
     fa.grid_persistent = persistent_grid(c->sm_count, P.compat_reference != 0);
+    fa.grid_trace = trace_grid(c->sm_count);
 }
 
 xr_status upload_ubo(Context* c, const XrUniformBufferObject* ubo) {
@@ -141,7 +149,7 @@ xr_status upload_ubo(Context* c, const XrUniformBufferObject* ubo) {
 
 xr_status check_flags(Context* c) {
     uint32_t flags = 0;
-    xr_status s = cuda_check(c, cudaMemcpy(&flags, c->d_counters + 63, 4, cudaMemcpyDeviceToHost), "read device flags");
+    xr_status s = cuda_check(c, cudaMemcpy(&flags, c->d_counters + kCntError, 4, cudaMemcpyDeviceToHost), "read device flags");
     if (s) return s;
     if (flags & ~c->error_flags) {
         c->error_flags |= flags;
@@ -223,8 +231,10 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     if (prop.major < 10) { s = fail(c, XR_ERR_UNSUPPORTED, "create: this library is built for sm_103a (GB300)"); goto bad; }
     c->sm_count = prop.multiProcessorCount;
     if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) goto bad;
-    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_counters, 64 * 4), "counters"))) goto bad;
-    if ((s = cuda_check(c, cudaMemset(c->d_counters, 0, 64 * 4), "counters"))) goto bad;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_counters, kCounterWords * 4), "counters"))) goto bad;
+    if ((s = cuda_check(c, cudaMemset(c->d_counters, 0, kCounterWords * 4), "counters"))) goto bad;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_work, 2 * sizeof(unsigned long long)), "work counters"))) goto bad;
+    if ((s = cuda_check(c, cudaMemset(c->d_work, 0, 2 * sizeof(unsigned long long)), "work counters"))) goto bad;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_ubo, sizeof(XrUniformBufferObject)), "ubo"))) goto bad;
     if ((s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, sizeof(XrUniformBufferObject)), "ubo staging"))) goto bad;
     for (int i = 0; i < 6; i++)
@@ -252,7 +262,7 @@ void xr_destroy(XrContext* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_pixels(c);
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
-    cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo);
+    cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo); cudaFree(c->d_work);
     if (c->h_ubo) cudaFreeHost(c->h_ubo);
     for (int i = 0; i < 6; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
@@ -339,7 +349,8 @@ xr_status xr_set_params(XrContext* c, const XrParams* p) {
     DeviceGuard g(c->device);
     const XrParams& o = c->params;
     bool realloc = !c->pix_mem || o.width != p->width || o.height != p->height || o.compat_reference != p->compat_reference ||
-                   o.write_pt != p->write_pt || o.write_hdr != p->write_hdr;
+                   o.write_pt != p->write_pt || o.write_hdr != p->write_hdr ||
+                   (!p->compat_reference && o.n_neighbours != p->n_neighbours);
     c->params = *p;
     c->params_set = true;
     if (realloc) {
@@ -366,7 +377,7 @@ xr_status xr_render_frame(XrContext* c, const XrUniformBufferObject* ubo) {
     xr_status s = upload_ubo(c, ubo);
     if (s) return s;
     set_frame_pointers(c, ubo->current_frame % 2u);
-    cudaMemsetAsync(c->d_counters, 0, 63 * 4, c->stream);   // keep the sticky error word [63]
+    cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);   // keep the sticky error word
     const bool compat = c->params.compat_reference != 0;
     cudaEventRecord(c->ev[0], c->stream);
     launch_initial(c->fa, ubo->number_of_bounces, c->stream);
@@ -377,6 +388,7 @@ xr_status xr_render_frame(XrContext* c, const XrUniformBufferObject* ubo) {
     if (compat || c->params.spatial_on) launch_spatial(c->fa, c->stream);
     cudaEventRecord(c->ev[3], c->stream);
     c->frames++;
+    c->last_bounces = ubo->number_of_bounces;
     return cuda_check(c, cudaGetLastError(), "render_frame launch");
 }
 
@@ -431,13 +443,21 @@ xr_status xr_get_stats(XrContext* c, XrStats* st) {
         cudaEventElapsedTime(&o.ms_temporal, c->ev[1], c->ev[2]);
         cudaEventElapsedTime(&o.ms_spatial, c->ev[2], c->ev[3]);
         cudaEventElapsedTime(&o.ms_frame, c->ev[0], c->ev[3]);
-        uint32_t cnt[64];
+        uint32_t cnt[kCounterWords];
         cudaMemcpy(cnt, c->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost);
-        o.rays_traced = cnt[33];
-        o.shadow_rays = cnt[32];
+        o.rays_traced = 0;
+        for (uint32_t b = 0; b < c->last_bounces && b <= kMaxBounces; b++) o.rays_traced += cnt[b];
+        o.shadow_rays = cnt[kCntShadow];
     }
     o.bvh_nodes = c->n_nodes; o.bvh_triangles = c->n_tri_slots; o.bvh_depth = c->bvh_depth;
     o.ms_bvh_build = c->ms_bvh;
+    if (c->query_rays) {
+        unsigned long long w[2] = {0, 0};
+        cudaMemcpy(w, c->d_work, sizeof(w), cudaMemcpyDeviceToHost);
+        o.query_rays = c->query_rays;
+        o.query_node_visits = w[0];
+        o.query_tri_tests = w[1];
+    }
     *st = o;
     return s;
 }
@@ -531,7 +551,11 @@ xr_status xr_trace_rays_device(XrContext* c, const float* d_rays, uint32_t n, in
     if (!c->bvh_ready) return fail(c, XR_ERR_STATE, "trace: build the BVH first");
     if (n && (!d_rays || !d_prim || !d_t || !d_bary)) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null array");
     DeviceGuard g(c->device);
-    launch_trace(c->fa.sc, d_rays, n, any_hit, d_prim, d_t, d_bary, c->d_counters + 63, c->sm_count, c->stream);
+    cudaMemsetAsync(c->d_counters + kCntFetchQuery, 0, 4, c->stream);
+    cudaMemsetAsync(c->d_work, 0, 2 * sizeof(unsigned long long), c->stream);
+    c->query_rays = n;
+    launch_trace(c->fa.sc, d_rays, n, any_hit, d_prim, d_t, d_bary, c->d_counters + kCntFetchQuery,
+                 c->d_counters + kCntError, c->d_work, c->sm_count, c->stream);
     return cuda_check(c, cudaGetLastError(), "trace launch");
 }
 

@@ -34,6 +34,15 @@ namespace xr {
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr int kStackSize = 40;
 
+// Per-context device counter words (zeroed per frame except the error word).
+constexpr uint32_t kCntShadow = 32;        // shadow rays queued by the spatial pass
+constexpr uint32_t kCntFetchPath = 64;     // + bounce: ray-fetch counter of that bounce's trace
+constexpr uint32_t kCntFetchShadow = 96;   // ray-fetch counter of the shadow trace
+constexpr uint32_t kCntFetchQuery = 97;    // ray-fetch counter of xr_trace_rays
+constexpr uint32_t kCntError = 127;        // sticky XR_DEVFLAG_* bits
+constexpr uint32_t kCounterWords = 128;
+constexpr uint32_t kMaxBounces = 31;
+
 // 8-wide compressed BVH node, 80 B (five 16-byte words).
 //  w0: origin p.xyz, byte-packed {e.x, e.y, e.z (biased by 127), internal mask}
 //  w1: child_base, tri_base, meta[0..3], meta[4..7]
@@ -86,8 +95,11 @@ struct FrameArgs {
     uchar4* out_ldr; float4* out_hdr; float4* out_pt;
     // wavefront
     float4* q_in[3]; float4* q_out[3];
-    uint32_t* counters;       // [0..7] queue counts, [8] shadow rays, [9] rays, [15] error flags
-    uint32_t grid_persistent;
+    uint4* hits;              // closest-hit record per queue slot {prim, t, b1, b2}
+    uint2* shadow_q;          // corrected spatial pass: {pixel << 5 | slot, neighbour pixel}
+    uint32_t* occ;            // per pixel: occluded neighbour slots
+    uint32_t* counters;       // [b] paths entering bounce b, then the kCnt* words above
+    uint32_t grid_persistent, grid_trace;
 };
 
 struct Context {
@@ -130,6 +142,9 @@ struct Context {
 
     // statistics
     uint32_t frames = 0;
+    uint32_t last_bounces = 0;
+    unsigned long long* d_work = nullptr;   // node visits, triangle tests of the last ray query
+    uint64_t query_rays = 0;
     uint32_t error_flags = 0;
     cudaEvent_t ev[6] = {};
     cudaEvent_t user_ev[8] = {};
@@ -143,8 +158,10 @@ xr_status cuda_check(Context* ctx, cudaError_t e, const char* what);
 xr_status build_bvh(Context* ctx);
 
 // ---- launch wrappers (trace.cu) ----
+// `fetch` must be zero when the launch starts (the kernel's ray-fetch counter).
 void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_hit, int32_t* prim, float* t,
-                  float* bary, uint32_t* flags, int sm_count, cudaStream_t st);
+                  float* bary, uint32_t* fetch, uint32_t* flags, unsigned long long* work, int sm_count,
+                  cudaStream_t st);
 
 // ---- launch wrappers (restir.cu) ----
 void launch_initial(const FrameArgs& fa, uint32_t number_of_bounces, cudaStream_t st);
