@@ -382,7 +382,7 @@ __global__ void k_collapse(CollapseArgs a) {
         }
         uint32_t r = refs[c];
         if (imask & (1u << s)) {
-            meta[s] = 0x80;
+            meta[s] = (uint8_t)(0x20u | (24u + (uint32_t)s));   // one bit, at 24 + slot
             uint32_t rank = __popc(imask & ((1u << s) - 1u));
             uint32_t slot = atomicAdd(&a.counters[2], 1u);
             a.task_out[slot] = r;
@@ -403,7 +403,7 @@ __global__ void k_collapse(CollapseArgs a) {
             }
             uint32_t cnt = cnt_of[c];
             if (np != cnt) { atomicOr(&a.counters[3], 2u); cnt = min(np, 3u); }
-            meta[s] = (uint8_t)((cnt << 5) | off);
+            meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | off);   // cnt bits, at the triangle offset
             for (uint32_t j = 0; j < cnt; j++) {
                 uint32_t prim = prims[j];
                 uint4 id = a.tri_idx[prim];

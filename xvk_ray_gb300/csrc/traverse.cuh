@@ -1,4 +1,4 @@
-// traverse.cuh -- closest-hit / any-hit traversal of the 8-wide compressed BVH.
+// traverse.cuh -- ray/triangle and node primitives of the 8-wide compressed BVH traversal.
 //
 // Replaces TraceRay against the driver-built BLAS/TLAS (ReSTIRGIInitialSample.rgen.hlsl:90-98,
 // ReSTIRGISpatialReuse.rgen.hlsl:58-59): opaque triangles, no culling, hits accepted
@@ -93,104 +93,6 @@ struct HitRec {
 __device__ __forceinline__ uint32_t byte_of(uint32_t w0, uint32_t w1, uint32_t i) {
     uint32_t w = i < 4 ? w0 : w1;
     return (w >> ((i & 3u) * 8u)) & 0xFFu;
-}
-
-// One ray through the wide BVH.  ANY: stop at the first accepted hit.
-// Returns false when the traversal stack would overflow or the tree is malformed
-// (the caller flags it).
-template <bool ANY>
-__device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 o, float3 d, float tmin, float tmax,
-                                         HitRec& h) {
-    h.prim = -1; h.t = tmax; h.b1 = 0.0f; h.b2 = 0.0f;
-    if (sc.n_nodes == 0) return true;
-    const RayTri rt = prep_ray(o, d);
-    const float idx = 1.0f / d.x, idy = 1.0f / d.y, idz = 1.0f / d.z;
-    // visit near children first: slot bit k set means the child lies on the +k side
-    const uint32_t flip = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-    const float tmin_box = tmin * (1.0f - 1e-6f) - 1e-30f;
-
-    uint2 stack[kStackSize];
-    int sp = 0;
-    uint32_t node = 0;
-    bool ok = true;
-    // a well-formed tree visits each node at most once; the limit only stops a
-    // corrupted one from looping
-    uint32_t visits_left = sc.n_nodes;
-    // group = children of the last visited node still to visit
-    uint32_t g_base = 0, g_hits = 0, g_imask = 0;
-    while (true) {
-        // ---- visit `node`: test its 8 child boxes, then its leaf triangles ----
-        if (node >= sc.n_nodes || visits_left == 0u) { ok = false; break; }
-        visits_left--;
-        {
-            const uint4* np = reinterpret_cast<const uint4*>(sc.nodes + node);
-            uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-            float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-            uint32_t ex = w0.w & 0xFFu, ey = (w0.w >> 8) & 0xFFu, ez = (w0.w >> 16) & 0xFFu;
-            uint32_t imask = w0.w >> 24;
-            float sx = __uint_as_float(ex << 23) * idx;   // 2^(e-127) / d
-            float sy = __uint_as_float(ey << 23) * idy;
-            float sz = __uint_as_float(ez << 23) * idz;
-            float ax = (px - o.x) * idx, ay = (py - o.y) * idy, az = (pz - o.z) * idz;
-            const float tlimit = h.t * (1.0f + 1e-6f) + 1e-30f;
-            uint32_t hits = 0, trimask = 0;
-#pragma unroll
-            for (uint32_t i = 0; i < 8; i++) {
-                uint32_t meta = byte_of(w1.z, w1.w, i);
-                float qlx = (float)byte_of(w2.x, w2.y, i), qly = (float)byte_of(w2.z, w2.w, i);
-                float qlz = (float)byte_of(w3.x, w3.y, i), qhx = (float)byte_of(w3.z, w3.w, i);
-                float qhy = (float)byte_of(w4.x, w4.y, i), qhz = (float)byte_of(w4.z, w4.w, i);
-                float tx0 = __fmaf_rn(qlx, sx, ax), tx1 = __fmaf_rn(qhx, sx, ax);
-                float ty0 = __fmaf_rn(qly, sy, ay), ty1 = __fmaf_rn(qhy, sy, ay);
-                float tz0 = __fmaf_rn(qlz, sz, az), tz1 = __fmaf_rn(qhz, sz, az);
-                float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin_box));
-                float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tlimit));
-                bool hit = meta != 0u && tn <= tf * (1.0f + 2e-6f) + 1e-30f;
-                if (hit) {
-                    if (meta == 0x80u) {
-                        hits |= 1u << (i ^ flip);
-                    } else {
-                        uint32_t cnt = meta >> 5, off = meta & 31u;
-                        trimask |= ((1u << cnt) - 1u) << off;
-                    }
-                }
-            }
-            uint32_t tri_base = w1.y;
-            while (trimask) {
-                uint32_t bit = __ffs(trimask) - 1u;
-                trimask &= trimask - 1u;
-                if (tri_base + bit >= sc.ntri) { ok = false; continue; }
-                const float4* tp = sc.tri + 3u * (tri_base + bit);
-                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                int32_t prim = (int32_t)__float_as_uint(a.w);
-                float tt, b1, b2;
-                if (hit_triangle(rt, xyz(a), xyz(b), xyz(c), tmin, h.t, &tt, &b1, &b2)) {
-                    if (h.prim < 0 || tt < h.t || (tt == h.t && prim < h.prim)) {
-                        h.prim = prim; h.t = tt; h.b1 = b1; h.b2 = b2;
-                        if (ANY) return ok;
-                    }
-                }
-            }
-            if (hits) {
-                if (g_hits) {
-                    if (sp == kStackSize) { ok = false; }
-                    else stack[sp++] = make_uint2(g_base, g_hits | (g_imask << 8));
-                }
-                g_base = w1.x; g_hits = hits; g_imask = imask;
-            }
-        }
-        // ---- pick the next node ----
-        if (!g_hits) {
-            if (sp == 0) break;
-            uint2 e = stack[--sp];
-            g_base = e.x; g_hits = e.y & 0xFFu; g_imask = (e.y >> 8) & 0xFFu;
-        }
-        uint32_t k = __ffs(g_hits) - 1u;
-        g_hits &= g_hits - 1u;
-        uint32_t slot = k ^ flip;
-        node = g_base + __popc(g_imask & ((1u << slot) - 1u));
-    }
-    return ok;
 }
 
 }  // namespace xr

@@ -28,11 +28,27 @@ struct RayIn {
     float tmin, tmax;
 };
 
-// Byte k of `word` as an exact float: the byte becomes the low mantissa bits of
-// 2^23 (one byte permute), then 2^23 is subtracted -- no integer-to-float
-// conversion unit involved.
-__device__ __forceinline__ float qbyte(uint32_t word, uint32_t k) {
-    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7650u | k)) - 8388608.0f;
+// Byte k of `word` placed in mantissa bits 8..15 of 1.0f by one byte permute:
+// the result is exactly 1 + q / 32768.  A plane at q cells is then
+// t = q s + a = fma(1 + q / 32768, 32768 s, a - 32768 s), one instruction per
+// plane after the per-node constants; the extra rounding of a - 32768 s is
+// below 2^-9 of a cell, far inside the one-cell slack of the stored boxes.
+__device__ __forceinline__ float qplane(uint32_t word, uint32_t k) {
+    return __uint_as_float(__byte_perm(word, 0x3F800000u, 0x7604u | (k << 4)));
+}
+
+// Three-input minimum / maximum (PTX min.f32 / max.f32 with three sources,
+// sm_100 and later); like the two-input forms they return a non-NaN operand
+// when there is one, so a NaN plane drops out of the slab test.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 // LoadRay(i) -> RayIn; StoreHit(i, const HitRec&).  `next` is the fetch counter
@@ -116,12 +132,13 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 const uint4* np = reinterpret_cast<const uint4*>(sc.nodes + node);
                 const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
                             w4 = __ldg(np + 4);
-                const float sx = __uint_as_float((w0.w & 0xFFu) << 23) * idx;
-                const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * idy;
-                const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * idz;
-                const float ax = (__uint_as_float(w0.x) - o.x) * idx;
-                const float ay = (__uint_as_float(w0.y) - o.y) * idy;
-                const float az = (__uint_as_float(w0.z) - o.z) * idz;
+                // per axis: S = 32768 * 2^e / d and A = (p - o) / d - S (see qplane)
+                const float sx = __uint_as_float((w0.w & 0xFFu) << 23) * idx * 32768.0f;
+                const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * idy * 32768.0f;
+                const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * idz * 32768.0f;
+                const float ax = (__uint_as_float(w0.x) - o.x) * idx - sx;
+                const float ay = (__uint_as_float(w0.y) - o.y) * idy - sy;
+                const float az = (__uint_as_float(w0.z) - o.z) * idz - sz;
                 const float tlimit = h.t * (1.0f + 1e-6f) + 1e-30f;
                 // near and far quantised planes per axis, chosen once per node from the
                 // sign bits of the direction (a negative axis enters through the high plane)
@@ -132,27 +149,29 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 const uint32_t yf0 = ny ? w2.z : w4.x, yf1 = ny ? w2.w : w4.y;
                 const uint32_t zn0 = nz ? w4.z : w3.x, zn1 = nz ? w4.w : w3.y;
                 const uint32_t zf0 = nz ? w3.x : w4.z, zf1 = nz ? w3.y : w4.w;
-                uint32_t hits = 0, trimask = 0;
+                uint32_t hm = 0;   // bits 0..23 triangles, 24..31 internal children by slot
 #pragma unroll
                 for (uint32_t i = 0; i < 8; i++) {
-                    const uint32_t meta = byte_of(w1.z, w1.w, i);
-                    const float txn = __fmaf_rn(qbyte(i < 4 ? xn0 : xn1, i & 3u), sx, ax);
-                    const float txf = __fmaf_rn(qbyte(i < 4 ? xf0 : xf1, i & 3u), sx, ax);
-                    const float tyn = __fmaf_rn(qbyte(i < 4 ? yn0 : yn1, i & 3u), sy, ay);
-                    const float tyf = __fmaf_rn(qbyte(i < 4 ? yf0 : yf1, i & 3u), sy, ay);
-                    const float tzn = __fmaf_rn(qbyte(i < 4 ? zn0 : zn1, i & 3u), sz, az);
-                    const float tzf = __fmaf_rn(qbyte(i < 4 ? zf0 : zf1, i & 3u), sz, az);
-                    const float tn = fmaxf(fmaxf(txn, tyn), fmaxf(tzn, tmin_box));
-                    const float tf = fminf(fminf(txf, tyf), fminf(tzf, tlimit));
-                    if (meta != 0u && tn <= __fmaf_rn(tf, 1.0f + 2e-6f, 1e-30f)) {
-                        if (meta == 0x80u) hits |= 1u << (i ^ flip);
-                        else trimask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-                    }
+                    const uint32_t meta = __byte_perm(i < 4 ? w1.z : w1.w, 0u, 0x4440u | (i & 3u));
+                    const float txn = __fmaf_rn(qplane(i < 4 ? xn0 : xn1, i & 3u), sx, ax);
+                    const float txf = __fmaf_rn(qplane(i < 4 ? xf0 : xf1, i & 3u), sx, ax);
+                    const float tyn = __fmaf_rn(qplane(i < 4 ? yn0 : yn1, i & 3u), sy, ay);
+                    const float tyf = __fmaf_rn(qplane(i < 4 ? yf0 : yf1, i & 3u), sy, ay);
+                    const float tzn = __fmaf_rn(qplane(i < 4 ? zn0 : zn1, i & 3u), sz, az);
+                    const float tzf = __fmaf_rn(qplane(i < 4 ? zf0 : zf1, i & 3u), sz, az);
+                    const float tn = fmaxf(max3f(txn, tyn, tzn), tmin_box);
+                    const float tf = fminf(min3f(txf, tyf, tzf), tlimit);
+                    if (tn <= __fmaf_rn(tf, 1.0f + 2e-6f, 1e-30f)) hm |= __funnelshift_l(0u, meta >> 5, meta);
                 }
+                // internal hits from slot order to near-to-far order (bit k = slot k ^ flip)
+                uint32_t ih = hm >> 24;
+                if (flip & 1u) ih = ((ih & 0x55u) << 1) | ((ih >> 1) & 0x55u);
+                if (flip & 2u) ih = ((ih & 0x33u) << 2) | ((ih >> 2) & 0x33u);
+                if (flip & 4u) ih = ((ih & 0x0Fu) << 4) | ((ih >> 4) & 0x0Fu);
                 ng_base = w1.x;
-                ng_bits = hits | ((w0.w >> 24) << 8);
+                ng_bits = ih | ((w0.w >> 24) << 8);
                 tg_base = w1.y;
-                tg_mask = trimask;
+                tg_mask = hm & 0x00FFFFFFu;
             }
         }
 

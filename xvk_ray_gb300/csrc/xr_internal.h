@@ -47,9 +47,10 @@ constexpr uint32_t kMaxBounces = 31;
 //  w0: origin p.xyz, byte-packed {e.x, e.y, e.z (biased by 127), internal mask}
 //  w1: child_base, tri_base, meta[0..3], meta[4..7]
 //  w2..w4: q_lo.x[8], q_lo.y[8], q_lo.z[8], q_hi.x[8], q_hi.y[8], q_hi.z[8]
-// meta: 0 empty, 0x80 internal child, (count << 5) | offset for a leaf of 1..3
-// triangles at tri_base + offset.  Internal child in slot s is node
-// child_base + popc(imask & ((1 << s) - 1)).
+// meta byte = (bits << 5) | position: a hit child contributes bits << position
+// to one 32-bit mask.  Empty: 0.  Leaf of 1..3 triangles at tri_base + offset:
+// bits = 1, 3 or 7 (unary count), position = offset (0..23).  Internal child in
+// slot s: bits = 1, position = 24 + s; it is node child_base + popc(imask & ((1 << s) - 1)).
 struct alignas(16) WideNode {
     float px, py, pz;
     uint32_t exyz_imask;
