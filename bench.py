@@ -41,6 +41,9 @@ METRIC = "ms/frame 1080p & relMSE vs FP64 ref: plain ReSTIR GI vs ReSTIR GI+MLP 
 # reads G-buffer 16+4, candidate 16+16, previous G-buffer 4+16, previous reservoir 32; writes reservoir 32
 TEMPORAL_BYTES_PER_PX = 136
 SPATIAL_BYTES_PER_PX = 104   # reads G-buffer 16+4, candidate 16, reservoir 32; writes reservoir 32 + RGBA8 4
+# DRAM bytes (read + write) of one k_temporal launch at 1920x1080 measured with ncu
+# (profiles/k_temporal_1080p_1M_triangles.md): 179.5 MB + 44.0 MB
+TEMPORAL_DRAM_BYTES_1080P = 223.5e6
 
 
 def _peaks():
@@ -119,13 +122,19 @@ def _barrier(dist, local):
         torch.cuda.synchronize(local)
 
 
-def _max_over_ranks(dist, local, v: float) -> float:
+def _max_over_ranks(dist, v: float, device: str = "cpu") -> float:
+    """Largest value over the ranks (the slowest replica sets the job time)."""
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_ms_per_frame(max_rank_ms: float, steps: int, world: int) -> float:
+    """Replicas render `steps` frames each: job time per frame over all ranks' frames."""
+    return max_rank_ms / (steps * world)
 
 
 def camera_ubos(xr, scene, n_frames):
@@ -243,8 +252,8 @@ def run_ours(args):
     L.check(lib.xr_event_elapsed(r.ctx, 0, 1, C.byref(ms)), r.ctx)
     clk = clocks.stop()
     r.sync()
-    total_ms = _max_over_ranks(dist, local, float(ms.value))
-    ms_per_frame = total_ms / (args.steps * ws)
+    total_ms = _max_over_ranks(dist, float(ms.value), f"cuda:{local}")
+    ms_per_frame = whole_job_ms_per_frame(total_ms, args.steps, ws)
 
     # ---- per-pass breakdown (events inside the library, one frame at a time) ----
     t_init, t_temp, t_spat, rays, shadow = [], [], [], [], []
@@ -266,7 +275,7 @@ def run_ours(args):
         L.check(lib.xr_render_frame(r.ctx, C.byref(u)), r.ctx)
         L.check(lib.xr_read_output(r.ctx, L.XR_OUT_LDR8, out.ctypes.data, out.nbytes), r.ctx)
     e2e_ms = (time.perf_counter() - t0) * 1e3
-    e2e_ms = _max_over_ranks(dist, local, e2e_ms) / (args.steps * ws)
+    e2e_ms = whole_job_ms_per_frame(_max_over_ranks(dist, e2e_ms, f"cuda:{local}"), args.steps, ws)
     fi += args.steps
     img_mean = float(out.reshape(-1, 4)[:, :3].mean())
     pinned.free()
@@ -295,7 +304,8 @@ def run_ours(args):
         "rays_per_s": (rays_pf + shadow_pf) / ((ms_init + ms_spat) * 1e-3),
         "roofline": {"kernel": "temporal reuse (k_temporal)", "bound": "hbm", "achieved": round(temporal_gbs, 1),
                      "peak": hbm, "unit": "GB/s", "frac": round(temporal_gbs / hbm, 4),
-                     "traffic": None, "peak_source": peak_note,
+                     "traffic": TEMPORAL_DRAM_BYTES_1080P if (W, H) == (1920, 1080) else None,
+                     "traffic_unit": "bytes per launch (ncu)", "peak_source": peak_note,
                      "algorithmic_bytes_per_px": TEMPORAL_BYTES_PER_PX},
         "bvh": bvh,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": C.sizeof(L.XrUniformBufferObject),
