@@ -150,6 +150,37 @@ def camera_ubos(xr, scene, n_frames):
     return ubos
 
 
+RELMSE_EPS = 1e-2
+
+
+def relmse(img: "np.ndarray", ref: "np.ndarray") -> float:
+    """mean over pixels and channels of (x - r)^2 / (r^2 + 1e-2)."""
+    import numpy as np
+    x = img[:, :3].astype(np.float64)
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + RELMSE_EPS)))
+
+
+def measure_relmse(xr, scene, ubos, frames: int, ref_spp: int, device: int) -> dict:
+    """relMSE of plain ReSTIR GI and of the 1-spp path tracer after `frames` frames of
+    the camera path, against the FP64-accumulated reference of the last frame's camera."""
+    L = xr._lib
+    r = xr.Renderer(W, H, device=device)
+    r.set_params(xr.params_default(W, H, write_hdr=1, write_pt=1))
+    r.upload_scene(scene)
+    r.build_bvh()
+    for u in ubos[:frames]:
+        r.render(u)
+    hdr = r.read_output(L.XR_OUT_HDR)
+    pt = r.read_output(L.XR_OUT_PT)
+    t0 = time.perf_counter()
+    ref = r.render_reference(ubos[frames - 1], 1_000_000, ref_spp)
+    ref_s = time.perf_counter() - t0
+    r.close()
+    return {"restir_gi": relmse(hdr, ref), "pt_1spp": relmse(pt, ref), "restir_gi_mlp_cache": None,
+            "reference": f"FP64-accumulated path tracer, {ref_spp} spp, same path depth; frame {frames - 1}",
+            "eps": RELMSE_EPS, "reference_seconds": round(ref_s, 2)}
+
+
 def cpu_baseline(scene, ubos, seconds_budget: float = 20.0) -> dict:
     """The oracle on the host cores: whole frames of the same scene and camera
     path at 1/64 of the pixels (240x135), scaled to 1080p."""
@@ -284,6 +315,9 @@ def run_ours(args):
 
     if rank != 0:
         return
+    rel = None
+    if args.relmse_spp > 0:
+        rel = measure_relmse(xr, scene, ubos, min(24, len(ubos)), args.relmse_spp, local)
     peaks = _peaks()
     hbm = peaks.get("hbm_gbs")
     peak_note = "measured" if hbm else "fallback"
@@ -312,7 +346,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": W * H * 4},
         "gpu_launches": (BOUNCES + 2) * args.steps,
         "clocks": clk,
-        "relmse": None,
+        "relmse": rel,
         "image_mean_ldr": round(img_mean, 3),
         "device_error_flags": st.error_flags,
     }
@@ -329,6 +363,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--relmse-spp", type=int, default=1024, help="spp of the FP64 reference (0: skip relMSE)")
     ap.add_argument("--width", type=int, default=1920, help="smaller extents are for profiling only")
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--objects", type=int, default=4096, help="scene objects (4096 -> 998,442 triangles)")

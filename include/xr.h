@@ -158,6 +158,16 @@ xr_status xr_get_params(XrContext* ctx, XrParams* params);
         (src/pathTracer.cpp:169-201). ---- */
 xr_status xr_render_frame(XrContext* ctx, const XrUniformBufferObject* ubo);
 
+/* Converged reference: the plain path tracer with the initial-sample pass's path
+   semantics (shader/HLSL/ReSTIRGI/ReSTIRGIInitialSample.rgen.hlsl:41-181; the
+   reference's own multi-spp mode is shader/HLSL/rgen.hlsl:31-151) averaged over
+   `spp` samples with FP64 accumulation; sample k uses current_frame = frame0 + k
+   for its random numbers.  host_rgb receives width*height*3 doubles.  Needs
+   params.write_pt; overwrites the frame's G-buffer and candidates, so the next
+   xr_render_frame starts without temporal history. */
+xr_status xr_render_reference(XrContext* ctx, const XrUniformBufferObject* ubo, uint32_t frame0, uint32_t spp,
+                              double* host_rgb);
+
 /* Output images (the reference's OutputImage, ApplicationReSTIRGI.cpp:248-271). */
 enum {
     XR_OUT_LDR8 = 0,   /* width*height RGBA8: ACES + gamma 1/2.2 */

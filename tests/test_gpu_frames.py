@@ -102,3 +102,19 @@ def test_corrected_mode_procedural_ggx():
             o.render(u)
             _compare_frame(r, o, False, f"frame {f}")
         assert r.stats().shadow_rays > 0
+
+
+@pytest.mark.parametrize("compat", [False, True])
+def test_fp64_reference_matches_oracle(compat):
+    """xr_render_reference: FP64 accumulation, bit-identical to the oracle's."""
+    scene = xr.Scene.cornell()
+    W, H = 40, 32
+    p = (xr.params_reference if compat else xr.params_default)(W, H, write_pt=1)
+    ubo = camera_sequence(scene, W, H, 1, 4)[0]
+    with xr.Renderer(W, H) as r:
+        r.set_params(p)
+        r.upload_scene(scene)
+        r.build_bvh()
+        g = r.render_reference(ubo, 500, 16)
+    o = ob.pt_reference(ob.OracleScene.from_scene(scene), p, ubo, 500, 16)
+    assert np.array_equal(g.view(np.uint64), o.view(np.uint64))

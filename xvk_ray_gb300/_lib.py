@@ -114,6 +114,7 @@ _SIGS = {
     "xr_get_params": (_i32, [_P, C.POINTER(XrParams)]),
     "xr_render_frame": (_i32, [_P, C.POINTER(XrUniformBufferObject)]),
     "xr_read_output": (_i32, [_P, _u32, _P, C.c_size_t]),
+    "xr_render_reference": (_i32, [_P, C.POINTER(XrUniformBufferObject), _u32, _u32, _P]),
     "xr_output_device_ptr": (_i32, [_P, _u32, C.POINTER(_P)]),
     "xr_sync": (_i32, [_P]),
     "xr_get_stats": (_i32, [_P, C.POINTER(XrStats)]),

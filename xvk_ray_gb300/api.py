@@ -160,6 +160,12 @@ class Renderer:
         self._c(self._lib.xr_read_output(self.ctx, which, _ptr(out), out.nbytes))
         return out
 
+    def render_reference(self, ubo: L.XrUniformBufferObject, frame0: int, spp: int) -> np.ndarray:
+        """FP64-accumulated plain path tracer over `spp` samples: (width*height, 3) float64."""
+        out = np.empty((self.width * self.height, 3), np.float64)
+        self._c(self._lib.xr_render_reference(self.ctx, C.byref(ubo), frame0, spp, _ptr(out)))
+        return out
+
     def output_device_ptr(self, which: int = L.XR_OUT_LDR8) -> int:
         p = C.c_void_p()
         self._c(self._lib.xr_output_device_ptr(self.ctx, which, C.byref(p)))

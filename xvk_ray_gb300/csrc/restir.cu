@@ -732,6 +732,26 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
 // ---------------------------------------------------------------------------
 // conversion to and from the reference layouts (ReSTIRGICommon.hlsl:6-30)
 // ---------------------------------------------------------------------------
+// FP64 accumulation of one sample of the plain path tracer: the initial-sample
+// path's radiance, throughput0 * L_out for a surface seen directly, the emission
+// (or sky) otherwise -- the pixel value the reservoir passes estimate.
+__global__ void k_accumulate_sample(FrameArgs fa, double* __restrict__ acc) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    float3 v;
+    if (fa.compat) {
+        const bool valid = __float_as_uint(fa.s_xv[p].w) != kInvalid;
+        v = valid ? xyz(fa.thr0[p]) * xyz(fa.s_L[p]) : xyz(fa.le0[p]);
+    } else {
+        const float4 b = fa.cand_b[p];
+        const bool valid = fa.gb_mat_cur[p] != kInvalid, has = (__float_as_uint(b.w) >> 31) != 0u;
+        v = valid ? xyz(fa.thr0[p]) * (has ? xyz(b) : f3(0, 0, 0)) : xyz(b);
+    }
+    acc[3u * p + 0u] += (double)v.x;
+    acc[3u * p + 1u] += (double)v.y;
+    acc[3u * p + 2u] += (double)v.z;
+}
+
 __global__ void k_export_samples(FrameArgs fa, uint32_t* __restrict__ out) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
@@ -910,6 +930,10 @@ void launch_import_res_wide(float4* const planes[4], uint32_t n, const uint32_t*
 }
 void launch_import_res_packed(float4* p0, float4* p1, uint32_t n, const uint32_t* in, cudaStream_t st) {
     k_import_res_packed<<<(n + 255u) / 256u, 256, 0, st>>>(p0, p1, n, in);
+}
+
+void launch_accumulate_sample(const FrameArgs& fa, double* acc, cudaStream_t st) {
+    k_accumulate_sample<<<(fa.N + 255u) / 256u, 256, 0, st>>>(fa, acc);
 }
 
 void launch_spatial(const FrameArgs& fa, cudaStream_t st) {

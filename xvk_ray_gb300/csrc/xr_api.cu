@@ -392,6 +392,39 @@ xr_status xr_render_frame(XrContext* c, const XrUniformBufferObject* ubo) {
     return cuda_check(c, cudaGetLastError(), "render_frame launch");
 }
 
+xr_status xr_render_reference(XrContext* c, const XrUniformBufferObject* ubo, uint32_t frame0, uint32_t spp,
+                              double* host_rgb) {
+    if (!c || !ubo || !host_rgb || spp == 0) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_reference: bad argument");
+    if (!c->params_set || !c->bvh_ready) return fail(c, XR_ERR_STATE, "render_reference: parameters and BVH required");
+    if (!c->params.write_pt) return fail(c, XR_ERR_STATE, "render_reference: set write_pt in the parameters");
+    if (ubo->number_of_bounces > kMaxBounces) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_reference: too many bounces");
+    if (c->params.compat_reference && c->scene_has_non_lambert)
+        return fail(c, XR_ERR_UNSUPPORTED, "render_reference: reference mode renders only Lambertian and DiffuseLight materials");
+    DeviceGuard g(c->device);
+    const size_t n3 = (size_t)c->N * 3;
+    double* acc = nullptr;
+    xr_status s = cuda_check(c, cudaMalloc((void**)&acc, n3 * sizeof(double)), "render_reference alloc");
+    if (s) return s;
+    cudaMemsetAsync(acc, 0, n3 * sizeof(double), c->stream);
+    XrUniformBufferObject u = *ubo;
+    for (uint32_t k = 0; k < spp && !s; k++) {
+        u.current_frame = frame0 + k;
+        if ((s = upload_ubo(c, &u))) break;
+        set_frame_pointers(c, u.current_frame % 2u);
+        cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);
+        launch_initial(c->fa, u.number_of_bounces, c->stream);
+        launch_accumulate_sample(c->fa, acc, c->stream);
+        s = cuda_check(c, cudaGetLastError(), "render_reference launch");
+    }
+    if (!s) s = cuda_check(c, cudaMemcpyAsync(host_rgb, acc, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                           "render_reference copy");
+    if (!s) s = xr_sync(c);
+    cudaFree(acc);
+    if (s) return s;
+    for (size_t i = 0; i < n3; i++) host_rgb[i] /= (double)spp;
+    return XR_OK;
+}
+
 xr_status xr_sync(XrContext* c) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "sync: null context");
     DeviceGuard g(c->device);

@@ -168,6 +168,7 @@ void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_
 void launch_initial(const FrameArgs& fa, uint32_t number_of_bounces, cudaStream_t st);
 void launch_temporal(const FrameArgs& fa, bool write_image, cudaStream_t st);
 void launch_spatial(const FrameArgs& fa, cudaStream_t st);
+void launch_accumulate_sample(const FrameArgs& fa, double* acc, cudaStream_t st);
 void launch_export_samples(const FrameArgs& fa, uint32_t* out, cudaStream_t st);
 void launch_import_samples(const FrameArgs& fa, const uint32_t* in, cudaStream_t st);
 void launch_export_res_wide(float4* const planes[4], uint32_t n, uint32_t* out, cudaStream_t st);
