@@ -44,6 +44,14 @@ SPATIAL_BYTES_PER_PX = 104   # reads G-buffer 16+4, candidate 16, reservoir 32; 
 # DRAM bytes (read + write) of one k_temporal launch at 1920x1080 measured with ncu
 # (profiles/k_temporal_1080p_1M_triangles.md): 179.5 MB + 44.0 MB
 TEMPORAL_DRAM_BYTES_1080P = 223.5e6
+# kernels per frame: raygen, (trace + shade) per bounce, temporal, spatial select,
+# shadow trace, spatial resolve
+FRAME_LAUNCHES = 1 + 2 * BOUNCES + 4
+
+
+def workload(frames: int) -> str:
+    return (f"procedural 1920x1080, 998442 triangles, {frames}-frame camera path, corrected ReSTIR GI "
+            "(M cap 20, 5 neighbours, 30 px, shadow rays), depth 4")
 
 
 def _peaks():
@@ -235,8 +243,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms/frame", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "procedural 1920x1080, 998442 triangles, 32-frame camera path, corrected ReSTIR GI "
-                                   "(M cap 20, 5 neighbours, 30 px, shadow rays), depth 4",
+            "config": {"workload": workload(args.steps),
                        "sample": f"{sw}x{sh} per step, scaled x{scale:.0f}"},
             "cpu_baseline": {"value": v, "unit": "ms/frame", "cores": cores, "kind": "port",
                              "sample": f"{args.steps} frames at {sw}x{sh} (1/64 of the pixels), scaled to 1080p; "
@@ -328,8 +335,7 @@ def run_ours(args):
         "metric": METRIC, "value": round(ms_per_frame, 4), "unit": "ms/frame", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_frame, 4), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seed 1)",
-        "config": {"workload": "procedural 1920x1080, 998442 triangles, 32-frame camera path, corrected ReSTIR GI "
-                               "(M cap 20, 5 neighbours, 30 px, shadow rays), depth 4",
+        "config": {"workload": workload(args.steps),
                    "resolution": [W, H], "triangles": scene.n_triangles, "bounces": BOUNCES,
                    "l2": "per-frame working set 0.66 GB > 129 MB L2 (no flush needed); BVH stays L2-resident",
                    "parallelism": f"replicas x{ws}"},
@@ -344,7 +350,7 @@ def run_ours(args):
         "bvh": bvh,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": C.sizeof(L.XrUniformBufferObject),
                 "d2h_bytes_per_step": W * H * 4},
-        "gpu_launches": (BOUNCES + 2) * args.steps,
+        "gpu_launches": FRAME_LAUNCHES * args.steps,
         "clocks": clk,
         "relmse": rel,
         "image_mean_ldr": round(img_mean, 3),
@@ -358,7 +364,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=32)
+    ap.add_argument("--steps", type=int, default=240)
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

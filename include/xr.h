@@ -128,6 +128,7 @@ typedef struct XrStats {
     uint64_t query_rays;         /* rays of the last xr_trace_rays call */
     uint64_t query_node_visits;  /* BVH nodes visited by those rays */
     uint64_t query_tri_tests;    /* triangle tests of those rays */
+    uint64_t nonfinite_rays;     /* rays of the last frame ended as misses for a non-finite origin/direction */
 } XrStats;
 enum { XR_DEVFLAG_STACK_OVERFLOW = 1u, XR_DEVFLAG_QUEUE_OVERFLOW = 2u, XR_DEVFLAG_BAD_INDEX = 4u };
 

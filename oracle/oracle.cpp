@@ -938,6 +938,7 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         }
         jac = fminf(fmaxf(jac, 0.1f), 10.0f);
         float ph = p_hat_of(r_nb.s.L_out) * jac;
+        bool occluded = false;
         if (!compat && R.P.visibility && ph > 0.0f) {
             // corrected CheckVisibility (ReSTIRGISpatialReuse.rgen.hlsl:44-62): from
             // the centre pixel's visible point, not the selected sample's
@@ -946,10 +947,14 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
             float dist = length(dir);
             f3 ro = from + s_new.n_view * 0.01f;
             Hit hh = trace(*R.sc, ro, normalize(dir), 0.0f, dist - 0.01f, true);
-            if (hh.prim >= 0) ph = 0.0f;
+            occluded = hh.prim >= 0;
+            if (occluded) ph = 0.0f;
         }
         merge_reservoir(r_s, r_nb, ph, rng);
-        if (ph == 0.0f) r_s.m -= r_nb.m;
+        // reference: a neighbour whose weight is zero does not count towards M
+        // (ReSTIRGISpatialReuse.rgen.hlsl:140-143); corrected: every similar
+        // neighbour counts (1/M normalisation) except one whose sample is occluded
+        if (compat ? ph == 0.0f : occluded) r_s.m -= r_nb.m;
     }
     if (compat) {
         r_s.m = std::min(r_s.m, 300u);

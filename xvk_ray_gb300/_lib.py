@@ -75,7 +75,8 @@ class XrStats(C.Structure):
                 ("ms_temporal", C.c_float), ("ms_spatial", C.c_float), ("ms_frame", C.c_float),
                 ("rays_traced", C.c_uint64), ("shadow_rays", C.c_uint64), ("bvh_nodes", C.c_uint32),
                 ("bvh_triangles", C.c_uint32), ("bvh_depth", C.c_uint32), ("ms_bvh_build", C.c_float),
-                ("query_rays", C.c_uint64), ("query_node_visits", C.c_uint64), ("query_tri_tests", C.c_uint64)]
+                ("query_rays", C.c_uint64), ("query_node_visits", C.c_uint64), ("query_tri_tests", C.c_uint64),
+                ("nonfinite_rays", C.c_uint64)]
 
 
 class XrCamera(C.Structure):

@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 // ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
 __global__ void __launch_bounds__(kBlock) k_trace_paths(DeviceScene sc, const float4* __restrict__ q0,
                                                         const float4* __restrict__ q1, uint4* __restrict__ hits,
-                                                        const uint32_t* count_ptr, uint32_t* next, uint32_t* err) {
+                                                        const uint32_t* count_ptr, uint32_t* next, uint32_t* err,
+                                                        uint32_t* nonfinite) {
     const uint32_t count = *(volatile const uint32_t*)count_ptr;
     trace_persistent<false>(
         sc, count, next,
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_paths(DeviceScene sc, const fl
         [&](uint32_t i, const HitRec& h) {
             hits[i] = make_uint4((uint32_t)h.prim, __float_as_uint(h.t), __float_as_uint(h.b1), __float_as_uint(h.b2));
         },
-        err);
+        err, nullptr, nonfinite);
 }
 
 // Shading of one bounce over the queue (persistent grid): coherent per-path
@@ -677,7 +678,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_shadow(FrameArgs fa) {
                 atomicOr(&fa.occ[owner >> 5], 1u << (owner & 31u));
             }
         },
-        &fa.counters[kCntError]);
+        &fa.counters[kCntError], nullptr, &fa.counters[kCntNonFinite]);
 }
 
 // Spatial reuse, step 3 of 3: the merge of ReSTIRGISpatialReuse.rgen.hlsl:91-176
@@ -715,9 +716,13 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
         Res rn; load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
         float jac = jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
         float ph = length(rn.L) * jac;
-        if (ph > 0.0f && ((occ >> i) & 1u)) ph = 0.0f;
+        const bool occluded = ph > 0.0f && ((occ >> i) & 1u);
+        if (occluded) ph = 0.0f;
         res_merge(r, rn, ph, rng);
-        if (ph == 0.0f) r.m -= rn.m;
+        // every similar neighbour counts towards M (1/M normalisation) except one
+        // whose sample is occluded; the reference also drops zero-weight neighbours
+        // (ReSTIRGISpatialReuse.rgen.hlsl:140-143), which biases the estimate upwards
+        if (occluded) r.m -= rn.m;
     }
     if (r.m > fa.m_cap_s) {
         r.w_sum *= (float)fa.m_cap_s / (float)r.m;
@@ -899,7 +904,8 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
         // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
         k_trace_paths<<<fa.grid_trace, kBlock, 0, st>>>(fa.sc, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
-                                                        fa.counters + kCntFetchPath + b, fa.counters + kCntError);
+                                                        fa.counters + kCntFetchPath + b, fa.counters + kCntError,
+                                                        fa.counters + kCntNonFinite);
         if (fa.compat) k_shade<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
         else k_shade<false><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
     }

@@ -22,6 +22,7 @@ namespace xr {
 
 constexpr uint32_t kTriGroupBit = 0x80000000u;   // stack entry holds a triangle group
 constexpr int kPostponeBelow = 12;                // lanes; fewer testing triangles -> postpone
+constexpr float kMinDir = 1e-20f;                 // smallest direction component seen by the box test
 
 struct RayIn {
     float3 o, d;
@@ -54,13 +55,14 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // LoadRay(i) -> RayIn; StoreHit(i, const HitRec&).  `next` is the fetch counter
 // (zeroed before the launch), `count` the number of rays, `err` the error word.
 // With `work` non-null (query kernels only) the node visits and triangle tests
-// are summed into work[0] and work[1].
+// are summed into work[0] and work[1]; with `nonfinite` non-null, the rays ended
+// early for a non-finite origin or direction are counted there.
 template <bool ANY, typename LoadRay, typename StoreHit>
 __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t count, uint32_t* next,
                                                  LoadRay load, StoreHit store, uint32_t* err,
-                                                 unsigned long long* work = nullptr) {
+                                                 unsigned long long* work = nullptr, uint32_t* nonfinite = nullptr) {
     const uint32_t FULL = 0xFFFFFFFFu;
-    uint32_t n_visits = 0, n_tests = 0;
+    uint32_t n_visits = 0, n_tests = 0, n_nonfinite = 0;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
     bool active = false, drained = false;
@@ -96,7 +98,17 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     o = r.o;
                     tmin = r.tmin;
                     tmin_box = r.tmin * (1.0f - 1e-6f) - 1e-30f;
-                    idx = 1.0f / r.d.x; idy = 1.0f / r.d.y; idz = 1.0f / r.d.z;
+                    // Box-test reciprocals of the direction with each component kept at
+                    // least kMinDir in magnitude (sign kept): an exactly zero component
+                    // would give an infinite reciprocal, and inf - inf in the per-node
+                    // plane constants below is NaN, which drops that axis from every slab
+                    // test and walks the whole tree.  The box test then follows a ray that
+                    // departs from the true one by at most kMinDir * t, far inside the
+                    // one-cell slack of the stored boxes, so no box holding a hit is culled;
+                    // the triangle test uses the true direction.
+                    idx = 1.0f / copysignf(fmaxf(fabsf(r.d.x), kMinDir), r.d.x);
+                    idy = 1.0f / copysignf(fmaxf(fabsf(r.d.y), kMinDir), r.d.y);
+                    idz = 1.0f / copysignf(fmaxf(fabsf(r.d.z), kMinDir), r.d.z);
                     rt = prep_ray(r.o, r.d);
                     // sign bits (so that -0 selects the same planes as its infinite reciprocal)
                     flip = (__float_as_uint(r.d.x) >> 31) | ((__float_as_uint(r.d.y) >> 31) << 1) |
@@ -108,6 +120,14 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     // a virtual group whose only child is the root (node 0)
                     ng_base = 0;
                     ng_bits = sc.n_nodes ? (1u | ((1u << flip) << 8)) : 0u;
+                    // A non-finite origin or direction (or a zero direction) can hit
+                    // nothing -- every triangle test fails -- but would make every box
+                    // test pass through NaN slabs and walk the whole tree: end it as a miss.
+                    const float chk = r.o.x + r.o.y + r.o.z + r.d.x + r.d.y + r.d.z;
+                    if (!isfinite(chk) || (r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f)) {
+                        ng_bits = 0u;
+                        n_nonfinite++;
+                    }
                 }
             }
         }
@@ -222,6 +242,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
         }
     }
     if (__any_sync(FULL, bad) && bad) atomicOr(err, (uint32_t)XR_DEVFLAG_STACK_OVERFLOW);
+    if (n_nonfinite && nonfinite) atomicAdd(nonfinite, n_nonfinite);
     if (work) {
         atomicAdd(&work[0], (unsigned long long)n_visits);
         atomicAdd(&work[1], (unsigned long long)n_tests);

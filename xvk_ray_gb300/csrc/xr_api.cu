@@ -481,6 +481,7 @@ xr_status xr_get_stats(XrContext* c, XrStats* st) {
         o.rays_traced = 0;
         for (uint32_t b = 0; b < c->last_bounces && b <= kMaxBounces; b++) o.rays_traced += cnt[b];
         o.shadow_rays = cnt[kCntShadow];
+        o.nonfinite_rays = cnt[kCntNonFinite];
     }
     o.bvh_nodes = c->n_nodes; o.bvh_triangles = c->n_tri_slots; o.bvh_depth = c->bvh_depth;
     o.ms_bvh_build = c->ms_bvh;

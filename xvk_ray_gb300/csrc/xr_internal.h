@@ -39,6 +39,7 @@ constexpr uint32_t kCntShadow = 32;        // shadow rays queued by the spatial 
 constexpr uint32_t kCntFetchPath = 64;     // + bounce: ray-fetch counter of that bounce's trace
 constexpr uint32_t kCntFetchShadow = 96;   // ray-fetch counter of the shadow trace
 constexpr uint32_t kCntFetchQuery = 97;    // ray-fetch counter of xr_trace_rays
+constexpr uint32_t kCntNonFinite = 98;     // rays ended early for a non-finite origin or direction
 constexpr uint32_t kCntError = 127;        // sticky XR_DEVFLAG_* bits
 constexpr uint32_t kCounterWords = 128;
 constexpr uint32_t kMaxBounces = 31;
