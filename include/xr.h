@@ -130,7 +130,8 @@ typedef struct XrStats {
     uint64_t query_tri_tests;    /* triangle tests of those rays */
     uint64_t nonfinite_rays;     /* rays of the last frame ended as misses for a non-finite origin/direction */
 } XrStats;
-enum { XR_DEVFLAG_STACK_OVERFLOW = 1u, XR_DEVFLAG_QUEUE_OVERFLOW = 2u, XR_DEVFLAG_BAD_INDEX = 4u };
+enum { XR_DEVFLAG_STACK_OVERFLOW = 1u, XR_DEVFLAG_QUEUE_OVERFLOW = 2u, XR_DEVFLAG_BAD_INDEX = 4u,
+       XR_DEVFLAG_MMA_TIMEOUT = 8u /* a tensor-core completion wait of the radiance cache gave up (1 s) */ };
 
 /* ---- lifetime: replaces Application/ApplicationRT/ApplicationReSTIRGI construction
         (src/Vulkan/RayTracing/ApplicationReSTIRGI.cpp:25-29) ---- */
@@ -260,6 +261,75 @@ xr_status xr_scene_procedural(const XrProceduralDesc* desc, XrSceneData* out);
 /* Page-locked host memory for the read-back images (cudaMallocHost). */
 xr_status xr_alloc_host(size_t bytes, void** ptr);
 void xr_free_host(void* ptr);
+
+/* ---- learned radiance cache ----
+   No counterpart in the reference renderer (it has no learned component): the
+   cache of Mueller et al., "Real-time Neural Radiance Caching for Path Tracing"
+   (SIGGRAPH 2021) over the multiresolution hash encoding of "Instant Neural
+   Graphics Primitives" (SIGGRAPH 2022).  16 levels x 2 features x 2^19 binary16
+   entries (resolutions 16 ... 2048 over the scene cube), inputs position,
+   normal, direction, roughness, albedo, material kind -> 4 x 64 ReLU layers ->
+   RGB; bfloat16 weights, FP32 accumulation on the tensor cores; Adam.
+   With `enabled`, corrected-mode paths end at their first secondary vertex x_s
+   and the ReSTIR GI candidate takes L_out = Le(x_s) + cache(x_s); the
+   `train_samples` training paths of a frame continue to full depth and their
+   suffix radiance at x_s is the training target (relative L2 loss); one Adam
+   step per frame when `train` is set.  xr_render_reference never uses the cache. */
+typedef struct XrCacheParams {
+    uint32_t enabled;            /* paths terminate into the cache (corrected mode only) */
+    uint32_t train;              /* one Adam step per rendered frame */
+    uint32_t train_samples;      /* training paths per frame, <= 1,048,576 (default 65,536) */
+    float learning_rate;         /* Adam step size (default 1e-2) */
+    float beta1, beta2, epsilon; /* Adam (defaults 0.9, 0.99, 1e-15) */
+    uint32_t seed;               /* parameter initialisation used by xr_cache_reset */
+} XrCacheParams;
+
+/* One cache sample (queries and training through the API).  kind = material
+   model (XR_MAT_*): 1 and 5 set the metal and plastic inputs.  72 bytes. */
+typedef struct XrCacheSample {
+    float pos[3];
+    float normal[3];
+    float wo[3];                 /* unit direction from pos towards the previous path vertex */
+    float albedo[3];
+    float roughness;
+    uint32_t kind;
+    float target[3];             /* outgoing radiance (training only) */
+    uint32_t pixel;              /* carried through, unused by the API calls */
+} XrCacheSample;
+
+typedef struct XrCacheStats {
+    uint32_t steps;              /* Adam steps taken since the last reset */
+    uint32_t queries;            /* cache queries of the last frame */
+    uint32_t train_samples;      /* training samples of the last frame (before rounding to 128) */
+    float loss;                  /* mean relative L2 loss of the last training step */
+    float ms_infer, ms_train;    /* last frame: inference, training + Adam (CUDA events) */
+    float bounds_lo[3];          /* scene cube: unit position = (x - lo) * inv_extent */
+    float inv_extent;
+} XrCacheStats;
+
+enum { XR_CACHE_MLP = 0, XR_CACHE_GRID = 1, XR_CACHE_MLP_GRAD = 2, XR_CACHE_GRID_GRAD = 3,
+       XR_CACHE_MLP_M = 4, XR_CACHE_MLP_V = 5, XR_CACHE_GRID_M = 6, XR_CACHE_GRID_V = 7,
+       XR_CACHE_QUERIES = 8,        /* last frame's query records, 8 words each */
+       XR_CACHE_TRAIN_RECORDS = 9   /* last frame's training records, 12 words each */ };
+/* MLP arrays: 17,408 floats, layer l < 4 at l * 4096 as [64 out][64 in], layer 4 at
+   16384 as [16 out][64 in] (outputs 3..15 unused).  Table arrays: 16 x 2^19 x 2
+   floats, level-major, 2 features per entry (the binary16 table is derived). */
+
+void xr_cache_params_default(XrCacheParams* out);
+xr_status xr_cache_set_params(XrContext* ctx, const XrCacheParams* p);   /* allocates ~0.3 GB on first use */
+xr_status xr_cache_get_params(XrContext* ctx, XrCacheParams* out);
+xr_status xr_cache_reset(XrContext* ctx, uint32_t seed);               /* re-initialise weights, table, Adam state */
+xr_status xr_cache_set_bounds(XrContext* ctx, const float lo[3], float inv_extent);
+/* Predicted outgoing radiance of n samples (host arrays). */
+xr_status xr_cache_query(XrContext* ctx, const XrCacheSample* s, uint32_t n, float* out_rgb);
+/* Gradients of the mean relative L2 loss over n samples (n a multiple of 128,
+   <= 1,048,576); with apply != 0 followed by one Adam step.  *loss may be NULL. */
+xr_status xr_cache_train(XrContext* ctx, const XrCacheSample* s, uint32_t n, int apply, float* loss);
+/* One Adam step on the current gradients (e.g. written with xr_cache_write), which it then zeroes. */
+xr_status xr_cache_step(XrContext* ctx);
+xr_status xr_cache_read(XrContext* ctx, int which, void* host, size_t bytes, size_t* bytes_needed);
+xr_status xr_cache_write(XrContext* ctx, int which, const void* host, size_t bytes);   /* arrays 0..7 */
+xr_status xr_cache_get_stats(XrContext* ctx, XrCacheStats* out);
 
 const char* xr_last_error(const XrContext* ctx);   /* ctx may be NULL: last global error */
 uint32_t xr_api_version(void);

@@ -13,6 +13,7 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 
 BUF_SAMPLES, BUF_TEMPORAL, BUF_SPATIAL, BUF_HDR, BUF_LDR, BUF_PT, BUF_GBUF_POS, BUF_MOTION, BUF_WRITTEN = range(9)
+BUF_CACHE_QUERIES, BUF_CACHE_TRAIN = 9, 10
 
 _lib = None
 
@@ -35,6 +36,7 @@ def load():
             "or_trace": (None, [P, P, u32, C.c_int, P, P, P]),
             "or_renderer_create": (P, [P, P]),
             "or_renderer_destroy": (None, [P]),
+            "or_renderer_set_cache": (C.c_int, [P, C.c_int, u32, P]),
             "or_render_frame": (C.c_int, [P, P]),
             "or_set_samples": (C.c_int, [P, P, P]),
             "or_end_frame": (C.c_int, [P]),
@@ -42,6 +44,16 @@ def load():
             "or_read": (C.c_size_t, [P, C.c_int, P, C.c_size_t]),
             "or_write_temporal": (C.c_int, [P, P, C.c_size_t]),
             "or_pt_reference": (C.c_int, [P, P, P, u32, u32, P]),
+            "or_nrc_create": (P, [u32]),
+            "or_nrc_destroy": (None, [P]),
+            "or_nrc_set_bounds": (None, [P, P, C.c_float]),
+            "or_nrc_params": (C.POINTER(C.c_float), [P, C.c_int, C.POINTER(C.c_size_t)]),
+            "or_nrc_pack": (None, [P, u32, P]),
+            "or_nrc_inputs": (None, [P, P, u32, P, C.c_int]),
+            "or_nrc_infer": (None, [P, P, u32, P, C.c_int]),
+            "or_nrc_backward": (C.c_double, [P, P, P, u32, C.c_int, C.c_int]),
+            "or_nrc_loss": (C.c_double, [P, P, P, u32, C.c_int, C.c_int]),
+            "or_nrc_adam": (None, [P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -158,7 +170,17 @@ class OracleRenderer:
             return raw.reshape(-1, 4)
         if which == BUF_MOTION:
             return raw.view(np.float32).reshape(-1, 2)
+        if which == BUF_CACHE_QUERIES:
+            return raw.view(np.uint32).reshape(-1, 8)
+        if which == BUF_CACHE_TRAIN:
+            return raw.view(np.uint32).reshape(-1, 12)
         return raw.view(np.uint32)
+
+    def set_cache(self, enabled: bool, train_samples: int = 65536, cache: "OracleCache | None" = None):
+        rc = load().or_renderer_set_cache(self.h, int(enabled), train_samples, cache.h if cache else None)
+        if rc:
+            raise ValueError("the radiance cache runs in corrected mode only")
+        self._cache = cache   # keep the cache alive while the renderer uses it
 
     def close(self):
         if self.h:
@@ -176,3 +198,70 @@ def pt_reference(scene: OracleScene, params, ubo, frame0: int, spp: int) -> np.n
     out = np.empty((params.width * params.height, 3), np.float64)
     load().or_pt_reference(scene.h, _bytes_of(params), _bytes_of(ubo), frame0, spp, _p(out))
     return out
+
+
+# ---- learned radiance cache (nrc.cpp) ----
+# XrCacheSample / OrCacheSample: pos[3] normal[3] wo[3] albedo[3] roughness kind target[3] pixel (72 B)
+CACHE_SAMPLE_DTYPE = np.dtype([("pos", "<f4", 3), ("normal", "<f4", 3), ("wo", "<f4", 3), ("albedo", "<f4", 3),
+                               ("roughness", "<f4"), ("kind", "<u4"), ("target", "<f4", 3), ("pixel", "<u4")])
+NRC_MLP, NRC_GRID, NRC_MLP_GRAD, NRC_GRID_GRAD, NRC_MLP_M, NRC_MLP_V, NRC_GRID_M, NRC_GRID_V = range(8)
+
+
+def pack_cache_samples(samples: np.ndarray) -> np.ndarray:
+    s = np.ascontiguousarray(samples, CACHE_SAMPLE_DTYPE)
+    rec = np.empty((len(s), 8), np.uint32)
+    load().or_nrc_pack(_p(s.view(np.uint8)), len(s), _p(rec))
+    return rec
+
+
+class OracleCache:
+    """CPU restatement of the learned radiance cache (hash grid + MLP + Adam)."""
+
+    def __init__(self, seed: int = 1):
+        self.h = load().or_nrc_create(seed)
+
+    def set_bounds(self, lo, inv_extent: float):
+        lo = np.ascontiguousarray(lo, np.float32)
+        load().or_nrc_set_bounds(self.h, _p(lo), float(inv_extent))
+
+    def param(self, which: int) -> np.ndarray:
+        """A live view of one parameter / gradient / moment array."""
+        n = C.c_size_t()
+        ptr = load().or_nrc_params(self.h, which, C.byref(n))
+        return np.ctypeslib.as_array(ptr, shape=(n.value,))
+
+    def inputs(self, records: np.ndarray, exact: bool = False) -> np.ndarray:
+        r = np.ascontiguousarray(records, np.uint32)
+        x = np.empty((len(r), 64), np.float32)
+        load().or_nrc_inputs(self.h, _p(r), len(r), _p(x), int(exact))
+        return x
+
+    def infer(self, records: np.ndarray, exact: bool = False) -> np.ndarray:
+        r = np.ascontiguousarray(records, np.uint32)
+        out = np.empty((len(r), 3), np.float32)
+        load().or_nrc_infer(self.h, _p(r), len(r), _p(out), int(exact))
+        return out
+
+    def backward(self, records, targets, exact: bool = False, loss_kind: int = 0) -> float:
+        r = np.ascontiguousarray(records, np.uint32)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, 3)
+        return load().or_nrc_backward(self.h, _p(r), _p(t), len(r), int(exact), loss_kind)
+
+    def loss(self, records, targets, exact: bool = False, loss_kind: int = 0) -> float:
+        r = np.ascontiguousarray(records, np.uint32)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, 3)
+        return load().or_nrc_loss(self.h, _p(r), _p(t), len(r), int(exact), loss_kind)
+
+    def adam(self, lr, b1, b2, eps, bc1, bc2):
+        load().or_nrc_adam(self.h, lr, b1, b2, eps, bc1, bc2)
+
+    def close(self):
+        if self.h:
+            load().or_nrc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -8,6 +8,7 @@
 // (recipe in oracle/Makefile).  -ffp-contract=off is load-bearing: every
 // expression below is evaluated as written, one rounding per operation.
 #include "xr_oracle.h"
+#include "common.h"
 
 #include <algorithm>
 #include <cmath>
@@ -17,27 +18,8 @@
 
 namespace {
 
-// ----------------------------------------------------------------------------
-// vector types and IEEE-exact helpers
-// ----------------------------------------------------------------------------
-struct f2 { float x, y; };
-struct f3 { float x, y, z; };
-struct f4 { float x, y, z, w; };
-
-inline f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-inline f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
-inline f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-inline f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-inline f3 operator/(f3 a, f3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
-inline float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline float length(f3 a) { return sqrtf(dot(a, a)); }
-inline f3 normalize(f3 a) { float r = 1.0f / sqrtf(dot(a, a)); return a * r; }
-inline f3 cross(f3 a, f3 b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-inline float comp(f3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
-inline f3 xyz(f4 v) { return {v.x, v.y, v.z}; }
+// vector types, IEEE-exact helpers, Wang hash, octahedral codes: common.h
+using namespace xro;
 
 // HLSL mul(M, v) with a glm column-major matrix: out_r = sum_c M[c][r] v_c,
 // summed left to right.
@@ -112,15 +94,6 @@ inline uint32_t next_random(uint32_t& state) {
 inline float random_float(uint32_t& state) {
     return (float)(next_random(state) & 0x00FFFFFFu) / 16777216.0f;
 }
-// Integer mix (same steps as the Wang hash in init_random_seed).
-inline uint32_t wang(uint32_t s) {
-    s = (s ^ 61u) ^ (s >> 16);
-    s *= 9u;
-    s = s ^ (s >> 4);
-    s *= 0x27d4eb2du;
-    s = s ^ (s >> 15);
-    return s;
-}
 enum { PASS_INITIAL = 0, PASS_TEMPORAL = 1, PASS_SPATIAL = 2 };
 // Reference: every pass reseeds with InitRandomSeed(pixel, frame) (quirk kept in
 // compatibility mode).  Corrected mode decorrelates passes and mixes the seed.
@@ -129,44 +102,6 @@ inline uint32_t pass_rng(bool compat, uint32_t x, uint32_t y, uint32_t w, uint32
     uint32_t s = init_random_seed(x, y, w, frame);
     if (compat) return s;
     return s ^ wang(frame * 0x9E3779B9u + pass * 0x85EBCA6Bu + seed * 0xC2B2AE35u);
-}
-
-// ----------------------------------------------------------------------------
-// Octahedral unit-vector codes used by the corrected-mode storage layout.
-// bits = 16: 16+16 bits; bits = 12: 12+12 bits in the low 24 bits.
-// ----------------------------------------------------------------------------
-inline float sgn_nz(float v) { return v >= 0.0f ? 1.0f : -1.0f; }
-inline uint32_t oct_encode(f3 n, uint32_t bits) {
-    float l1 = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
-    float u = n.x / l1, v = n.y / l1;
-    if (n.z < 0.0f) {
-        float ou = (1.0f - fabsf(v)) * sgn_nz(u);
-        float ov = (1.0f - fabsf(u)) * sgn_nz(v);
-        u = ou; v = ov;
-    }
-    float scale = (float)((1u << (bits - 1)) - 1u);
-    u = fminf(fmaxf(u, -1.0f), 1.0f);
-    v = fminf(fmaxf(v, -1.0f), 1.0f);
-    int32_t qu = (int32_t)rintf(u * scale);
-    int32_t qv = (int32_t)rintf(v * scale);
-    uint32_t mask = (1u << bits) - 1u;
-    return ((uint32_t)qu & mask) | (((uint32_t)qv & mask) << bits);
-}
-inline f3 oct_decode(uint32_t code, uint32_t bits) {
-    uint32_t mask = (1u << bits) - 1u;
-    int32_t qu = (int32_t)(code & mask), qv = (int32_t)((code >> bits) & mask);
-    int32_t half = 1 << (bits - 1);
-    if (qu >= half) qu -= (1 << bits);
-    if (qv >= half) qv -= (1 << bits);
-    float scale = (float)((1u << (bits - 1)) - 1u);
-    float u = (float)qu / scale, v = (float)qv / scale;
-    float z = 1.0f - fabsf(u) - fabsf(v);
-    if (z < 0.0f) {
-        float ou = (1.0f - fabsf(v)) * sgn_nz(u);
-        float ov = (1.0f - fabsf(u)) * sgn_nz(v);
-        u = ou; v = ov;
-    }
-    return normalize(f3{u, v, z});
 }
 
 // ----------------------------------------------------------------------------
@@ -625,7 +560,24 @@ struct Renderer {
     std::vector<f4> hdr, pt;
     std::vector<uint8_t> ldr;
     std::vector<uint32_t> written;
+    // learned radiance cache (corrected mode, or_renderer_set_cache): per pixel the
+    // query record (8 words) and training record (12 words) of the last frame
+    bool cache_on = false;
+    uint32_t cache_sel_n = 0;
+    void* nrc = nullptr;
+    std::vector<uint32_t> cache_q, cache_t;
+    std::vector<uint8_t> cache_q_valid, cache_t_valid;
 };
+
+inline uint32_t unorm8_of(float v) { return (uint32_t)(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f + 0.5f); }
+
+// Training pixels of a frame: (pixel * (2^31 - 1) + off) mod N < sel_n, with
+// off = frame * 2654435761 mod N -- a permutation of the pixels per frame.
+inline bool cache_training_pixel(const Renderer& R, uint32_t p, uint32_t frame) {
+    if (R.cache_sel_n == 0) return false;
+    const uint64_t off = ((uint64_t)frame * 2654435761ull) % (uint64_t)R.N;
+    return ((uint64_t)p * 2147483647ull + off) % (uint64_t)R.N < R.cache_sel_n;
+}
 
 void write_output(Renderer& R, uint32_t p, f3 hdr_c, bool tonemap) {
     f3 c = hdr_c;
@@ -665,6 +617,9 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
     uint32_t mat_idx = 0xFFFFFFFFu, rand_seed = 0;
     f2 test_uv{0, 0};
     bool valid = false, has_sample = false;
+    bool cache_query = false, cache_train = false;
+    uint32_t rec[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const bool cache = !compat && R.cache_on;
     const f3 sky{1, 1, 1};
     for (uint32_t bounce = 0;; bounce++) {
         if (bounce == u.number_of_bounces) break;
@@ -715,7 +670,19 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         } else {
             throughput = throughput * factor;
         }
+        if (cache && bounce == 1) {
+            // the path ends here into the cache unless the pixel trains it
+            cache_query = true;
+            cache_train = cache_training_pixel(R, p, u.current_frame);
+            rec[0] = f32_bits(pl.pos.x); rec[1] = f32_bits(pl.pos.y); rec[2] = f32_bits(pl.pos.z); rec[3] = p;
+            rec[4] = oct_encode(pl.normal, 16);
+            rec[5] = oct_encode(wo, 16);
+            rec[6] = unorm8_of(mat.base[0]) | (unorm8_of(mat.base[1]) << 8) | (unorm8_of(mat.base[2]) << 16) |
+                     ((mat.model & 255u) << 24);
+            rec[7] = f32_bits(mat.fuzz);
+        }
         if (!compat && !(pdf > 0.0f)) break;   // corrected mode: an absorbed path ends here
+        if (cache && bounce == 1 && !cache_train) break;
         if (bounce > 3) {
             float pr = fmaxf(throughput.x, fmaxf(throughput.y, throughput.z));
             if (random_float(rng) > pr) break;
@@ -726,6 +693,30 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         f3 off = dot(wi, gn) > 0.0f ? gn : -gn;
         o = hit_position + off * 0.01f;
         direction = wi;
+    }
+    if (cache) {
+        R.cache_q_valid[p] = cache_query;
+        R.cache_t_valid[p] = cache_train;
+        if (cache_query) {
+            std::memcpy(&R.cache_q[(size_t)p * 8], rec, sizeof(rec));
+            if (cache_train) {
+                // the suffix radiance (bounces >= 2) is the training target
+                std::memcpy(&R.cache_t[(size_t)p * 12], rec, sizeof(rec));
+                R.cache_t[(size_t)p * 12 + 8] = f32_bits(L_out.x);
+                R.cache_t[(size_t)p * 12 + 9] = f32_bits(L_out.y);
+                R.cache_t[(size_t)p * 12 + 10] = f32_bits(L_out.z);
+                R.cache_t[(size_t)p * 12 + 11] = 0u;
+            }
+            // the candidate takes the cache's radiance (clamped at zero; non-finite -> 0)
+            f3 Lc{0.0f, 0.0f, 0.0f};
+            if (R.nrc) {
+                float pred[3];
+                or_nrc_infer(R.nrc, rec, 1, pred, 0);
+                Lc = f3{fmaxf(pred[0], 0.0f), fmaxf(pred[1], 0.0f), fmaxf(pred[2], 0.0f)};
+                if (!std::isfinite(Lc.x + Lc.y + Lc.z)) Lc = f3{0.0f, 0.0f, 0.0f};
+            }
+            L_out = f3{0.0f, 0.0f, 0.0f} + Lc;
+        }
     }
     Sample s;
     s.x_view = x_view; s.n_view = n_view; s.x_sample = x_sample; s.n_sample = n_sample;
@@ -768,6 +759,45 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         s.randSeed = R.gnrm_code[p];   // corrected layout keeps the oct16 code of n_view here
     }
     R.samples[p] = s;
+}
+
+// Corrected-mode target function: |L f(wo, wi) cos| with the BSDF of the
+// pixel's visible point (position, normal, material, wo towards the camera) --
+// the factor the reservoir's estimate is shaded with, so W absorbs it and a
+// glossy lobe cannot turn the resampled estimate into fireflies.  Reference mode
+// keeps the reference's |L| (ReSTIRGITemporalReuse.rgen.hlsl:33-40,
+// ReSTIRGISpatialReuse.rgen.hlsl:91-133), which is exact for its Lambertian-only
+// scenes up to the cosine.
+// Near-specular visible points (GGX conductor or plastic coat with roughness
+// below 0.25) take no temporal or spatial reuse in corrected mode: their
+// reservoir is the initial candidate alone (the path-traced estimate), since a
+// reconnection sample from another pixel lands in their sharp lobe with a
+// target far above the one it was resampled for.
+constexpr float kReuseMinRoughness = 0.25f;
+
+struct PixelShading {
+    const Material* m;
+    f3 x, n, wo, T, B;
+    bool reuse;
+};
+inline PixelShading pixel_shading(const Renderer& R, const Sample& s, const OrUBO& u) {
+    PixelShading P;
+    P.m = &R.sc->mat[s.materialID];
+    P.x = s.x_view;
+    P.n = s.n_view;
+    f3 cam = xyz(mul(u.view_inverse, f4{0, 0, 0, 1}));
+    P.wo = normalize(cam - P.x);
+    branchless_onb(P.n, &P.T, &P.B);
+    const bool glossy = (P.m->model == MAT_METALLIC || P.m->model == MAT_PLASTIC) && P.m->fuzz < kReuseMinRoughness;
+    P.reuse = !glossy;
+    return P;
+}
+inline float target_corrected(const PixelShading& P, f3 xs, f3 L) {
+    f3 wi = normalize(xs - P.x);
+    float c = dot(P.n, wi);
+    if (c <= 0.0f) return 0.0f;
+    f3 f = eval_material(*P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n)).f;
+    return length(L * f * c);
 }
 
 void shade_output(Renderer& R, uint32_t p, const Reservoir& r, const Sample& s_new, const OrUBO& u) {
@@ -834,7 +864,7 @@ void temporal_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u, bool ou
             }
         }
         if (!R.P.temporal_on) found = false;
-    } else if (R.P.temporal_on) {
+    } else if (R.P.temporal_on && pixel_shading(R, s_new, u).reuse) {
         f2 puv = world_to_screen_uv(s_new.x_view, u.view_prev, u.projection_prev);
         float fx = floorf(puv.x * (float)R.W), fy = floorf(puv.y * (float)R.H);
         if (fx >= 0.0f && fx < (float)R.W && fy >= 0.0f && fy < (float)R.H) {
@@ -848,12 +878,17 @@ void temporal_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u, bool ou
     }
     f3 x_curr = s_new.x_view;
     f3 n_curr = normalize(s_new.n_view);
+    PixelShading P{};
+    if (!compat) P = pixel_shading(R, s_new, u);
+    auto target = [&](const Sample& smp) {
+        return compat ? eval_target(smp, x_curr, n_curr) : target_corrected(P, smp.x_sample, smp.L_out);
+    };
     Reservoir r_final = init_reservoir();
-    float tp_new = eval_target(s_new, x_curr, n_curr);
+    float tp_new = target(s_new);
     float w_new = (s_new.p_q > 1e-6f) ? (tp_new / s_new.p_q) : 0.0f;
     update_reservoir(r_final, s_new, w_new, rng);
     if (found) {
-        float tp_prev = eval_target(r_prev.s, x_curr, n_curr);
+        float tp_prev = target(r_prev.s);
         merge_reservoir(r_final, r_prev, tp_prev, rng);
     } else {
         r_final.m = 1;
@@ -863,7 +898,7 @@ void temporal_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u, bool ou
         r_final.w_sum *= (float)cap / (float)r_final.m;
         r_final.m = cap;
     }
-    float tp_final = eval_target(r_final.s, x_curr, n_curr);
+    float tp_final = target(r_final.s);
     if (tp_final > 1e-6f && r_final.m > 0) r_final.W = r_final.w_sum / ((float)r_final.m * tp_final);
     else r_final.W = 0.0f;
     R.temporal[cur + p] = r_final;
@@ -911,8 +946,13 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
     }
     Reservoir center = R.temporal[read_off + p];
     Reservoir r_s = init_reservoir();
-    merge_reservoir(r_s, center, p_hat_of(center.s.L_out), rng);
-    const uint32_t nn = compat ? 6u : R.P.n_neighbours;
+    PixelShading P{};
+    if (!compat) P = pixel_shading(R, s_new, u);
+    auto target = [&](const Sample& smp) {
+        return compat ? p_hat_of(smp.L_out) : target_corrected(P, smp.x_sample, smp.L_out);
+    };
+    merge_reservoir(r_s, center, target(center.s), rng);
+    const uint32_t nn = compat ? 6u : (P.reuse ? R.P.n_neighbours : 0u);
     const float radius = compat ? 5.0f : R.P.radius_px;
     for (uint32_t i = 0; i < nn; i++) {
         uint32_t nb = neighbor_index(x, y, R.W, R.H, radius, rng);
@@ -937,7 +977,7 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
             if (cpo > 1e-6f) jac = (cpc * d2o) / (cpo * d2c);
         }
         jac = fminf(fmaxf(jac, 0.1f), 10.0f);
-        float ph = p_hat_of(r_nb.s.L_out) * jac;
+        float ph = target(r_nb.s) * jac;
         bool occluded = false;
         if (!compat && R.P.visibility && ph > 0.0f) {
             // corrected CheckVisibility (ReSTIRGISpatialReuse.rgen.hlsl:44-62): from
@@ -962,7 +1002,7 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         r_s.w_sum *= (float)R.P.m_cap_spatial / (float)r_s.m;
         r_s.m = R.P.m_cap_spatial;
     }
-    float phf = p_hat_of(r_s.s.L_out);
+    float phf = target(r_s.s);
     if (phf > 1e-6f && r_s.m > 0) r_s.W = r_s.w_sum / ((float)r_s.m * phf);
     else r_s.W = 0.0f;
     R.spatial[write_off + p] = r_s;
@@ -1147,6 +1187,21 @@ int or_write_temporal(void* rp, const float* words, size_t bytes) {
     return 0;
 }
 
+int or_renderer_set_cache(void* rp, int enabled, uint32_t train_samples, void* nrc) {
+    Renderer& R = *(Renderer*)rp;
+    if (enabled && R.compat) return 1;
+    R.cache_on = enabled != 0;
+    R.cache_sel_n = enabled ? std::min(train_samples, R.N) : 0u;
+    R.nrc = nrc;
+    if (R.cache_on && R.cache_q.empty()) {
+        R.cache_q.assign((size_t)R.N * 8, 0u);
+        R.cache_t.assign((size_t)R.N * 12, 0u);
+        R.cache_q_valid.assign(R.N, 0);
+        R.cache_t_valid.assign(R.N, 0);
+    }
+    return 0;
+}
+
 size_t or_read(void* rp, int which, void* dst, size_t bytes) {
     Renderer& R = *(Renderer*)rp;
     const void* src = nullptr;
@@ -1162,6 +1217,22 @@ size_t or_read(void* rp, int which, void* dst, size_t bytes) {
         case OR_BUF_GBUF_POS: src = R.gpos.data(); n = R.gpos.size() * sizeof(f4); break;
         case OR_BUF_MOTION: src = R.motion.data(); n = R.motion.size() * sizeof(f2); break;
         case OR_BUF_WRITTEN: src = R.written.data(); n = R.written.size() * 4; break;
+        case OR_BUF_CACHE_QUERIES:
+        case OR_BUF_CACHE_TRAIN: {
+            // valid records only, in pixel order
+            const bool q = which == OR_BUF_CACHE_QUERIES;
+            const size_t words = q ? 8 : 12;
+            std::vector<uint32_t> out;
+            if (R.cache_on)
+                for (uint32_t p = 0; p < R.N; ++p)
+                    if (q ? R.cache_q_valid[p] : R.cache_t_valid[p]) {
+                        const uint32_t* r = q ? &R.cache_q[(size_t)p * 8] : &R.cache_t[(size_t)p * 12];
+                        out.insert(out.end(), r, r + words);
+                    }
+            n = out.size() * 4;
+            if (dst && bytes >= n && n) memcpy(dst, out.data(), n);
+            return n;
+        }
         default: return 0;
     }
     if (dst && bytes >= n) memcpy(dst, src, n);

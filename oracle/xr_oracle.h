@@ -68,7 +68,9 @@ enum {
     OR_BUF_PT = 5,          /* N x 4 float: plain 1-spp path-traced radiance */
     OR_BUF_GBUF_POS = 6,    /* N x 4 float (x_view, valid) */
     OR_BUF_MOTION = 7,      /* N x 2 float (after RG16F rounding in compat mode) */
-    OR_BUF_WRITTEN = 8      /* N x u32: 1 where this frame wrote the output image */
+    OR_BUF_WRITTEN = 8,     /* N x u32: 1 where this frame wrote the output image */
+    OR_BUF_CACHE_QUERIES = 9,   /* radiance-cache query records of the frame, 8 words each, pixel order */
+    OR_BUF_CACHE_TRAIN = 10     /* radiance-cache training records, 12 words each, pixel order */
 };
 
 /* ---- known-answer helpers (random.hlsl, Sampling.hlsl) ---- */
@@ -89,6 +91,10 @@ void or_trace(void* scene, const float* rays, uint32_t n, int any_hit,
 /* ---- the frame pipeline ---- */
 void* or_renderer_create(void* scene, const OrParams* params);
 void or_renderer_destroy(void* r);
+/* Corrected mode: paths end into the learned radiance cache at their first
+   secondary vertex (training pixels continue); nrc (or_nrc_create, may be NULL:
+   prediction 0) supplies the candidates' radiance.  Returns non-zero in reference mode. */
+int or_renderer_set_cache(void* r, int enabled, uint32_t train_samples, void* nrc);
 int or_render_frame(void* r, const OrUBO* ubo);
 /* Fixed-candidate checks: load samples (N x 24 words, as read back from the
    CUDA path), optionally the temporal reservoirs, then run one reuse pass. */
@@ -103,6 +109,32 @@ int or_write_temporal(void* r, const float* words, size_t bytes);
    pass): frames [frame0, frame0+spp) each contribute one sample per pixel. */
 int or_pt_reference(void* scene, const OrParams* params, const OrUBO* ubo,
                     uint32_t frame0, uint32_t spp, double* out_rgb);
+
+/* ---- learned radiance cache (nrc.cpp) ----
+   Mirrors XrCacheSample in include/xr.h (72 B). */
+typedef struct OrCacheSample {
+    float pos[3];
+    float normal[3];
+    float wo[3];
+    float albedo[3];
+    float roughness;
+    uint32_t kind;
+    float target[3];
+    uint32_t pixel;
+} OrCacheSample;
+
+void* or_nrc_create(uint32_t seed);
+void or_nrc_destroy(void* nrc);
+void or_nrc_set_bounds(void* nrc, const float* lo3, float inv_extent);
+/* 0 MLP weights, 1 hash table, 2 MLP gradient, 3 table gradient, 4/5 MLP Adam m/v, 6/7 table Adam m/v */
+float* or_nrc_params(void* nrc, int which, size_t* count);
+void or_nrc_pack(const OrCacheSample* s, uint32_t n, uint32_t* records8);
+void or_nrc_inputs(void* nrc, const uint32_t* records8, uint32_t n, float* x64, int exact);
+void or_nrc_infer(void* nrc, const uint32_t* records8, uint32_t n, float* out3, int exact);
+double or_nrc_backward(void* nrc, const uint32_t* records8, const float* target3, uint32_t n, int exact,
+                       int loss_kind);
+double or_nrc_loss(void* nrc, const uint32_t* records8, const float* target3, uint32_t n, int exact, int loss_kind);
+void or_nrc_adam(void* nrc, float lr, float b1, float b2, float eps, float bc1, float bc2);
 
 #ifdef __cplusplus
 }

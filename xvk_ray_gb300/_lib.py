@@ -95,6 +95,29 @@ class XrProceduralDesc(C.Structure):
                 ("extent", C.c_float), ("sphere_subdiv", C.c_uint32)]
 
 
+class XrCacheParams(C.Structure):
+    _fields_ = [("enabled", C.c_uint32), ("train", C.c_uint32), ("train_samples", C.c_uint32),
+                ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("seed", C.c_uint32)]
+
+
+class XrCacheSample(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("normal", C.c_float * 3), ("wo", C.c_float * 3), ("albedo", C.c_float * 3),
+                ("roughness", C.c_float), ("kind", C.c_uint32), ("target", C.c_float * 3), ("pixel", C.c_uint32)]
+
+
+class XrCacheStats(C.Structure):
+    _fields_ = [("steps", C.c_uint32), ("queries", C.c_uint32), ("train_samples", C.c_uint32), ("loss", C.c_float),
+                ("ms_infer", C.c_float), ("ms_train", C.c_float), ("bounds_lo", C.c_float * 3),
+                ("inv_extent", C.c_float)]
+
+
+XR_CACHE_MLP, XR_CACHE_GRID, XR_CACHE_MLP_GRAD, XR_CACHE_GRID_GRAD = 0, 1, 2, 3
+XR_CACHE_MLP_M, XR_CACHE_MLP_V, XR_CACHE_GRID_M, XR_CACHE_GRID_V = 4, 5, 6, 7
+XR_CACHE_QUERIES, XR_CACHE_TRAIN_RECORDS = 8, 9
+XR_DEVFLAG_MMA_TIMEOUT = 8
+
+assert C.sizeof(XrCacheParams) == 32 and C.sizeof(XrCacheSample) == 72 and C.sizeof(XrCacheStats) == 40
 assert C.sizeof(XrVertex) == 36 and C.sizeof(XrMaterial) == 32
 assert C.sizeof(XrUniformBufferObject) == 412 and C.sizeof(XrParams) == 52
 
@@ -133,6 +156,17 @@ _SIGS = {
     "xr_event_elapsed": (_i32, [_P, _u32, _u32, C.POINTER(C.c_float)]),
     "xr_alloc_host": (_i32, [C.c_size_t, C.POINTER(_P)]),
     "xr_free_host": (None, [_P]),
+    "xr_cache_params_default": (None, [C.POINTER(XrCacheParams)]),
+    "xr_cache_set_params": (_i32, [_P, C.POINTER(XrCacheParams)]),
+    "xr_cache_get_params": (_i32, [_P, C.POINTER(XrCacheParams)]),
+    "xr_cache_reset": (_i32, [_P, _u32]),
+    "xr_cache_set_bounds": (_i32, [_P, _P, C.c_float]),
+    "xr_cache_query": (_i32, [_P, _P, _u32, _P]),
+    "xr_cache_train": (_i32, [_P, _P, _u32, C.c_int, C.POINTER(C.c_float)]),
+    "xr_cache_step": (_i32, [_P]),
+    "xr_cache_read": (_i32, [_P, C.c_int, _P, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "xr_cache_write": (_i32, [_P, C.c_int, _P, C.c_size_t]),
+    "xr_cache_get_stats": (_i32, [_P, C.POINTER(XrCacheStats)]),
 }
 
 EXPORTED = tuple(_SIGS)

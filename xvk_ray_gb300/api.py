@@ -109,6 +109,7 @@ class Renderer:
         L.check(lib.xr_create(C.byref(L.XrDeviceDesc(device, width, height)), C.byref(h)))
         self.ctx = h
         self.width, self.height = width, height
+        self.cache = Cache(self)
 
     def _c(self, status: int) -> None:
         L.check(status, self.ctx)
@@ -201,6 +202,85 @@ class Renderer:
         self._c(self._lib.xr_trace_rays(self.ctx, _ptr(rays), n, 1 if any_hit else 0, _ptr(prim), _ptr(t),
                                         _ptr(bary)))
         return prim, t, bary
+
+
+# host layout of XrCacheSample (72 B)
+CACHE_SAMPLE_DTYPE = np.dtype([("pos", "<f4", 3), ("normal", "<f4", 3), ("wo", "<f4", 3), ("albedo", "<f4", 3),
+                               ("roughness", "<f4"), ("kind", "<u4"), ("target", "<f4", 3), ("pixel", "<u4")])
+assert CACHE_SAMPLE_DTYPE.itemsize == C.sizeof(L.XrCacheSample)
+
+
+def cache_params_default() -> L.XrCacheParams:
+    p = L.XrCacheParams()
+    L.load().xr_cache_params_default(C.byref(p))
+    return p
+
+
+class Cache:
+    """The learned radiance cache of one Renderer (xr_cache_* entry points)."""
+
+    ARRAY_FLOATS = {0: 17408, 1: 16 * (1 << 19) * 2}
+
+    def __init__(self, renderer: "Renderer"):
+        self._r = renderer
+
+    def _c(self, status):
+        self._r._c(status)
+
+    @property
+    def _ctx(self):
+        return self._r.ctx
+
+    def set_params(self, p: L.XrCacheParams) -> None:
+        self._c(L.load().xr_cache_set_params(self._ctx, C.byref(p)))
+
+    def params(self) -> L.XrCacheParams:
+        p = L.XrCacheParams()
+        self._c(L.load().xr_cache_get_params(self._ctx, C.byref(p)))
+        return p
+
+    def reset(self, seed: int = 1) -> None:
+        self._c(L.load().xr_cache_reset(self._ctx, seed))
+
+    def set_bounds(self, lo, inv_extent: float) -> None:
+        lo = np.ascontiguousarray(lo, np.float32)
+        self._c(L.load().xr_cache_set_bounds(self._ctx, _ptr(lo), float(inv_extent)))
+
+    def query(self, samples: np.ndarray) -> np.ndarray:
+        s = np.ascontiguousarray(samples, CACHE_SAMPLE_DTYPE)
+        out = np.empty((len(s), 3), np.float32)
+        self._c(L.load().xr_cache_query(self._ctx, _ptr(s.view(np.uint8)), len(s), _ptr(out)))
+        return out
+
+    def train(self, samples: np.ndarray, apply: bool = True) -> float:
+        s = np.ascontiguousarray(samples, CACHE_SAMPLE_DTYPE)
+        loss = C.c_float()
+        self._c(L.load().xr_cache_train(self._ctx, _ptr(s.view(np.uint8)), len(s), int(apply), C.byref(loss)))
+        return loss.value
+
+    def step(self) -> None:
+        self._c(L.load().xr_cache_step(self._ctx))
+
+    def read(self, which: int) -> np.ndarray:
+        n = C.c_size_t()
+        self._c(L.load().xr_cache_read(self._ctx, which, None, 0, C.byref(n)))
+        if which in (L.XR_CACHE_QUERIES, L.XR_CACHE_TRAIN_RECORDS):
+            out = np.empty(n.value // 4, np.uint32)
+            if n.value:
+                self._c(L.load().xr_cache_read(self._ctx, which, _ptr(out), out.nbytes, None))
+            return out.reshape(-1, 8 if which == L.XR_CACHE_QUERIES else 12)
+        out = np.empty(n.value // 4, np.float32)
+        self._c(L.load().xr_cache_read(self._ctx, which, _ptr(out), out.nbytes, None))
+        return out
+
+    def write(self, which: int, values: np.ndarray) -> None:
+        v = np.ascontiguousarray(values, np.float32)
+        self._c(L.load().xr_cache_write(self._ctx, which, _ptr(v), v.nbytes))
+
+    def stats(self) -> L.XrCacheStats:
+        st = L.XrCacheStats()
+        self._c(L.load().xr_cache_get_stats(self._ctx, C.byref(st)))
+        return st
 
 
 class PinnedBuffer:

@@ -1,0 +1,550 @@
+// nrc.cu -- learned radiance cache kernels: inference and training on the
+// 5th-generation tensor cores (tcgen05, BF16 operands, FP32 accumulators in
+// tensor memory), Adam, initialisation.
+//
+// Tiles of 128 samples (one per thread of a 4-warp CTA; thread t of warp w owns
+// row 32 w + t and reads accumulator lane 32 w + t).  Per layer the CTA stages
+// the tile's activations in shared memory (K-major canonical layout, bfloat16),
+// one thread issues the MMAs of the layer (K = 64 in four K = 16 steps) against
+// the layer's weights kept in shared memory, tcgen05.commit arrives on an
+// mbarrier, and every thread reads its accumulator row back with tcgen05.ld,
+// applies ReLU and writes the next layer's activations.
+//
+// Training (forward + backward fused per tile) keeps every layer's activations
+// in shared memory and accumulates the weight gradients of all tiles a CTA
+// processes in tensor memory (dW_l = dZ_l^T H_l, M = 128 with the rows beyond
+// the layer's outputs zero); the hash-table gradients are scattered with
+// vector atomics.  Every wait on the tensor core is bounded (1 s of wall time);
+// on expiry the kernel sets XR_DEVFLAG_MMA_TIMEOUT, stops and frees its tensor
+// memory.
+#include <cmath>
+
+#include "nrc.cuh"
+#include "umma.cuh"
+#include "xr_internal.h"
+
+namespace xr {
+namespace nrc {
+namespace {
+
+constexpr uint64_t kWaitNs = 1000000000ull;
+constexpr uint32_t kActBytes = kTile * kIn * 2;   // one [128][64] bf16 operand (16 KB)
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    return (uint32_t)umma::bf16_bits(a) | ((uint32_t)umma::bf16_bits(b) << 16);
+}
+
+// Row r of a K-major [*][K] bf16 operand <- K float values (rounded to bfloat16).
+template <int K>
+__device__ __forceinline__ void store_row(uint8_t* base, uint32_t r, const float* v) {
+#pragma unroll
+    for (int c = 0; c < K; c += 8) {
+        uint4 w = make_uint4(pack2(v[c], v[c + 1]), pack2(v[c + 2], v[c + 3]), pack2(v[c + 4], v[c + 5]),
+                             pack2(v[c + 6], v[c + 7]));
+        *reinterpret_cast<uint4*>(base + umma::kmajor_offset(r, c, K)) = w;
+    }
+}
+
+// Row r of a K-major [*][64] bf16 operand -> 64 float values.
+__device__ __forceinline__ void load_row64(const uint8_t* base, uint32_t r, float* v) {
+#pragma unroll
+    for (int c = 0; c < 64; c += 8) {
+        const uint4 w = *reinterpret_cast<const uint4*>(base + umma::kmajor_offset(r, c, 64));
+        const uint32_t u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            v[c + 2 * j] = umma::bf16_value((uint16_t)(u[j] & 0xFFFFu));
+            v[c + 2 * j + 1] = umma::bf16_value((uint16_t)(u[j] >> 16));
+        }
+    }
+}
+
+// Column `col` (a sample) of a K-major [rows][128] operand <- rows values.
+template <int ROWS>
+__device__ __forceinline__ void store_col128(uint8_t* base, uint32_t col, const float* v) {
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r)
+        *reinterpret_cast<uint16_t*>(base + umma::kmajor_offset(r, col, 128)) = umma::bf16_bits(v[r]);
+}
+
+__device__ __forceinline__ void copy_image(uint8_t* dst, const uint8_t* __restrict__ src, uint32_t bytes) {
+    for (uint32_t i = threadIdx.x * 16u; i < bytes; i += blockDim.x * 16u)
+        *reinterpret_cast<uint4*>(dst + i) = __ldg(reinterpret_cast<const uint4*>(src + i));
+}
+
+// Shared-memory writes of every thread become visible to the tensor core, and
+// every earlier tcgen05.ld of every thread is ordered before what follows.
+__device__ __forceinline__ void publish() {
+    umma::fence_proxy_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+}
+
+// D (+)= A[128][K] * B[N][K]^T, `steps` K = 16 steps; issued by one thread.
+__device__ __forceinline__ void gemm(uint32_t d_tmem, const uint8_t* A, const uint8_t* B, uint32_t K, uint32_t N,
+                                     uint32_t steps, bool accumulate) {
+    const uint32_t id = umma::idesc_bf16_f32(128, N);
+    const uint32_t a0 = umma::smem_u32(A), b0 = umma::smem_u32(B);
+    for (uint32_t s = 0; s < steps; ++s) {
+        const uint64_t ad = umma::smem_desc(a0 + 256u * s, 128u, K * 16u);
+        const uint64_t bd = umma::smem_desc(b0 + 256u * s, 128u, K * 16u);
+        umma::mma_bf16(d_tmem, ad, bd, id, (accumulate || s > 0) ? 1u : 0u);
+    }
+}
+
+// Every thread waits for the last commit; the outcome is the same in all threads.
+__device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& phase) {
+    bool ok = umma::mbar_wait(bar, phase & 1u, kWaitNs);
+    phase++;
+    ok = __syncthreads_and(ok) != 0;
+    umma::fence_after_sync();
+    return ok;
+}
+
+// 64 accumulator columns [c0, c0 + 64) of this thread's lane.
+__device__ __forceinline__ void tmem_row64(uint32_t taddr, float* v) {
+    umma::tmem_ld16(taddr, v);
+    umma::tmem_ld16(taddr + 16u, v + 16);
+    umma::tmem_ld16(taddr + 32u, v + 32);
+    umma::tmem_ld16(taddr + 48u, v + 48);
+    umma::tmem_wait_ld();
+}
+
+__device__ __forceinline__ void inputs_of(const Bounds& bnd, const __half2* table, const uint4* rec, uint32_t stride,
+                                          uint32_t i, float4& ra, uint4& rb, float* v) {
+    const uint4 a = rec[(size_t)i * stride], b = rec[(size_t)i * stride + 1];
+    ra = make_float4(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(a.w));
+    rb = b;
+    network_inputs(bnd, table, ra, rb, v);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// inference: MODE 0 writes out3[i] (test/API path), MODE 1 adds the prediction
+// (clamped at 0) to the candidate radiance cand_b[pixel].rgb of the frame.
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(128) k_cache_infer(const uint4* __restrict__ rec, const uint32_t* count_ptr,
+                                                     uint32_t count_host, Bounds bnd, const __half2* __restrict__ table,
+                                                     const uint8_t* __restrict__ w_fwd, float* __restrict__ out3,
+                                                     float4* __restrict__ cand_b, uint32_t* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sW = smem;                  // forward weight image
+    uint8_t* sX = smem + kImageBytes;    // activations of the current layer
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t count = count_ptr ? *(volatile const uint32_t*)count_ptr : count_host;
+    const uint32_t ntiles = (count + kTile - 1u) / kTile;
+    if (blockIdx.x >= ntiles) return;
+
+    if (warp == 0) umma::tmem_alloc(&tslot, 64);
+    if (tid == 0) { umma::mbar_init(&bar, 1); umma::mbar_fence_init(); }
+    copy_image(sW, w_fwd, kImageBytes);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const uint32_t i = tile * kTile + tid;
+        const bool valid = i < count;
+        float v[kIn];
+        float4 ra = make_float4(0, 0, 0, 0);
+        uint4 rb = make_uint4(0, 0, 0, 0);
+        if (valid) inputs_of(bnd, table, rec, 2u, i, ra, rb, v);
+        else {
+#pragma unroll
+            for (int j = 0; j < kIn; ++j) v[j] = 0.0f;
+        }
+        store_row<kIn>(sX, tid, v);
+        for (int l = 0; l <= kHidden && ok; ++l) {
+            publish();
+            if (tid == 0) {
+                gemm(tmem, sX, sW + l * kLayerBytes, 64u, l < kHidden ? 64u : 16u, 4u, false);
+                umma::commit(&bar);
+            }
+            ok = wait_mma(&bar, phase);
+            if (!ok) break;
+            if (l < kHidden) {
+                tmem_row64(lane_addr, v);
+#pragma unroll
+                for (int j = 0; j < kWidth; ++j) v[j] = fmaxf(v[j], 0.0f);
+                store_row<kIn>(sX, tid, v);
+            } else {
+                umma::tmem_ld16(lane_addr, v);
+                umma::tmem_wait_ld();
+                if (valid) {
+                    if (MODE == 0) {
+                        out3[(size_t)i * 3 + 0] = v[0];
+                        out3[(size_t)i * 3 + 1] = v[1];
+                        out3[(size_t)i * 3 + 2] = v[2];
+                    } else {
+                        const uint32_t pixel = __float_as_uint(ra.w);
+                        float3 L = f3(fmaxf(v[0], 0.0f), fmaxf(v[1], 0.0f), fmaxf(v[2], 0.0f));
+                        if (!isfinite(L.x + L.y + L.z)) L = f3(0.0f, 0.0f, 0.0f);
+                        float4 c = cand_b[pixel];
+                        c.x = c.x + L.x; c.y = c.y + L.y; c.z = c.z + L.z;
+                        cand_b[pixel] = c;
+                    }
+                }
+            }
+        }
+    }
+    if (!ok && tid == 0) atomicOr(err, (uint32_t)XR_DEVFLAG_MMA_TIMEOUT);
+    if (!ok) umma::mbar_wait(&bar, phase & 1u, kWaitNs);   // let an MMA still in flight finish
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 64);
+}
+
+// ---------------------------------------------------------------------------
+// training: forward + backward of every tile, gradients of the mean relative
+// L2 loss over n = min(count, cap) rounded down to a multiple of 128 samples.
+// Shared memory (217,088 B): forward image, backward image, H_0..H_4, dZ,
+// dZ^T [128][128] (rows beyond the layer's outputs zero), H^T [64][128].
+// Tensor memory (512 columns): 0..63 forward / dX accumulator, 64 + 64 l: dW_l.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kOffWf = 0, kOffWb = kImageBytes, kOffX = 2 * kImageBytes;
+constexpr uint32_t kOffDZ = kOffX + 5 * kActBytes, kOffDZT = kOffDZ + kActBytes, kOffHT = kOffDZT + 2 * kActBytes;
+constexpr uint32_t kTrainSmem = kOffHT + kActBytes;
+static_assert(kTrainSmem == 217088, "training shared memory layout");
+
+__global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict__ rec, const uint32_t* count_ptr,
+                                                        uint32_t count_host, uint32_t cap, Bounds bnd,
+                                                        const __half2* __restrict__ table,
+                                                        const uint8_t* __restrict__ w_fwd,
+                                                        const uint8_t* __restrict__ w_bwd, float* mlp_grad,
+                                                        float2* grid_grad, float* loss_acc, uint32_t* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sWf = smem + kOffWf;
+    uint8_t* sWb = smem + kOffWb;
+    uint8_t* sX = smem + kOffX;
+    uint8_t* sDZ = smem + kOffDZ;
+    uint8_t* sDZT = smem + kOffDZT;
+    uint8_t* sHT = smem + kOffHT;
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    uint32_t count = count_ptr ? *(volatile const uint32_t*)count_ptr : count_host;
+    if (count > cap) count = cap;
+    const uint32_t n = count & ~(kTile - 1u);
+    const uint32_t ntiles = n / kTile;
+    if (blockIdx.x >= ntiles) return;
+    const float inv_count = 1.0f / (float)(3u * n);
+
+    if (warp == 0) umma::tmem_alloc(&tslot, 512);
+    if (tid == 0) { umma::mbar_init(&bar, 1); umma::mbar_fence_init(); }
+    copy_image(sWf, w_fwd, kImageBytes);
+    copy_image(sWb, w_bwd, kImageBytes);
+    // rows 64..127 of dZ^T (bytes 16384..32767: row groups 8..15 of 2048 B) stay
+    // zero -- the padding of the M = 128 weight-gradient MMAs
+    for (uint32_t off = 16384u + tid * 16u; off < 32768u; off += 128u * 16u)
+        *reinterpret_cast<uint4*>(sDZT + off) = make_uint4(0, 0, 0, 0);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+    uint32_t phase = 0;
+    bool ok = true, first = true;
+    float loss = 0.0f;
+
+    for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const uint32_t i = tile * kTile + tid;
+        float v[kIn];
+        float4 ra;
+        uint4 rb;
+        inputs_of(bnd, table, rec, 3u, i, ra, rb, v);
+        const uint4 rt = rec[(size_t)i * 3 + 2];
+        store_row<kIn>(sX, tid, v);
+        // ---- forward, keeping H_0..H_4 ----
+        float y[16];
+        for (int l = 0; l <= kHidden && ok; ++l) {
+            publish();
+            if (tid == 0) {
+                gemm(tmem, sX + l * kActBytes, sWf + l * kLayerBytes, 64u, l < kHidden ? 64u : 16u, 4u, false);
+                umma::commit(&bar);
+            }
+            ok = wait_mma(&bar, phase);
+            if (!ok) break;
+            if (l < kHidden) {
+                tmem_row64(lane_addr, v);
+#pragma unroll
+                for (int j = 0; j < kWidth; ++j) v[j] = fmaxf(v[j], 0.0f);
+                store_row<kIn>(sX + (l + 1) * kActBytes, tid, v);
+            } else {
+                umma::tmem_ld16(lane_addr, y);
+                umma::tmem_wait_ld();
+            }
+        }
+        if (!ok) break;
+        // ---- loss and output gradient ----
+        float dz[kWidth];
+        {
+            const float t[3] = {__uint_as_float(rt.x), __uint_as_float(rt.y), __uint_as_float(rt.z)};
+#pragma unroll
+            for (int c = 0; c < 16; ++c) dz[c] = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float d = y[c] - t[c];
+                const float den = y[c] * y[c] + 0.01f;
+                loss += d * d / den * inv_count;
+                dz[c] = 2.0f * d / den * inv_count;
+            }
+        }
+        store_row<16>(sDZ, tid, dz);
+        store_col128<16>(sDZT, tid, dz);
+        // rows 16..63 of dZ^T (bytes 4096..16383): zero -- the previous tile's
+        // hidden layers left values there
+        for (uint32_t off = 4096u + tid * 16u; off < 16384u; off += 128u * 16u)
+            *reinterpret_cast<uint4*>(sDZT + off) = make_uint4(0, 0, 0, 0);
+        // ---- backward: layer 4 .. 0 ----
+        for (int l = kHidden; l >= 0 && ok; --l) {
+            // H_l^T from this thread's own row of H_l
+            load_row64(sX + l * kActBytes, tid, v);
+            store_col128<64>(sHT, tid, v);
+            publish();
+            if (tid == 0) {
+                const uint32_t K = l == kHidden ? 16u : 64u;
+                gemm(tmem, sDZ, sWb + l * kLayerBytes, K, 64u, K / 16u, false);                  // dX = dZ W_l
+                gemm(tmem + 64u + 64u * (uint32_t)l, sDZT, sHT, 128u, 64u, 8u, !first);       // dW_l += dZ^T H_l
+                umma::commit(&bar);
+            }
+            ok = wait_mma(&bar, phase);
+            if (!ok) break;
+            float dx[kWidth];
+            tmem_row64(lane_addr, dx);
+            if (l > 0) {
+                // dZ_l = dH_l * relu'(Z_l), with Z_l > 0 exactly where this thread's row of H_l (in v) is
+#pragma unroll
+                for (int j = 0; j < kWidth; ++j) dz[j] = v[j] > 0.0f ? dx[j] : 0.0f;
+                store_row<kIn>(sDZ, tid, dz);
+                // the bf16-rounded values of dz, as the MMA will see them
+#pragma unroll
+                for (int j = 0; j < kWidth; ++j) dz[j] = umma::bf16_value(umma::bf16_bits(dz[j]));
+                store_col128<64>(sDZT, tid, dz);
+            } else {
+                // hash-table gradients through the trilinear interpolation
+                const float3 p = unit_pos(bnd, xyz(ra));
+#pragma unroll 1
+                for (int lv = 0; lv < kLevels; ++lv) {
+                    LevelCorners c;
+                    level_corners(lv, p, c);
+                    const float g0 = dx[2 * lv], g1 = dx[2 * lv + 1];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        atomicAdd(grid_grad + (size_t)lv * kT + c.idx[k], make_float2(c.w[k] * g0, c.w[k] * g1));
+                }
+            }
+        }
+        first = false;
+    }
+    // loss (mean over the batch)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, o);
+    if (lane == 0 && ok) atomicAdd(loss_acc, loss);
+    // weight gradients: rows 0..63 live in warps 0 and 1
+    if (ok && !first && warp < 2) {
+        for (int l = 0; l <= kHidden; ++l) {
+            const uint32_t rows = l < kHidden ? 64u : 16u;
+            for (uint32_t c = 0; c < 64u; c += 16u) {
+                float g[16];
+                umma::tmem_ld16(lane_addr + 64u + 64u * (uint32_t)l + c, g);
+                umma::tmem_wait_ld();
+                if (tid < rows) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) atomicAdd(mlp_grad + l * 4096 + tid * 64u + c + j, g[j]);
+                }
+            }
+        }
+    }
+    if (!ok && tid == 0) atomicOr(err, (uint32_t)XR_DEVFLAG_MMA_TIMEOUT);
+    if (!ok) umma::mbar_wait(&bar, phase & 1u, kWaitNs);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 512);
+}
+
+// ---------------------------------------------------------------------------
+// Adam (Kingma and Ba 2015) and weight images
+// ---------------------------------------------------------------------------
+struct AdamArgs {
+    float lr, b1, b2, eps, bc1, bc2;
+};
+
+__device__ __forceinline__ void adam_step(float& w, float& m, float& v, float g, const AdamArgs& a) {
+    m = a.b1 * m + (1.0f - a.b1) * g;
+    v = a.b2 * v + (1.0f - a.b2) * (g * g);
+    const float mh = m / a.bc1, vh = v / a.bc2;
+    w = w - a.lr * mh / (sqrtf(vh) + a.eps);
+}
+
+__device__ __forceinline__ void write_images(uint32_t i, float w, uint8_t* w_fwd, uint8_t* w_bwd) {
+    const uint32_t l = i < 16384u ? i >> 12 : 4u;
+    const uint32_t rem = i - l * 4096u, o = rem >> 6, in = rem & 63u;
+    const uint16_t b = umma::bf16_bits(w);
+    *reinterpret_cast<uint16_t*>(w_fwd + l * kLayerBytes + umma::kmajor_offset(o, in, 64)) = b;
+    *reinterpret_cast<uint16_t*>(w_bwd + l * kLayerBytes + umma::kmajor_offset(in, o, l < 4 ? 64u : 16u)) = b;
+}
+
+__global__ void k_cache_adam_mlp(float* w, float* g, float* m, float* v, uint8_t* w_fwd, uint8_t* w_bwd, AdamArgs a,
+                                 int apply) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)kMlpParams) return;
+    float wi = w[i];
+    if (apply) {
+        float mi = m[i], vi = v[i];
+        adam_step(wi, mi, vi, g[i], a);
+        w[i] = wi; m[i] = mi; v[i] = vi;
+        g[i] = 0.0f;
+    }
+    write_images(i, wi, w_fwd, w_bwd);
+}
+
+// Sparse update: a table value changes only where its gradient is non-zero.
+__global__ void k_cache_adam_grid(float2* w, float2* g, float2* m, float2* v, __half2* table, AdamArgs a) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kGridParams / 2) return;
+    const float2 gr = g[e];
+    if (gr.x == 0.0f && gr.y == 0.0f) return;
+    float2 wi = w[e], mi = m[e], vi = v[e];
+    if (gr.x != 0.0f) adam_step(wi.x, mi.x, vi.x, gr.x, a);
+    if (gr.y != 0.0f) adam_step(wi.y, mi.y, vi.y, gr.y, a);
+    w[e] = wi; m[e] = mi; v[e] = vi;
+    g[e] = make_float2(0.0f, 0.0f);
+    table[e] = __floats2half2_rn(wi.x, wi.y);
+}
+
+__global__ void k_cache_init_grid(float2* w, __half2* table, uint32_t seed) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kGridParams / 2) return;
+    const float a = (init_u01((uint32_t)(2 * e), seed, 1u) * 2.0f - 1.0f) * 1e-4f;
+    const float b = (init_u01((uint32_t)(2 * e + 1), seed, 1u) * 2.0f - 1.0f) * 1e-4f;
+    w[e] = make_float2(a, b);
+    table[e] = __floats2half2_rn(a, b);
+}
+
+__global__ void k_cache_table_from_master(const float2* w, __half2* table) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kGridParams / 2) return;
+    const float2 x = w[e];
+    table[e] = __floats2half2_rn(x.x, x.y);
+}
+
+// XrCacheSample (18 words) -> record (stride 2 or 3 uint4)
+__global__ void k_cache_pack(const XrCacheSample* s, uint32_t n, uint4* rec, uint32_t stride) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const XrCacheSample q = s[i];
+    rec[(size_t)i * stride] = make_uint4(__float_as_uint(q.pos[0]), __float_as_uint(q.pos[1]),
+                                         __float_as_uint(q.pos[2]), q.pixel);
+    rec[(size_t)i * stride + 1] = pack_b(f3(q.normal[0], q.normal[1], q.normal[2]), f3(q.wo[0], q.wo[1], q.wo[2]),
+                                         f3(q.albedo[0], q.albedo[1], q.albedo[2]), q.kind, q.roughness);
+    if (stride == 3)
+        rec[(size_t)i * stride + 2] = make_uint4(__float_as_uint(q.target[0]), __float_as_uint(q.target[1]),
+                                                 __float_as_uint(q.target[2]), 0u);
+}
+
+}  // namespace nrc
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+using namespace nrc;
+
+static nrc::AdamArgs adam_args(const CacheState& cs) {
+    nrc::AdamArgs a;
+    a.lr = cs.params.learning_rate;
+    a.b1 = cs.params.beta1;
+    a.b2 = cs.params.beta2;
+    a.eps = cs.params.epsilon;
+    a.bc1 = (float)(1.0 - std::pow((double)cs.params.beta1, (double)cs.step));
+    a.bc2 = (float)(1.0 - std::pow((double)cs.params.beta2, (double)cs.step));
+    return a;
+}
+
+static nrc::Bounds bounds_of(const CacheState& cs) {
+    nrc::Bounds b;
+    b.lo[0] = cs.lo[0]; b.lo[1] = cs.lo[1]; b.lo[2] = cs.lo[2];
+    b.inv_ext = cs.inv_ext;
+    return b;
+}
+
+cudaError_t cache_configure_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(k_cache_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_cache_infer<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kImageBytes + kActBytes));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_cache_infer<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(kImageBytes + kActBytes));
+}
+
+void launch_cache_init(CacheState& cs, uint32_t seed, cudaStream_t st) {
+    const uint32_t n2 = (uint32_t)(kGridParams / 2);
+    k_cache_init_grid<<<(n2 + 255) / 256, 256, 0, st>>>(reinterpret_cast<float2*>(cs.grid), cs.table, seed);
+    k_cache_adam_mlp<<<(kMlpParams + 255) / 256, 256, 0, st>>>(cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.w_fwd,
+                                                                cs.w_bwd, adam_args(cs), 0);
+}
+
+void launch_cache_refresh(CacheState& cs, cudaStream_t st) {
+    const uint32_t n2 = (uint32_t)(kGridParams / 2);
+    k_cache_table_from_master<<<(n2 + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float2*>(cs.grid), cs.table);
+    k_cache_adam_mlp<<<(kMlpParams + 255) / 256, 256, 0, st>>>(cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.w_fwd,
+                                                                cs.w_bwd, adam_args(cs), 0);
+}
+
+void launch_cache_pack(const XrCacheSample* s, uint32_t n, uint4* rec, uint32_t stride, cudaStream_t st) {
+    if (n) k_cache_pack<<<(n + 127) / 128, 128, 0, st>>>(s, n, rec, stride);
+}
+
+void launch_cache_infer(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                        float* out3, float4* cand_b, uint32_t* err, int sm_count, cudaStream_t st) {
+    const uint32_t smem = kImageBytes + kActBytes;
+    uint32_t grid = (uint32_t)sm_count * 4u;
+    if (!count_ptr) {
+        const uint32_t tiles = (count_host + kTile - 1u) / kTile;
+        if (tiles == 0) return;
+        if (tiles < grid) grid = tiles;
+    }
+    if (cand_b)
+        k_cache_infer<1><<<grid, 128, smem, st>>>(rec, count_ptr, count_host, bounds_of(cs), cs.table, cs.w_fwd,
+                                                  nullptr, cand_b, err);
+    else
+        k_cache_infer<0><<<grid, 128, smem, st>>>(rec, count_ptr, count_host, bounds_of(cs), cs.table, cs.w_fwd,
+                                                  out3, nullptr, err);
+}
+
+void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                        uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st) {
+    uint32_t grid = (uint32_t)sm_count;
+    if (!count_ptr) {
+        const uint32_t tiles = (count_host < cap ? count_host : cap) / kTile;
+        if (tiles < grid) grid = tiles;
+    }
+    cudaMemsetAsync(cs.loss, 0, sizeof(float), st);
+    if (grid)
+        k_cache_train<<<grid, 128, kTrainSmem, st>>>(rec, count_ptr, count_host, cap, bounds_of(cs), cs.table, cs.w_fwd,
+                                                     cs.w_bwd, cs.mlp_grad, reinterpret_cast<float2*>(cs.grid_grad),
+                                                     cs.loss, err);
+    if (apply) launch_cache_adam(cs, st);
+}
+
+void launch_cache_adam(CacheState& cs, cudaStream_t st) {
+    cs.step++;
+    const nrc::AdamArgs a = adam_args(cs);
+    k_cache_adam_mlp<<<(kMlpParams + 255) / 256, 256, 0, st>>>(cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.w_fwd,
+                                                                cs.w_bwd, a, 1);
+    const uint32_t n2 = (uint32_t)(kGridParams / 2);
+    k_cache_adam_grid<<<(n2 + 255) / 256, 256, 0, st>>>(
+        reinterpret_cast<float2*>(cs.grid), reinterpret_cast<float2*>(cs.grid_grad),
+        reinterpret_cast<float2*>(cs.grid_m), reinterpret_cast<float2*>(cs.grid_v), cs.table, a);
+}
+
+}  // namespace xr

@@ -18,6 +18,7 @@
 #include <utility>
 
 #include "bsdf.cuh"
+#include "nrc.cuh"
 #include "wavefront_trace.cuh"
 
 namespace xr {
@@ -100,12 +101,41 @@ __device__ __forceinline__ void add_radiance(const FrameArgs& fa, uint32_t p, fl
     dst[p] = f4(L, v.w);
 }
 
+// Radiance found at bounce >= 2.  With the radiance cache on, only training
+// paths live past bounce 1, and what they find is the training target of their
+// record (index carried in the p_q slot, which is free after bounce 1).
+template <bool COMPAT>
+__device__ __forceinline__ void add_suffix_radiance(const FrameArgs& fa, const PathState& s, float3 add) {
+    if (!COMPAT && fa.cache_on) {
+        float4* tgt = reinterpret_cast<float4*>(fa.cache_t + (size_t)__float_as_uint(s.pq) * 3u + 2u);
+        float4 v = *tgt;
+        *tgt = make_float4(v.x + add.x, v.y + add.y, v.z + add.z, v.w);
+    } else {
+        add_radiance<COMPAT>(fa, s.pixel, add);
+    }
+}
+
+// What the shading of bounce 1 hands to the radiance cache (corrected mode).
+struct CacheEmit {
+    bool query;        // x_s is a surface: the candidate takes the cache's radiance
+    bool train;        // the pixel is one of the frame's training pixels
+    float4 ra;         // record {x_s, pixel}
+    uint4 rb;          // record {oct16(n_s), oct16(wo), albedo | kind, roughness}
+};
+
+__device__ __forceinline__ bool cache_training_pixel(const FrameArgs& fa, uint32_t pixel) {
+    if (fa.cache_sel_n == 0u) return false;
+    const uint64_t k = ((uint64_t)pixel * 2147483647ull + fa.cache_sel_off) % (uint64_t)fa.N;
+    return k < fa.cache_sel_n;
+}
+
 // Shades the traced hit `h` of one path: records the bounce's sample fields,
 // samples the BSDF and returns true when the path continues to bounce + 1
 // (state updated in place).
 template <bool COMPAT>
 __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
-                                           uint32_t bounce, uint32_t nb, PathState& s, const HitRec& h) {
+                                           uint32_t bounce, uint32_t nb, PathState& s, const HitRec& h,
+                                           CacheEmit& ce) {
     const uint32_t p = s.pixel;
     HitPayload pl;
     pl.mat = -1;
@@ -120,7 +150,7 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
             if (sky) L = L + s.thr * sky_c;
             write_sample<COMPAT>(fa, p, s.o + s.d * 1000.0f, -s.d, L, s.pq);
         } else if (sky) {
-            add_radiance<COMPAT>(fa, p, s.thr * sky_c);
+            add_suffix_radiance<COMPAT>(fa, s, s.thr * sky_c);
         }
         return false;
     }
@@ -145,7 +175,7 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
             float3 L = f3(0.0f, 0.0f, 0.0f) + term;
             write_sample<COMPAT>(fa, p, pl.pos, pl.normal, L, s.pq);
         } else {
-            add_radiance<COMPAT>(fa, p, term);
+            add_suffix_radiance<COMPAT>(fa, s, term);
         }
         return false;
     }
@@ -178,6 +208,13 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
     }
     if (bounce + 1 >= nb) alive = false;   // the next iteration would hit the depth limit
     if (bounce == 1) write_sample<COMPAT>(fa, p, x_s, n_s, f3(0.0f, 0.0f, 0.0f), s.pq);
+    if (!COMPAT && fa.cache_on && bounce == 1) {
+        ce.query = true;
+        ce.train = cache_training_pixel(fa, p);
+        ce.ra = f4(x_s, __uint_as_float(p));
+        ce.rb = nrc::pack_b(n_s, wo, f3(mat.base_color[0], mat.base_color[1], mat.base_color[2]),
+                            mat.material_model, mat.fuzziness);
+    }
     if (bounce == 0 && !alive) {
         if (COMPAT) {
             fa.s_xs[p] = make_float4(0.0f, 0.0f, 0.0f, pdf);
@@ -212,6 +249,52 @@ __device__ __forceinline__ void push_path(const FrameArgs& fa, bool alive, const
         fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
         fa.q_out[2][i] = f4(s.thr, s.pq);
     }
+}
+
+// Radiance-cache records of bounce 1 (all lanes of the warp call this): one
+// query per surface x_s, appended with one atomic per warp; training pixels also
+// take a training record (target zero, filled by the rest of the path) and keep
+// their path alive with the record index in the p_q slot; every other path ends.
+__device__ __forceinline__ bool cache_emit(const FrameArgs& fa, const CacheEmit& ce, bool alive, PathState& s) {
+    const uint32_t lane = lane_id();
+    const uint32_t qmask = __ballot_sync(0xFFFFFFFFu, ce.query);
+    if (qmask) {
+        const int leader = __ffs(qmask) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&fa.counters[kCntCacheQuery], (uint32_t)__popc(qmask));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (ce.query) {
+            const uint32_t q = base + (uint32_t)__popc(qmask & ((1u << lane) - 1u));
+            if (q < fa.N) {
+                fa.cache_q[(size_t)q * 2u] = make_uint4(__float_as_uint(ce.ra.x), __float_as_uint(ce.ra.y),
+                                                        __float_as_uint(ce.ra.z), __float_as_uint(ce.ra.w));
+                fa.cache_q[(size_t)q * 2u + 1u] = ce.rb;
+            } else {
+                flag_error(fa, XR_DEVFLAG_QUEUE_OVERFLOW);
+            }
+        }
+    }
+    const bool want = ce.query && ce.train;
+    const uint32_t tmask = __ballot_sync(0xFFFFFFFFu, want);
+    bool trained = false;
+    if (tmask) {
+        const int leader = __ffs(tmask) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&fa.counters[kCntCacheTrain], (uint32_t)__popc(tmask));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (want) {
+            const uint32_t t = base + (uint32_t)__popc(tmask & ((1u << lane) - 1u));
+            if (t < fa.cache_t_cap) {
+                fa.cache_t[(size_t)t * 3u] = make_uint4(__float_as_uint(ce.ra.x), __float_as_uint(ce.ra.y),
+                                                        __float_as_uint(ce.ra.z), __float_as_uint(ce.ra.w));
+                fa.cache_t[(size_t)t * 3u + 1u] = ce.rb;
+                fa.cache_t[(size_t)t * 3u + 2u] = make_uint4(0u, 0u, 0u, 0u);
+                s.pq = __uint_as_float(t);
+                trained = true;
+            }
+        }
+    }
+    return alive && trained;
 }
 
 // Camera rays (ReSTIRGIInitialSample.rgen.hlsl:41-52) for a 16 x 8 pixel tile per
@@ -275,6 +358,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformB
         uint32_t i = base + threadIdx.x;
         PathState s;
         bool alive = false;
+        CacheEmit ce;
+        ce.query = false;
+        ce.train = false;
         if (i < count) {
             float4 a = fa.q_in[0][i], b = fa.q_in[1][i], c = fa.q_in[2][i];
             uint4 hr = fa.hits[i];
@@ -283,8 +369,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformB
             s.thr = xyz(c); s.pq = c.w;
             HitRec h;
             h.prim = (int32_t)hr.x; h.t = __uint_as_float(hr.y); h.b1 = __uint_as_float(hr.z); h.b2 = __uint_as_float(hr.w);
-            alive = shade_step<COMPAT>(fa, u, bounce, nb, s, h);
+            alive = shade_step<COMPAT>(fa, u, bounce, nb, s, h, ce);
         }
+        if (!COMPAT && fa.cache_on && bounce == 1u) alive = cache_emit(fa, ce, alive, s);
         push_path(fa, alive, s, bounce + 1u);
     }
 }
@@ -515,6 +602,46 @@ __global__ void __launch_bounds__(256) k_spatial_compat(FrameArgs fa, const XrUn
 }
 
 // ---- corrected mode ----
+// Target function: |L f(wo, wi) cos| with the BSDF of the pixel's visible point
+// (position, normal, material, wo towards the camera) -- the factor the
+// reservoir's estimate is shaded with, so W absorbs it and a glossy lobe cannot
+// turn the resampled estimate into fireflies.  Reference mode keeps the
+// reference's |L| (ReSTIRGITemporalReuse.rgen.hlsl:33-40), exact for its
+// Lambertian-only scenes up to the cosine.
+// Near-specular visible points (GGX conductor or plastic coat with roughness
+// below this) take no temporal or spatial reuse: a reconnection sample from
+// another pixel lands in their sharp lobe with a target far above the one it
+// was resampled for, and the 1/M-weighted merge turns that into fireflies; their
+// reservoir is the initial candidate alone, i.e. the path-traced estimate.
+constexpr float kReuseMinRoughness = 0.25f;
+
+struct PixelShading {
+    XrMaterial m;
+    float3 x, n, wo, T, B;
+    bool reuse;
+};
+__device__ __forceinline__ PixelShading pixel_shading(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
+                                                      float3 x, float3 n, uint32_t mat) {
+    PixelShading P;
+    P.m = fa.sc.mats[mat];
+    P.x = x;
+    P.n = n;
+    const float3 cam = xyz(mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));
+    P.wo = normalize(cam - x);
+    branchless_onb(n, &P.T, &P.B);
+    const bool glossy = (P.m.material_model == XR_MAT_METALLIC || P.m.material_model == XR_MAT_PLASTIC) &&
+                        P.m.fuzziness < kReuseMinRoughness;
+    P.reuse = !glossy;
+    return P;
+}
+__device__ __forceinline__ float target_corrected(const PixelShading& P, float3 xs, float3 L) {
+    const float3 wi = normalize(xs - P.x);
+    const float c = dot(P.n, wi);
+    if (c <= 0.0f) return 0.0f;
+    const float3 f = eval_material(P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n)).f;
+    return length(L * f * c);
+}
+
 __device__ __forceinline__ float3 shade_corrected(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
                                                   const Res& r, float3 x_view, float3 n_view, uint32_t mat) {
     float3 c = f3(0, 0, 0);
@@ -554,9 +681,10 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     Res s_new;
     s_new.xs = xyz(a); s_new.L = xyz(b); s_new.code = bw & 0x00FFFFFFu; s_new.ns = oct_decode(s_new.code, 12);
     s_new.f = f3(0, 0, 0);
+    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat);
     bool found = false;
     Res r_prev; res_init(r_prev);
-    if (fa.temporal_on) {
+    if (fa.temporal_on && P.reuse) {
         float2 puv = world_to_screen_uv(x_view, u->view_prev, u->projection_prev);
         float fx = floorf(puv.x * (float)fa.W), fy = floorf(puv.y * (float)fa.H);
         if (fx >= 0.0f && fx < (float)fa.W && fy >= 0.0f && fy < (float)fa.H) {
@@ -572,14 +700,12 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
             }
         }
     }
-    const float3 x_curr = x_view;
-    const float3 n_curr = normalize(n_view);
     Res r; res_init(r);
-    float tp_new = eval_target(s_new.xs, s_new.L, x_curr, n_curr);
+    float tp_new = target_corrected(P, s_new.xs, s_new.L);
     float w_new = (a.w > 1e-6f) ? (tp_new / a.w) : 0.0f;
     res_update(r, s_new, w_new, rng);
     if (found) {
-        float tp_prev = eval_target(r_prev.xs, r_prev.L, x_curr, n_curr);
+        float tp_prev = target_corrected(P, r_prev.xs, r_prev.L);
         res_merge(r, r_prev, tp_prev, rng);
     } else {
         r.m = 1u;
@@ -588,7 +714,7 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
         r.w_sum *= (float)fa.m_cap_t / (float)r.m;
         r.m = fa.m_cap_t;
     }
-    float tpf = eval_target(r.xs, r.L, x_curr, n_curr);
+    float tpf = target_corrected(P, r.xs, r.L);
     r.W = (tpf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * tpf) : 0.0f;
     store_packed(fa.rt_cur0, fa.rt_cur1, p, r);
     if (out_here) write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);
@@ -614,8 +740,9 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
             uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
             const float3 x_view = xyz(g);
             const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
+            const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat);
             (void)random_float(rng);   // the centre merge's draw
-            for (uint32_t i = 0; i < fa.n_nb; i++) {
+            for (uint32_t i = 0; i < (P.reuse ? fa.n_nb : 0u); i++) {
                 const uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, fa.radius, rng);
                 const uint32_t nmat = fa.gb_mat_cur[nbi];
                 if (nmat == kInvalid) continue;
@@ -626,7 +753,7 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
                 if (mat != nmat) continue;
                 Res rn;
                 load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
-                const float ph = length(rn.L) * jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
+                const float ph = target_corrected(P, rn.xs, rn.L) * jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
                 (void)random_float(rng);   // the merge's draw
                 if (ph > 0.0f) { emit_mask |= 1u << i; nb_of[i] = nbi; }
             }
@@ -701,10 +828,11 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
     const float3 x_view = xyz(g);
     const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
     const uint32_t occ = fa.visibility ? fa.occ[p] : 0u;
+    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat);
     Res center; load_packed(fa.rt_cur0, fa.rt_cur1, p, center);
     Res r; res_init(r);
-    res_merge(r, center, length(center.L), rng);
-    for (uint32_t i = 0; i < fa.n_nb; i++) {
+    res_merge(r, center, target_corrected(P, center.xs, center.L), rng);
+    for (uint32_t i = 0; i < (P.reuse ? fa.n_nb : 0u); i++) {
         uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, fa.radius, rng);
         uint32_t nmat = fa.gb_mat_cur[nbi];
         if (nmat == kInvalid) continue;
@@ -715,7 +843,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
         if (mat != nmat) continue;
         Res rn; load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
         float jac = jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
-        float ph = length(rn.L) * jac;
+        float ph = target_corrected(P, rn.xs, rn.L) * jac;
         const bool occluded = ph > 0.0f && ((occ >> i) & 1u);
         if (occluded) ph = 0.0f;
         res_merge(r, rn, ph, rng);
@@ -728,7 +856,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
         r.w_sum *= (float)fa.m_cap_s / (float)r.m;
         r.m = fa.m_cap_s;
     }
-    float phf = length(r.L);
+    float phf = target_corrected(P, r.xs, r.L);
     r.W = (phf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * phf) : 0.0f;
     store_packed(fa.rs0, fa.rs1, p, r);
     write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);

@@ -20,18 +20,6 @@ std::mutex g_err_mu;
 std::string g_last_error;
 thread_local std::string t_err_copy;
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 size_t align256(size_t v) { return (v + 255u) & ~size_t(255u); }
 }  // namespace
 
@@ -147,20 +135,26 @@ xr_status upload_ubo(Context* c, const XrUniformBufferObject* ubo) {
     return cuda_check(c, cudaEventRecord(c->ev[5], c->stream), "ubo event");
 }
 
+}  // namespace
+
 xr_status check_flags(Context* c) {
     uint32_t flags = 0;
     xr_status s = cuda_check(c, cudaMemcpy(&flags, c->d_counters + kCntError, 4, cudaMemcpyDeviceToHost), "read device flags");
     if (s) return s;
-    if (flags & ~c->error_flags) {
+    const uint32_t fresh = flags & ~c->error_flags;
+    if (fresh) {
         c->error_flags |= flags;
         std::string m = "device-side check failed:";
         if (flags & XR_DEVFLAG_STACK_OVERFLOW) m += " traversal stack overflow;";
         if (flags & XR_DEVFLAG_QUEUE_OVERFLOW) m += " path queue overflow;";
         if (flags & XR_DEVFLAG_BAD_INDEX) m += " material index out of range;";
-        return fail(c, XR_ERR_OVERFLOW, m);
+        if (flags & XR_DEVFLAG_MMA_TIMEOUT) m += " radiance-cache tensor-core wait timed out;";
+        return fail(c, fresh == XR_DEVFLAG_MMA_TIMEOUT ? XR_ERR_TIMEOUT : XR_ERR_OVERFLOW, m);
     }
     return XR_OK;
 }
+
+namespace {
 
 xr_status validate_params(const Context* c, const XrParams* p) {
     if (!p) return fail(c, XR_ERR_INVALID_ARGUMENT, "params: null");
@@ -223,6 +217,7 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
         return fail(nullptr, XR_ERR_CUDA, std::string("create: no CUDA device (") + cudaGetErrorString(e) + ")");
     if (desc->device < 0 || desc->device >= ndev) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "create: bad device ordinal");
     XrContext* c = new XrContext();
+    xr_cache_params_default(&c->cache.params);
     c->device = desc->device;
     DeviceGuard g(c->device);
     xr_status s = XR_OK;
@@ -237,7 +232,7 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     if ((s = cuda_check(c, cudaMemset(c->d_work, 0, 2 * sizeof(unsigned long long)), "work counters"))) goto bad;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_ubo, sizeof(XrUniformBufferObject)), "ubo"))) goto bad;
     if ((s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, sizeof(XrUniformBufferObject)), "ubo staging"))) goto bad;
-    for (int i = 0; i < 6; i++)
+    for (int i = 0; i < 8; i++)
         if ((s = cuda_check(c, cudaEventCreate(&c->ev[i]), "event"))) goto bad;
     for (int i = 0; i < 8; i++)
         if ((s = cuda_check(c, cudaEventCreate(&c->user_ev[i]), "event"))) goto bad;
@@ -261,10 +256,11 @@ void xr_destroy(XrContext* c) {
     DeviceGuard g(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_pixels(c);
+    cache_free(c);
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
     cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo); cudaFree(c->d_work);
     if (c->h_ubo) cudaFreeHost(c->h_ubo);
-    for (int i = 0; i < 6; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i < 8; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -325,6 +321,7 @@ xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const ui
     if ((s = cuda_check(c, cudaGetLastError(), "scene upload"))) return s;
     c->nv = nv; c->ntri = ntri; c->nm = nm;
     c->scene_has_non_lambert = non_lambert;
+    cache_scene_bounds(c, reinterpret_cast<const float*>(v), nv);
     c->scene_ready = true;
     return XR_OK;
 }
@@ -377,10 +374,12 @@ xr_status xr_render_frame(XrContext* c, const XrUniformBufferObject* ubo) {
     xr_status s = upload_ubo(c, ubo);
     if (s) return s;
     set_frame_pointers(c, ubo->current_frame % 2u);
+    if ((s = cache_prepare_frame(c, ubo->current_frame))) return s;
     cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);   // keep the sticky error word
     const bool compat = c->params.compat_reference != 0;
     cudaEventRecord(c->ev[0], c->stream);
     launch_initial(c->fa, ubo->number_of_bounces, c->stream);
+    cache_after_paths(c);   // radiance-cache inference and training (when enabled)
     cudaEventRecord(c->ev[1], c->stream);
     bool temporal_writes_image = compat ? (ubo->reuse == 0u) : (c->params.spatial_on == 0u);
     launch_temporal(c->fa, temporal_writes_image, c->stream);
@@ -411,6 +410,9 @@ xr_status xr_render_reference(XrContext* c, const XrUniformBufferObject* ubo, ui
         u.current_frame = frame0 + k;
         if ((s = upload_ubo(c, &u))) break;
         set_frame_pointers(c, u.current_frame % 2u);
+        c->fa.cache_on = 0;   // the converged reference is the plain path tracer
+        c->fa.cache_sel_n = 0;
+        c->cache.frame_used = false;
         cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);
         launch_initial(c->fa, u.number_of_bounces, c->stream);
         launch_accumulate_sample(c->fa, acc, c->stream);

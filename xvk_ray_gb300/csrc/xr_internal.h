@@ -24,6 +24,12 @@
 #include "../../include/xr.h"
 
 #ifdef __CUDACC__
+#include <cuda_fp16.h>
+#else
+struct __half2;
+#endif
+
+#ifdef __CUDACC__
 #include <cuda_runtime.h>
 #else
 #include <cuda_runtime_api.h>
@@ -40,6 +46,8 @@ constexpr uint32_t kCntFetchPath = 64;     // + bounce: ray-fetch counter of tha
 constexpr uint32_t kCntFetchShadow = 96;   // ray-fetch counter of the shadow trace
 constexpr uint32_t kCntFetchQuery = 97;    // ray-fetch counter of xr_trace_rays
 constexpr uint32_t kCntNonFinite = 98;     // rays ended early for a non-finite origin or direction
+constexpr uint32_t kCntCacheQuery = 99;    // radiance-cache query records of the frame
+constexpr uint32_t kCntCacheTrain = 100;   // radiance-cache training records of the frame
 constexpr uint32_t kCntError = 127;        // sticky XR_DEVFLAG_* bits
 constexpr uint32_t kCounterWords = 128;
 constexpr uint32_t kMaxBounces = 31;
@@ -102,6 +110,40 @@ struct FrameArgs {
     uint32_t* occ;            // per pixel: occluded neighbour slots
     uint32_t* counters;       // [b] paths entering bounce b, then the kCnt* words above
     uint32_t grid_persistent, grid_trace;
+    // learned radiance cache (corrected mode): paths end at x_s unless selected for training
+    uint32_t cache_on;
+    uint4* cache_q;           // query records, 2 uint4 each (capacity N)
+    uint4* cache_t;           // training records, 3 uint4 each (capacity cache_t_cap)
+    uint32_t cache_t_cap;
+    uint32_t cache_sel_n;     // training pixels: (pixel * 2^31-1 + cache_sel_off) mod N < cache_sel_n
+    uint32_t cache_sel_off;
+};
+
+// Learned radiance cache state (nrc.cu, cache_api.cu).
+struct CacheState {
+    bool allocated = false;
+    bool grads_dirty = false;        // gradients left by a gradient-only xr_cache_train
+    XrCacheParams params{};
+    float lo[3] = {0.0f, 0.0f, 0.0f};
+    float inv_ext = 1.0f;
+    uint32_t step = 0;               // Adam steps taken
+    float* mlp = nullptr;            // FP32 master weights (17,408)
+    float* mlp_grad = nullptr;
+    float* mlp_m = nullptr;
+    float* mlp_v = nullptr;
+    uint8_t* w_fwd = nullptr;        // bfloat16 weight images (shared-memory layout)
+    uint8_t* w_bwd = nullptr;
+    float* grid = nullptr;           // FP32 master table (16 x 2^19 x 2)
+    __half2* table = nullptr;        // binary16 table used by the kernels
+    float* grid_grad = nullptr;
+    float* grid_m = nullptr;
+    float* grid_v = nullptr;
+    float* loss = nullptr;           // mean loss of the last training launch
+    uint4* queries = nullptr;        // query records (capacity query_cap)
+    uint4* train = nullptr;          // training records (capacity train_cap)
+    uint32_t query_cap = 0, train_cap = 0;
+    bool frame_used = false;         // the last frame ran with the cache
+    bool frame_trained = false;
 };
 
 struct Context {
@@ -148,13 +190,28 @@ struct Context {
     unsigned long long* d_work = nullptr;   // node visits, triangle tests of the last ray query
     uint64_t query_rays = 0;
     uint32_t error_flags = 0;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[8] = {};          // 0..3 frame passes, 5 UBO staging, 6/7 cache inference / training
     cudaEvent_t user_ev[8] = {};
     XrStats stats{};
+    CacheState cache;
 };
 
 xr_status fail(const Context* ctx, xr_status code, const std::string& msg);
 xr_status cuda_check(Context* ctx, cudaError_t e, const char* what);
+xr_status check_flags(Context* c);   // reads the sticky device error word; new bits -> error status
+
+// Makes `dev` current for the scope of a C ABI call and restores the caller's device.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
 
 // ---- launch wrappers (bvh_build.cu) ----
 xr_status build_bvh(Context* ctx);
@@ -176,6 +233,23 @@ void launch_export_res_wide(float4* const planes[4], uint32_t n, uint32_t* out, 
 void launch_export_res_packed(const float4* p0, const float4* p1, uint32_t n, uint32_t* out, cudaStream_t st);
 void launch_import_res_wide(float4* const planes[4], uint32_t n, const uint32_t* in, cudaStream_t st);
 void launch_import_res_packed(float4* p0, float4* p1, uint32_t n, const uint32_t* in, cudaStream_t st);
+
+// ---- launch wrappers (nrc.cu) ----
+cudaError_t cache_configure_kernels();
+void launch_cache_init(CacheState& cs, uint32_t seed, cudaStream_t st);
+void launch_cache_refresh(CacheState& cs, cudaStream_t st);   // binary16 table + bfloat16 images from the masters
+void launch_cache_pack(const XrCacheSample* s, uint32_t n, uint4* rec, uint32_t stride, cudaStream_t st);
+// count from *count_ptr (device) when non-null, else count_host; cand_b non-null: add to candidates
+void launch_cache_infer(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host, float* out3,
+                        float4* cand_b, uint32_t* err, int sm_count, cudaStream_t st);
+void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                        uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st);
+void launch_cache_adam(CacheState& cs, cudaStream_t st);   // one Adam step (cs.step incremented) on the gradients
+// ---- cache_api.cu ----
+xr_status cache_prepare_frame(Context* c, uint32_t frame);   // capacities; sets the FrameArgs cache fields
+void cache_after_paths(Context* c);           // inference (+ training) after the bounce loop
+void cache_free(Context* c);
+void cache_scene_bounds(Context* c, const float* vertices, uint32_t nv);
 
 }  // namespace xr
 
