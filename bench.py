@@ -168,24 +168,67 @@ def relmse(img: "np.ndarray", ref: "np.ndarray") -> float:
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + RELMSE_EPS)))
 
 
-def measure_relmse(xr, scene, ubos, frames: int, ref_spp: int, device: int) -> dict:
-    """relMSE of plain ReSTIR GI and of the 1-spp path tracer after `frames` frames of
-    the camera path, against the FP64-accumulated reference of the last frame's camera."""
+RELMSE_EVAL_FRAMES = (16, 24, 32, 40, 48)
+
+
+def measure_relmse(xr, scene, ubos, eval_frames, ref_spp: int, device: int, train_samples: int = 65536) -> dict:
+    """relMSE of plain ReSTIR GI, of ReSTIR GI with the learned radiance cache and
+    of the 1-spp path tracer along the camera path, each against the
+    FP64-accumulated reference (plain path tracer, `ref_spp` samples) of the
+    evaluation frame's camera, averaged over the evaluation frames.  Both ReSTIR
+    variants render every frame of the path in their own context; their frame
+    times (library CUDA events, median) give the equal-time comparison."""
+    import numpy as np
     L = xr._lib
-    r = xr.Renderer(W, H, device=device)
-    r.set_params(xr.params_default(W, H, write_hdr=1, write_pt=1))
-    r.upload_scene(scene)
-    r.build_bvh()
-    for u in ubos[:frames]:
-        r.render(u)
-    hdr = r.read_output(L.XR_OUT_HDR)
-    pt = r.read_output(L.XR_OUT_PT)
-    t0 = time.perf_counter()
-    ref = r.render_reference(ubos[frames - 1], 1_000_000, ref_spp)
-    ref_s = time.perf_counter() - t0
-    r.close()
-    return {"restir_gi": relmse(hdr, ref), "pt_1spp": relmse(pt, ref), "restir_gi_mlp_cache": None,
-            "reference": f"FP64-accumulated path tracer, {ref_spp} spp, same path depth; frame {frames - 1}",
+    n = max(eval_frames)
+    refs, ref_s = {}, 0.0
+    out = {}
+    for variant in ("restir_gi", "restir_gi_mlp_cache"):
+        r = xr.Renderer(W, H, device=device)
+        r.set_params(xr.params_default(W, H, write_hdr=1, write_pt=1))
+        r.upload_scene(scene)
+        r.build_bvh()
+        cache = variant == "restir_gi_mlp_cache"
+        if cache:
+            cp = xr.cache_params_default()
+            cp.enabled = 1
+            cp.train_samples = train_samples
+            r.cache.set_params(cp)
+        rel, rel_pt, ms, infer, train = [], [], [], [], []
+        for f, u in enumerate(ubos[:n]):
+            r.render(u)
+            st = r.stats()
+            ms.append(st.ms_frame)
+            if cache:
+                cs = r.cache.stats()
+                infer.append(cs.ms_infer)
+                train.append(cs.ms_train)
+            if f + 1 in eval_frames:
+                hdr = r.read_output(L.XR_OUT_HDR)
+                if f + 1 not in refs:
+                    t0 = time.perf_counter()
+                    refs[f + 1] = r.render_reference(u, 1_000_000, ref_spp)
+                    ref_s += time.perf_counter() - t0
+                rel.append(relmse(hdr, refs[f + 1]))
+                if not cache:
+                    rel_pt.append(relmse(r.read_output(L.XR_OUT_PT), refs[f + 1]))
+        entry = {"relmse": float(np.mean(rel)), "per_frame": [round(v, 4) for v in rel],
+                 "ms_per_frame": round(statistics.median(ms[8:]), 4)}
+        if cache:
+            cs = r.cache.stats()
+            entry.update({"ms_infer": round(statistics.median(infer[8:]), 4),
+                          "ms_train": round(statistics.median(train[8:]), 4), "queries": cs.queries,
+                          "train_samples": cs.train_samples, "adam_steps": cs.steps, "loss": round(cs.loss, 4)})
+        else:
+            out["pt_1spp"] = float(np.mean(rel_pt))
+        out[variant] = entry
+        r.close()
+    plain, cached = out["restir_gi"], out["restir_gi_mlp_cache"]
+    return {"restir_gi": plain["relmse"], "restir_gi_mlp_cache": cached["relmse"], "pt_1spp": out["pt_1spp"],
+            "ratio_cache_over_plain": round(cached["relmse"] / plain["relmse"], 4),
+            "detail": {"restir_gi": plain, "restir_gi_mlp_cache": cached},
+            "reference": f"FP64-accumulated plain path tracer, {ref_spp} spp, same path depth, "
+                         f"at frames {list(eval_frames)} of the camera path",
             "eps": RELMSE_EPS, "reference_seconds": round(ref_s, 2)}
 
 
@@ -324,7 +367,7 @@ def run_ours(args):
         return
     rel = None
     if args.relmse_spp > 0:
-        rel = measure_relmse(xr, scene, ubos, min(24, len(ubos)), args.relmse_spp, local)
+        rel = measure_relmse(xr, scene, ubos, RELMSE_EVAL_FRAMES, args.relmse_spp, local)
     peaks = _peaks()
     hbm = peaks.get("hbm_gbs")
     peak_note = "measured" if hbm else "fallback"

@@ -130,7 +130,15 @@ struct Scene {
     std::vector<BNode> nodes;
     std::vector<uint32_t> order;
     bool brute = true;
+    // emissive triangles (next-event estimation of the radiance cache's training paths)
+    std::vector<uint32_t> light_prim;
+    std::vector<float> light_cdf, light_pmf, prim_light_pdf;
 };
+
+// Light-sampling tables: power = area * luminance(4 * base colour) per
+// DiffuseLight triangle, pmf = power / total, inclusive CDF in primitive order
+// (last entry 1), per primitive pmf / area.
+void build_lights(Scene& s);
 
 struct RayPre { f3 o, d; int kx, ky, kz; float Sx, Sy, Sz; };
 inline RayPre prep_ray(f3 o, f3 d) {
@@ -541,6 +549,82 @@ inline uint8_t to_unorm8(float v) {
     return (uint8_t)(int)(v * 255.0f + 0.5f);
 }
 
+void build_lights(Scene& s) {
+    std::vector<float> area, power;
+    for (uint32_t t = 0; t < s.ntri; t++) {
+        const int32_t mi = vert_mat(s, s.idx[(size_t)t * 3]);
+        if (mi < 0 || (uint32_t)mi >= s.nm || s.mat[mi].model != MAT_DIFFUSE_LIGHT) continue;
+        const f3 cr = cross(s.p2[t] - s.p0[t], s.p1[t] - s.p0[t]);
+        const float a = 0.5f * sqrtf(dot(cr, cr));
+        const float lr = s.mat[mi].base[0] * 4.0f, lg = s.mat[mi].base[1] * 4.0f, lb = s.mat[mi].base[2] * 4.0f;
+        const float lum = 0.2126f * lr + 0.7152f * lg + 0.0722f * lb;
+        const float pw = a * lum;
+        if (!(pw > 0.0f) || !std::isfinite(pw)) continue;
+        s.light_prim.push_back(t);
+        area.push_back(a);
+        power.push_back(pw);
+    }
+    const size_t n = s.light_prim.size();
+    s.prim_light_pdf.assign(s.ntri, 0.0f);
+    if (n == 0) return;
+    float total = 0.0f;
+    for (float pw : power) total = total + pw;
+    s.light_pmf.resize(n);
+    s.light_cdf.resize(n);
+    float run = 0.0f;
+    for (size_t k = 0; k < n; k++) {
+        s.light_pmf[k] = power[k] / total;
+        run = run + s.light_pmf[k];
+        s.light_cdf[k] = run;
+        s.prim_light_pdf[s.light_prim[k]] = s.light_pmf[k] / area[k];
+    }
+    s.light_cdf[n - 1] = 1.0f;
+}
+
+// Next-event estimation of a training path's vertex x (shading normal n,
+// geometric normal g facing wo): light by power (binary search of the CDF),
+// uniform point (square-root parameterisation), balance heuristic against the
+// BSDF sampling pdf; the contribution is added when the shadow ray is clear.
+// Consumes three random numbers in every case.
+f3 next_event(const Scene& sc, const Material& mat, f3 x, f3 n, f3 g, f3 wo, f3 thr, uint32_t& rng) {
+    const f3 zero{0.0f, 0.0f, 0.0f};
+    const float u0 = random_float(rng), u1 = random_float(rng), u2 = random_float(rng);
+    const uint32_t nl_count = (uint32_t)sc.light_prim.size();
+    if (nl_count == 0) return zero;
+    uint32_t lo = 0, hi = nl_count - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (u0 < sc.light_cdf[mid]) hi = mid;
+        else lo = mid + 1;
+    }
+    const uint32_t prim = sc.light_prim[lo];
+    const f3 p0 = sc.p0[prim], p1 = sc.p1[prim], p2 = sc.p2[prim];
+    const float su = sqrtf(u1);
+    const float b0 = 1.0f - su, b1 = u2 * su, b2 = 1.0f - b0 - b1;
+    const f3 y = p0 * b0 + p1 * b1 + p2 * b2;
+    const f3 nl = normalize(cross(p2 - p0, p1 - p0));
+    const f3 dv = y - x;
+    const float dist2 = dot(dv, dv);
+    const float dist = sqrtf(dist2);
+    if (!(dist > 0.05f)) return zero;
+    const f3 wi = dv * (1.0f / dist);
+    const float cos_l = fabsf(dot(nl, wi));
+    if (!(cos_l > 1e-6f)) return zero;
+    f3 T, B;
+    branchless_onb(n, &T, &B);
+    const f3 wil = to_local(wi, T, B, n);
+    if (!(wil.z > 0.0f)) return zero;
+    const Lobe lb = eval_material(mat, to_local(wo, T, B, n), wil);
+    const float pdf_l = sc.prim_light_pdf[prim] * dist2 / cos_l;
+    const Material& lm = sc.mat[vert_mat(sc, sc.idx[(size_t)prim * 3])];
+    const f3 Le = f3{lm.base[0], lm.base[1], lm.base[2]} * 4.0f;
+    const f3 contrib = thr * Le * lb.f * (wil.z / (pdf_l + lb.pdf));
+    if (!(contrib.x + contrib.y + contrib.z > 0.0f)) return zero;
+    const f3 off = dot(wi, g) > 0.0f ? g : -g;
+    const Hit h = trace(sc, x + off * 0.01f, wi, 0.0f, dist - 0.02f, true);
+    return h.prim >= 0 ? zero : contrib;
+}
+
 // ----------------------------------------------------------------------------
 // The renderer: initial sample, temporal, spatial (ApplicationReSTIRGI.cpp:150-275)
 // ----------------------------------------------------------------------------
@@ -620,6 +704,7 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
     bool cache_query = false, cache_train = false;
     uint32_t rec[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const bool cache = !compat && R.cache_on;
+    float prev_pdf = 0.0f;   // cache training paths: sampling pdf of the previous vertex (MIS)
     const f3 sky{1, 1, 1};
     for (uint32_t bounce = 0;; bounce++) {
         if (bounce == u.number_of_bounces) break;
@@ -645,7 +730,16 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         }
         if (mat.model == MAT_DIFFUSE_LIGHT) {
             f3 Le = f3{mat.base[0], mat.base[1], mat.base[2]} * 4.0f;
-            L_out = L_out + throughput * f3{mat.base[0], mat.base[1], mat.base[2]} * 4.0f;
+            f3 term = throughput * f3{mat.base[0], mat.base[1], mat.base[2]} * 4.0f;
+            if (cache && bounce >= 2) {
+                // balance heuristic against the previous vertex's next-event estimate
+                const float lp = sc.light_prim.empty() ? 0.0f : sc.prim_light_pdf[h.prim];
+                const float cos_l = fabsf(dot(pl.geo_normal, direction));
+                const float pdf_l = (lp > 0.0f && cos_l > 1e-6f && pl.hit_t > 0.05f)
+                                        ? lp * (pl.hit_t * pl.hit_t) / cos_l : 0.0f;
+                term = term * (prev_pdf / (prev_pdf + pdf_l));
+            }
+            L_out = L_out + term;
             if (bounce == 1) { x_sample = pl.pos; n_sample = pl.normal; has_sample = true; }
             if (bounce == 0) { x_view = pl.pos; n_view = pl.normal; le0 = Le; }
             break;
@@ -655,6 +749,9 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         f3 wo = -direction;
         if (bounce == 1) { x_sample = pl.pos; n_sample = pl.normal; has_sample = true; }
         uint32_t seed_this = rng;
+        if (cache && bounce >= 1 && bounce + 1 < u.number_of_bounces &&
+            (bounce >= 2 || cache_training_pixel(R, p, u.current_frame)))
+            L_out = L_out + next_event(sc, mat, pl.pos, pl.normal, pl.geo_normal, wo, throughput, rng);
         f3 f = sample_bsdf(compat, pl.normal, mat, wo, &wi, &pdf, &cos_theta, rng);
         f3 factor = f * cos_theta / f3{pdf, pdf, pdf};
         if (!compat && !(pdf > 0.0f)) factor = f3{0, 0, 0};
@@ -693,6 +790,7 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
         f3 off = dot(wi, gn) > 0.0f ? gn : -gn;
         o = hit_position + off * 0.01f;
         direction = wi;
+        prev_pdf = pdf;
     }
     if (cache) {
         R.cache_q_valid[p] = cache_query;
@@ -809,12 +907,17 @@ void shade_output(Renderer& R, uint32_t p, const Reservoir& r, const Sample& s_n
         float cos_theta = fmaxf(0.0f, dot(n_curr, wi));
         f3 f = r.s.f;
         if (!R.compat) {
-            const Material& m = R.sc->mat[s_new.materialID];
-            f3 cam = xyz(mul(u.view_inverse, f4{0, 0, 0, 1}));
-            f3 wo = normalize(cam - x_curr);
-            f3 T, B;
-            branchless_onb(n_curr, &T, &B);
-            f = eval_material(m, to_local(wo, T, B, n_curr), to_local(wi, T, B, n_curr)).f;
+            // corrected mode: the pixel's BSDF along the reconnection direction; a
+            // near-specular pixel (no reuse) takes the path tracer's ratio f cos / pdf
+            // at that one direction (the sampled direction left from a point offset
+            // along the normal, and in a sharp lobe f alone varies by orders of
+            // magnitude over that angle)
+            const PixelShading P = pixel_shading(R, s_new, u);
+            const Lobe lb = eval_material(*P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n));
+            if (P.reuse) color = r.s.L_out * r.W * lb.f * cos_theta;
+            else if (lb.pdf > 0.0f) color = r.s.L_out * lb.f * (cos_theta / lb.pdf);
+            write_output(R, p, color, true);
+            return;
         }
         color = r.s.L_out * r.W * f * cos_theta;
     }
@@ -1059,6 +1162,7 @@ void* or_scene_create(const float* vertices, uint32_t nv, const uint32_t* indice
     }
     s->brute = ntri <= 256;
     if (!s->brute) build_bvh(*s);
+    build_lights(*s);
     return s;
 }
 void or_scene_destroy(void* scene) { delete (Scene*)scene; }

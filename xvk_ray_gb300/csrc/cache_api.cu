@@ -111,9 +111,12 @@ xr_status ensure_records(Context* c, uint32_t queries, uint32_t train) {
     }
     if (train > cs.train_cap) {
         cudaFree(cs.train);
+        cudaFree(cs.nee);
         cs.train = nullptr;
+        cs.nee = nullptr;
         cs.train_cap = 0;
         if ((s = cuda_check(c, cudaMalloc((void**)&cs.train, (size_t)train * 48), "cache training records"))) return s;
+        if ((s = cuda_check(c, cudaMalloc((void**)&cs.nee, (size_t)train * 48), "cache next-event rays"))) return s;
         cs.train_cap = train;
     }
     return XR_OK;
@@ -148,7 +151,7 @@ xr_status upload_samples(Context* c, const XrCacheSample* s, uint32_t n, uint32_
 void cache_free(Context* c) {
     CacheState& cs = c->cache;
     void* ptrs[] = {cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.grid, cs.grid_grad, cs.grid_m, cs.grid_v,
-                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.queries, cs.train};
+                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.queries, cs.train, cs.nee};
     for (void* p : ptrs) cudaFree(p);
     cs = CacheState{};
 }
@@ -194,6 +197,7 @@ xr_status cache_prepare_frame(Context* c, uint32_t frame) {
     fa.cache_on = 1;
     fa.cache_q = cs.queries;
     fa.cache_t = cs.train;
+    fa.cache_nee = cs.nee;
     fa.cache_t_cap = tcap;
     fa.cache_sel_n = tcap < c->N ? tcap : c->N;
     fa.cache_sel_off = (uint32_t)(((uint64_t)frame * 2654435761ull) % (uint64_t)c->N);

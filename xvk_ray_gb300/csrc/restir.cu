@@ -103,11 +103,11 @@ __device__ __forceinline__ void add_radiance(const FrameArgs& fa, uint32_t p, fl
 
 // Radiance found at bounce >= 2.  With the radiance cache on, only training
 // paths live past bounce 1, and what they find is the training target of their
-// record (index carried in the p_q slot, which is free after bounce 1).
+// record (index carried in the pixel slot, which they no longer need).
 template <bool COMPAT>
 __device__ __forceinline__ void add_suffix_radiance(const FrameArgs& fa, const PathState& s, float3 add) {
     if (!COMPAT && fa.cache_on) {
-        float4* tgt = reinterpret_cast<float4*>(fa.cache_t + (size_t)__float_as_uint(s.pq) * 3u + 2u);
+        float4* tgt = reinterpret_cast<float4*>(fa.cache_t + (size_t)s.pixel * 3u + 2u);
         float4 v = *tgt;
         *tgt = make_float4(v.x + add.x, v.y + add.y, v.z + add.z, v.w);
     } else {
@@ -115,12 +115,74 @@ __device__ __forceinline__ void add_suffix_radiance(const FrameArgs& fa, const P
     }
 }
 
-// What the shading of bounce 1 hands to the radiance cache (corrected mode).
+// Next-event estimation of the radiance cache's training paths: a light picked
+// with probability pmf (its share of the emitted power) by binary search of the
+// CDF, a uniform point on it (square-root parameterisation), and the balance
+// heuristic against the BSDF sampling of the same vertex, so the contribution is
+// thr Le f cos / (pdf_light + pdf_bsdf); an emitter reached by BSDF sampling
+// takes the complementary weight.  Same expectation as the plain path tracer's
+// emission-only estimate, far lower variance for the small lights.
+struct NeeRay {
+    bool valid;
+    float3 o, d, contrib;
+    float tmax;
+};
+
+__device__ __forceinline__ uint32_t pick_light(const DeviceScene& sc, float u) {
+    uint32_t lo = 0, hi = sc.n_lights - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (u < sc.light_cdf[mid]) hi = mid;
+        else lo = mid + 1u;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ NeeRay next_event(const DeviceScene& sc, const XrMaterial& mat, float3 x, float3 n,
+                                             float3 g, float3 wo, float3 thr, uint32_t& rng) {
+    NeeRay r;
+    r.valid = false;
+    const float u0 = random_float(rng), u1 = random_float(rng), u2 = random_float(rng);
+    if (sc.n_lights == 0u) return r;
+    const uint32_t prim = sc.light_prim[pick_light(sc, u0)];
+    const uint4 id = __ldg(sc.tri_idx + prim);
+    const float3 p0 = xyz(__ldg(sc.vpos + id.x)), p1 = xyz(__ldg(sc.vpos + id.y)), p2 = xyz(__ldg(sc.vpos + id.z));
+    const float su = sqrtf(u1);
+    const float b0 = 1.0f - su, b1 = u2 * su, b2 = 1.0f - b0 - b1;
+    const float3 y = p0 * b0 + p1 * b1 + p2 * b2;
+    const float3 nl = normalize(cross(p2 - p0, p1 - p0));
+    const float3 dv = y - x;
+    const float dist2 = dot(dv, dv);
+    const float dist = sqrtf(dist2);
+    if (!(dist > 0.05f)) return r;
+    const float3 wi = dv * (1.0f / dist);
+    const float cos_l = fabsf(dot(nl, wi));
+    if (!(cos_l > 1e-6f)) return r;
+    float3 T, B;
+    branchless_onb(n, &T, &B);
+    const float3 wil = to_local(wi, T, B, n);
+    if (!(wil.z > 0.0f)) return r;
+    const Lobe lb = eval_material(mat, to_local(wo, T, B, n), wil);
+    const float pdf_l = sc.prim_light_pdf[prim] * dist2 / cos_l;
+    const XrMaterial& lm = sc.mats[id.w];
+    const float3 Le = f3(lm.base_color[0], lm.base_color[1], lm.base_color[2]) * 4.0f;
+    r.contrib = thr * Le * lb.f * (wil.z / (pdf_l + lb.pdf));
+    if (!(r.contrib.x + r.contrib.y + r.contrib.z > 0.0f)) return r;
+    const float3 off = dot(wi, g) > 0.0f ? g : -g;
+    r.o = x + off * 0.01f;
+    r.d = wi;
+    r.tmax = dist - 0.02f;
+    r.valid = true;
+    return r;
+}
+
+// What the shading of a bounce hands to the radiance cache (corrected mode).
 struct CacheEmit {
-    bool query;        // x_s is a surface: the candidate takes the cache's radiance
-    bool train;        // the pixel is one of the frame's training pixels
+    bool query;        // bounce 1: x_s is a surface, the candidate takes the cache's radiance
+    bool train;        // bounce 1: the pixel is one of the frame's training pixels
     float4 ra;         // record {x_s, pixel}
     uint4 rb;          // record {oct16(n_s), oct16(wo), albedo | kind, roughness}
+    NeeRay nee;        // training paths: the next-event ray of this vertex
 };
 
 __device__ __forceinline__ bool cache_training_pixel(const FrameArgs& fa, uint32_t pixel) {
@@ -175,7 +237,16 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
             float3 L = f3(0.0f, 0.0f, 0.0f) + term;
             write_sample<COMPAT>(fa, p, pl.pos, pl.normal, L, s.pq);
         } else {
-            add_suffix_radiance<COMPAT>(fa, s, term);
+            float3 add = term;
+            if (!COMPAT && fa.cache_on) {
+                // balance heuristic against the previous vertex's next-event estimate
+                // (its sampling pdf is carried in the p_q slot)
+                const float lp = fa.sc.n_lights ? fa.sc.prim_light_pdf[h.prim] : 0.0f;   // no tables without lights
+                const float cos_l = fabsf(dot(pl.geo, s.d));
+                const float pdf_l = (lp > 0.0f && cos_l > 1e-6f && pl.t > 0.05f) ? lp * (pl.t * pl.t) / cos_l : 0.0f;
+                add = term * (s.pq / (s.pq + pdf_l));
+            }
+            add_suffix_radiance<COMPAT>(fa, s, add);
         }
         return false;
     }
@@ -184,6 +255,9 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
     const float3 wo = -s.d;
     const float3 x_s = pl.pos, n_s = pl.normal;
     const uint32_t seed_this = s.rng;
+    if (!COMPAT && fa.cache_on && bounce >= 1u && bounce + 1u < nb &&
+        (bounce >= 2u || cache_training_pixel(fa, p)))
+        ce.nee = next_event(fa.sc, mat, pl.pos, pl.normal, pl.geo, wo, s.thr, s.rng);
     float3 f = sample_bsdf<COMPAT>(pl.normal, mat, wo, &wi, &pdf, &cos_theta, s.rng);
     float3 factor = div3(f * cos_theta, pdf);
     if (!COMPAT && !(pdf > 0.0f)) factor = f3(0.0f, 0.0f, 0.0f);
@@ -231,6 +305,9 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
         s.o = hit_pos + off * 0.01f;
         s.d = wi;
         if (bounce == 0) s.thr = f3(1.0f, 1.0f, 1.0f);
+        // training paths of the cache carry their sampling pdf for the MIS weight
+        // of an emitter at the next vertex (p_q was written with the sample above)
+        if (!COMPAT && fa.cache_on && bounce >= 1u) s.pq = pdf;
     }
     return alive;
 }
@@ -255,6 +332,28 @@ __device__ __forceinline__ void push_path(const FrameArgs& fa, bool alive, const
 // query per surface x_s, appended with one atomic per warp; training pixels also
 // take a training record (target zero, filled by the rest of the path) and keep
 // their path alive with the record index in the p_q slot; every other path ends.
+// Appends the valid next-event rays of the warp (all lanes call this) for the
+// training record `rec`.
+__device__ __forceinline__ void push_nee(const FrameArgs& fa, bool valid, const NeeRay& r, uint32_t rec) {
+    const uint32_t lane = lane_id();
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, valid);
+    if (mask == 0u) return;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(&fa.counters[kCntCacheNee], (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (valid) {
+        const uint32_t i = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+        if (i < fa.cache_t_cap) {
+            fa.cache_nee[(size_t)i * 3u] = f4(r.o, __uint_as_float(rec));
+            fa.cache_nee[(size_t)i * 3u + 1u] = f4(r.d, r.tmax);
+            fa.cache_nee[(size_t)i * 3u + 2u] = f4(r.contrib, 0.0f);
+        } else {
+            flag_error(fa, XR_DEVFLAG_QUEUE_OVERFLOW);
+        }
+    }
+}
+
 __device__ __forceinline__ bool cache_emit(const FrameArgs& fa, const CacheEmit& ce, bool alive, PathState& s) {
     const uint32_t lane = lane_id();
     const uint32_t qmask = __ballot_sync(0xFFFFFFFFu, ce.query);
@@ -289,11 +388,12 @@ __device__ __forceinline__ bool cache_emit(const FrameArgs& fa, const CacheEmit&
                                                         __float_as_uint(ce.ra.z), __float_as_uint(ce.ra.w));
                 fa.cache_t[(size_t)t * 3u + 1u] = ce.rb;
                 fa.cache_t[(size_t)t * 3u + 2u] = make_uint4(0u, 0u, 0u, 0u);
-                s.pq = __uint_as_float(t);
+                s.pixel = t;
                 trained = true;
             }
         }
     }
+    push_nee(fa, trained && ce.nee.valid, ce.nee, s.pixel);
     return alive && trained;
 }
 
@@ -361,6 +461,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformB
         CacheEmit ce;
         ce.query = false;
         ce.train = false;
+        ce.nee.valid = false;
         if (i < count) {
             float4 a = fa.q_in[0][i], b = fa.q_in[1][i], c = fa.q_in[2][i];
             uint4 hr = fa.hits[i];
@@ -372,6 +473,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformB
             alive = shade_step<COMPAT>(fa, u, bounce, nb, s, h, ce);
         }
         if (!COMPAT && fa.cache_on && bounce == 1u) alive = cache_emit(fa, ce, alive, s);
+        if (!COMPAT && fa.cache_on && bounce >= 2u) push_nee(fa, ce.nee.valid, ce.nee, s.pixel);
         push_path(fa, alive, s, bounce + 1u);
     }
 }
@@ -642,16 +744,21 @@ __device__ __forceinline__ float target_corrected(const PixelShading& P, float3 
     return length(L * f * c);
 }
 
-__device__ __forceinline__ float3 shade_corrected(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
-                                                  const Res& r, float3 x_view, float3 n_view, uint32_t mat) {
+// Final shading of a reservoir at its pixel: L W f cos along the reconnection
+// direction.  A near-specular pixel (no reuse: its reservoir is its own
+// candidate) is shaded with the path tracer's ratio f cos / pdf evaluated at that
+// one direction instead: the reconnection direction from the visible point
+// differs slightly from the sampled one (the path left from a point offset
+// along the normal), and in a lobe that sharp f alone changes by orders of
+// magnitude over that angle while the ratio stays bounded.
+__device__ __forceinline__ float3 shade_corrected(const PixelShading& P, const Res& r) {
     float3 c = f3(0, 0, 0);
-    if (r.W > 0.0f && mat < fa.sc.n_mats) {
-        float3 wi = normalize(r.xs - x_view);
-        float ct = fmaxf(0.0f, dot(n_view, wi));
-        float3 cam = xyz(mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));
-        float3 wo = normalize(cam - x_view);
-        float3 f = eval_world(fa.sc.mats[mat], n_view, wo, wi);
-        c = r.L * r.W * f * ct;
+    if (r.W > 0.0f) {
+        const float3 wi = normalize(r.xs - P.x);
+        const float ct = fmaxf(0.0f, dot(P.n, wi));
+        const Lobe lb = eval_material(P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n));
+        if (P.reuse) c = r.L * r.W * lb.f * ct;
+        else if (lb.pdf > 0.0f) c = r.L * lb.f * (ct / lb.pdf);
     }
     return c;
 }
@@ -717,7 +824,7 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     float tpf = target_corrected(P, r.xs, r.L);
     r.W = (tpf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * tpf) : 0.0f;
     store_packed(fa.rt_cur0, fa.rt_cur1, p, r);
-    if (out_here) write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);
+    if (out_here) write_out(fa, p, shade_corrected(P, r), true);
 }
 
 // Spatial reuse, step 1 of 3 (corrected mode with shadow rays): replays the
@@ -808,6 +915,33 @@ __global__ void __launch_bounds__(kBlock) k_trace_shadow(FrameArgs fa) {
         &fa.counters[kCntError], nullptr, &fa.counters[kCntNonFinite]);
 }
 
+// Next-event rays of the cache's training paths (one bounce): any-hit
+// traversal; an unoccluded ray adds its contribution to its record's target.
+__global__ void __launch_bounds__(kBlock) k_trace_nee(FrameArgs fa) {
+    const uint32_t count = *(volatile const uint32_t*)&fa.counters[kCntCacheNee];
+    trace_persistent<true>(
+        fa.sc, count < fa.cache_t_cap ? count : fa.cache_t_cap, &fa.counters[kCntFetchNee],
+        [&](uint32_t i) {
+            const float4 a = fa.cache_nee[(size_t)i * 3u], b = fa.cache_nee[(size_t)i * 3u + 1u];
+            RayIn r;
+            r.o = xyz(a);
+            r.d = xyz(b);
+            r.tmin = 0.0f;
+            r.tmax = b.w;
+            return r;
+        },
+        [&](uint32_t i, const HitRec& h) {
+            if (h.prim < 0) {
+                const uint32_t rec = __float_as_uint(fa.cache_nee[(size_t)i * 3u].w);
+                const float4 c = fa.cache_nee[(size_t)i * 3u + 2u];
+                float4* tgt = reinterpret_cast<float4*>(fa.cache_t + (size_t)rec * 3u + 2u);
+                const float4 v = *tgt;
+                *tgt = make_float4(v.x + c.x, v.y + c.y, v.z + c.z, v.w);
+            }
+        },
+        &fa.counters[kCntError], nullptr, &fa.counters[kCntNonFinite]);
+}
+
 // Spatial reuse, step 3 of 3: the merge of ReSTIRGISpatialReuse.rgen.hlsl:91-176
 // with the visibility of step 2, M cap, W, shading and tone mapping.
 __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
@@ -859,7 +993,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
     float phf = target_corrected(P, r.xs, r.L);
     r.W = (phf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * phf) : 0.0f;
     store_packed(fa.rs0, fa.rs1, p, r);
-    write_out(fa, p, shade_corrected(fa, u, r, x_view, n_view, mat), true);
+    write_out(fa, p, shade_corrected(P, r), true);
 }
 
 // ---------------------------------------------------------------------------
@@ -1028,14 +1162,18 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
     FrameArgs a = fa;
     if (fa.compat) k_raygen<true><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
     else k_raygen<false><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
+    const bool cache = !fa.compat && fa.cache_on;
     for (uint32_t b = 0; b < nb; b++) {
         // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
         k_trace_paths<<<fa.grid_trace, kBlock, 0, st>>>(fa.sc, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                         fa.counters + kCntFetchPath + b, fa.counters + kCntError,
                                                         fa.counters + kCntNonFinite);
+        const bool nee = cache && b >= 1u && b + 1u < nb;
+        if (nee) cudaMemsetAsync(fa.counters + kCntCacheNee, 0, 2 * sizeof(uint32_t), st);   // count + fetch
         if (fa.compat) k_shade<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
         else k_shade<false><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
+        if (nee) k_trace_nee<<<fa.grid_trace, kBlock, 0, st>>>(a);
     }
 }
 

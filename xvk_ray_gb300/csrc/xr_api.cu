@@ -251,6 +251,8 @@ bad:
     return s;
 }
 
+static void free_lights(Context* c);
+
 void xr_destroy(XrContext* c) {
     if (!c) return;
     DeviceGuard g(c->device);
@@ -259,11 +261,69 @@ void xr_destroy(XrContext* c) {
     cache_free(c);
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
     cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo); cudaFree(c->d_work);
+    free_lights(c);
     if (c->h_ubo) cudaFreeHost(c->h_ubo);
     for (int i = 0; i < 8; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+static void free_lights(Context* c) {
+    cudaFree(c->d_light_prim); cudaFree(c->d_light_cdf); cudaFree(c->d_light_pmf); cudaFree(c->d_prim_light_pdf);
+    c->d_light_prim = nullptr; c->d_light_cdf = nullptr; c->d_light_pmf = nullptr; c->d_prim_light_pdf = nullptr;
+    c->n_lights = 0;
+}
+
+// Light-sampling tables of the emissive (DiffuseLight) triangles: power =
+// area * luminance(4 * base colour) (the emission of shade_step), pmf = power /
+// total, inclusive CDF in primitive order with the last entry 1, and per
+// primitive pmf / area (the area-measure density of picking a point on it).
+static xr_status upload_lights(Context* c, const std::vector<uint4>& tri, const std::vector<float4>& pos,
+                        const XrMaterial* m, uint32_t nm) {
+    std::vector<uint32_t> prim;
+    std::vector<float> area, power;
+    for (uint32_t i = 0; i < (uint32_t)tri.size(); i++) {
+        const uint32_t mi = tri[i].w;
+        if (mi >= nm || m[mi].material_model != XR_MAT_DIFFUSE_LIGHT) continue;
+        const float4 p0 = pos[tri[i].x], p1 = pos[tri[i].y], p2 = pos[tri[i].z];
+        const float e0x = p2.x - p0.x, e0y = p2.y - p0.y, e0z = p2.z - p0.z;
+        const float e1x = p1.x - p0.x, e1y = p1.y - p0.y, e1z = p1.z - p0.z;
+        const float cx = e0y * e1z - e0z * e1y, cy = e0z * e1x - e0x * e1z, cz = e0x * e1y - e0y * e1x;
+        const float a = 0.5f * sqrtf(cx * cx + cy * cy + cz * cz);
+        const float lr = m[mi].base_color[0] * 4.0f, lg = m[mi].base_color[1] * 4.0f, lb = m[mi].base_color[2] * 4.0f;
+        const float lum = 0.2126f * lr + 0.7152f * lg + 0.0722f * lb;
+        const float pw = a * lum;
+        if (!(pw > 0.0f) || !std::isfinite(pw)) continue;
+        prim.push_back(i);
+        area.push_back(a);
+        power.push_back(pw);
+    }
+    const uint32_t n = (uint32_t)prim.size();
+    c->n_lights = n;
+    if (n == 0) return XR_OK;
+    float total = 0.0f;
+    for (float pw : power) total = total + pw;
+    std::vector<float> pmf(n), cdf(n), prim_pdf(tri.size(), 0.0f);
+    float run = 0.0f;
+    for (uint32_t k = 0; k < n; k++) {
+        pmf[k] = power[k] / total;
+        run = run + pmf[k];
+        cdf[k] = run;
+        prim_pdf[prim[k]] = pmf[k] / area[k];
+    }
+    cdf[n - 1] = 1.0f;
+    xr_status s;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_light_prim, (size_t)n * 4), "light tables")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_light_cdf, (size_t)n * 4), "light tables")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_light_pmf, (size_t)n * 4), "light tables")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_prim_light_pdf, tri.size() * 4), "light tables")))
+        return s;
+    cudaMemcpy(c->d_light_prim, prim.data(), (size_t)n * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_light_cdf, cdf.data(), (size_t)n * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_light_pmf, pmf.data(), (size_t)n * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_prim_light_pdf, prim_pdf.data(), tri.size() * 4, cudaMemcpyHostToDevice);
+    return XR_OK;
 }
 
 xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const uint32_t* idx, uint32_t ni,
@@ -307,6 +367,7 @@ xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const ui
     cudaStreamSynchronize(c->stream);
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
     c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr;
+    free_lights(c);
     c->scene_ready = false; c->bvh_ready = false;
     xr_status s;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_tri_idx, std::max<size_t>(ntri, 1) * 16), "scene alloc")) ||
@@ -318,6 +379,7 @@ xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const ui
     if (nv) { cudaMemcpy(c->d_vpos, pos.data(), (size_t)nv * 16, cudaMemcpyHostToDevice);
               cudaMemcpy(c->d_vnrm, nrm.data(), (size_t)nv * 16, cudaMemcpyHostToDevice); }
     if (nm) cudaMemcpy(c->d_mats, m, (size_t)nm * sizeof(XrMaterial), cudaMemcpyHostToDevice);
+    if ((s = upload_lights(c, tri, pos, m, nm))) return s;
     if ((s = cuda_check(c, cudaGetLastError(), "scene upload"))) return s;
     c->nv = nv; c->ntri = ntri; c->nm = nm;
     c->scene_has_non_lambert = non_lambert;
@@ -336,6 +398,8 @@ xr_status xr_build_bvh(XrContext* c) {
     sc.tri = c->d_tris; sc.nodes = c->d_nodes; sc.n_nodes = c->n_nodes;
     sc.tri_idx = c->d_tri_idx; sc.vpos = c->d_vpos; sc.vnrm = c->d_vnrm;
     sc.mats = c->d_mats; sc.n_mats = c->nm; sc.ntri = c->ntri;
+    sc.light_prim = c->d_light_prim; sc.light_cdf = c->d_light_cdf; sc.light_pmf = c->d_light_pmf;
+    sc.prim_light_pdf = c->d_prim_light_pdf; sc.n_lights = c->n_lights;
     return XR_OK;
 }
 

@@ -48,6 +48,8 @@ constexpr uint32_t kCntFetchQuery = 97;    // ray-fetch counter of xr_trace_rays
 constexpr uint32_t kCntNonFinite = 98;     // rays ended early for a non-finite origin or direction
 constexpr uint32_t kCntCacheQuery = 99;    // radiance-cache query records of the frame
 constexpr uint32_t kCntCacheTrain = 100;   // radiance-cache training records of the frame
+constexpr uint32_t kCntCacheNee = 101;     // next-event rays of the current bounce's training paths
+constexpr uint32_t kCntFetchNee = 102;     // ray-fetch counter of the next-event trace
 constexpr uint32_t kCntError = 127;        // sticky XR_DEVFLAG_* bits
 constexpr uint32_t kCounterWords = 128;
 constexpr uint32_t kMaxBounces = 31;
@@ -79,6 +81,12 @@ struct DeviceScene {
     const XrMaterial* mats;
     uint32_t n_mats;
     uint32_t ntri;
+    // emissive triangles (next-event estimation of the cache's training paths)
+    const uint32_t* light_prim;      // primitive of light k
+    const float* light_cdf;          // inclusive CDF of the power pmf (last entry 1)
+    const float* light_pmf;          // probability of light k (power / total power)
+    const float* prim_light_pdf;     // per primitive: pmf / area (0: not a sampled light)
+    uint32_t n_lights;
 };
 
 struct FrameArgs {
@@ -117,6 +125,7 @@ struct FrameArgs {
     uint32_t cache_t_cap;
     uint32_t cache_sel_n;     // training pixels: (pixel * 2^31-1 + cache_sel_off) mod N < cache_sel_n
     uint32_t cache_sel_off;
+    float4* cache_nee;        // next-event rays: 3 float4 each {o, record}, {d, tmax}, {contribution, 0}
 };
 
 // Learned radiance cache state (nrc.cu, cache_api.cu).
@@ -141,6 +150,7 @@ struct CacheState {
     float* loss = nullptr;           // mean loss of the last training launch
     uint4* queries = nullptr;        // query records (capacity query_cap)
     uint4* train = nullptr;          // training records (capacity train_cap)
+    float4* nee = nullptr;           // next-event rays of one bounce (capacity train_cap)
     uint32_t query_cap = 0, train_cap = 0;
     bool frame_used = false;         // the last frame ran with the cache
     bool frame_trained = false;
@@ -164,6 +174,13 @@ struct Context {
     bool scene_has_non_lambert = false;
 
     // BVH
+    // emissive triangles (light sampling tables)
+    uint32_t* d_light_prim = nullptr;
+    float* d_light_cdf = nullptr;
+    float* d_light_pmf = nullptr;
+    float* d_prim_light_pdf = nullptr;
+    uint32_t n_lights = 0;
+
     WideNode* d_nodes = nullptr;
     float4* d_tris = nullptr;
     uint32_t n_nodes = 0, n_tri_slots = 0, bvh_depth = 0;
