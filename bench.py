@@ -171,65 +171,78 @@ def relmse(img: "np.ndarray", ref: "np.ndarray") -> float:
 RELMSE_EVAL_FRAMES = (16, 24, 32, 40, 48)
 
 
-def measure_relmse(xr, scene, ubos, eval_frames, ref_spp: int, device: int, train_samples: int = 65536) -> dict:
-    """relMSE of plain ReSTIR GI, of ReSTIR GI with the learned radiance cache and
-    of the 1-spp path tracer along the camera path, each against the
-    FP64-accumulated reference (plain path tracer, `ref_spp` samples) of the
-    evaluation frame's camera, averaged over the evaluation frames.  Both ReSTIR
-    variants render every frame of the path in their own context; their frame
-    times (library CUDA events, median) give the equal-time comparison."""
+def _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, cache: bool, n_neighbours: int,
+                train_samples: int) -> dict:
+    """One variant along the camera path: relMSE at the evaluation frames (FP64
+    references computed once and shared) and its median frame time."""
     import numpy as np
     L = xr._lib
-    n = max(eval_frames)
-    refs, ref_s = {}, 0.0
-    out = {}
-    for variant in ("restir_gi", "restir_gi_mlp_cache"):
-        r = xr.Renderer(W, H, device=device)
-        r.set_params(xr.params_default(W, H, write_hdr=1, write_pt=1))
-        r.upload_scene(scene)
-        r.build_bvh()
-        cache = variant == "restir_gi_mlp_cache"
-        if cache:
-            cp = xr.cache_params_default()
-            cp.enabled = 1
-            cp.train_samples = train_samples
-            r.cache.set_params(cp)
-        rel, rel_pt, ms, infer, train = [], [], [], [], []
-        for f, u in enumerate(ubos[:n]):
-            r.render(u)
-            st = r.stats()
-            ms.append(st.ms_frame)
-            if cache:
-                cs = r.cache.stats()
-                infer.append(cs.ms_infer)
-                train.append(cs.ms_train)
-            if f + 1 in eval_frames:
-                hdr = r.read_output(L.XR_OUT_HDR)
-                if f + 1 not in refs:
-                    t0 = time.perf_counter()
-                    refs[f + 1] = r.render_reference(u, 1_000_000, ref_spp)
-                    ref_s += time.perf_counter() - t0
-                rel.append(relmse(hdr, refs[f + 1]))
-                if not cache:
-                    rel_pt.append(relmse(r.read_output(L.XR_OUT_PT), refs[f + 1]))
-        entry = {"relmse": float(np.mean(rel)), "per_frame": [round(v, 4) for v in rel],
-                 "ms_per_frame": round(statistics.median(ms[8:]), 4)}
+    r = xr.Renderer(W, H, device=device)
+    p = xr.params_default(W, H, write_hdr=1, write_pt=1)
+    if n_neighbours == 0:
+        p.spatial_on = 0
+    else:
+        p.n_neighbours = n_neighbours
+    r.set_params(p)
+    r.upload_scene(scene)
+    r.build_bvh()
+    if cache:
+        cp = xr.cache_params_default()
+        cp.enabled = 1
+        cp.train_samples = train_samples
+        r.cache.set_params(cp)
+    rel, rel_pt, ms, infer, train = [], [], [], [], []
+    for f, u in enumerate(ubos[:max(eval_frames)]):
+        r.render(u)
+        ms.append(r.stats().ms_frame)
         if cache:
             cs = r.cache.stats()
-            entry.update({"ms_infer": round(statistics.median(infer[8:]), 4),
-                          "ms_train": round(statistics.median(train[8:]), 4), "queries": cs.queries,
-                          "train_samples": cs.train_samples, "adam_steps": cs.steps, "loss": round(cs.loss, 4)})
-        else:
-            out["pt_1spp"] = float(np.mean(rel_pt))
-        out[variant] = entry
-        r.close()
-    plain, cached = out["restir_gi"], out["restir_gi_mlp_cache"]
-    return {"restir_gi": plain["relmse"], "restir_gi_mlp_cache": cached["relmse"], "pt_1spp": out["pt_1spp"],
-            "ratio_cache_over_plain": round(cached["relmse"] / plain["relmse"], 4),
-            "detail": {"restir_gi": plain, "restir_gi_mlp_cache": cached},
+            infer.append(cs.ms_infer)
+            train.append(cs.ms_train)
+        if f + 1 in eval_frames:
+            hdr = r.read_output(L.XR_OUT_HDR)
+            if f + 1 not in refs:
+                t0 = time.perf_counter()
+                refs[f + 1] = r.render_reference(u, 1_000_000, ref_spp)
+                refs["seconds"] = refs.get("seconds", 0.0) + time.perf_counter() - t0
+            rel.append(relmse(hdr, refs[f + 1]))
+            rel_pt.append(relmse(r.read_output(L.XR_OUT_PT), refs[f + 1]))
+    entry = {"relmse": float(np.mean(rel)), "per_frame": [round(v, 4) for v in rel],
+             "ms_per_frame": round(statistics.median(ms[8:]), 4), "n_neighbours": n_neighbours}
+    if cache:
+        cs = r.cache.stats()
+        entry.update({"ms_infer": round(statistics.median(infer[8:]), 4),
+                      "ms_train": round(statistics.median(train[8:]), 4), "queries": cs.queries,
+                      "train_samples": cs.train_samples, "adam_steps": cs.steps, "loss": round(cs.loss, 4)})
+    else:
+        entry["pt_1spp"] = float(np.mean(rel_pt))
+    r.close()
+    return entry
+
+
+def measure_relmse(xr, scene, ubos, eval_frames, ref_spp: int, device: int, train_samples: int = 65536) -> dict:
+    """relMSE against the FP64-accumulated reference (plain path tracer, `ref_spp`
+    samples, at each evaluation frame's camera), averaged over the evaluation
+    frames, for: plain ReSTIR GI (5 neighbours), ReSTIR GI + learned radiance
+    cache with the same reuse settings, and ReSTIR GI + cache at equal frame
+    time -- the most spatial neighbours (5 .. 0) whose median frame time does not
+    exceed plain ReSTIR GI's."""
+    refs = {}
+    plain = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, False, 5, train_samples)
+    same = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, 5, train_samples)
+    equal = same
+    for nb in (4, 3, 2, 1, 0):
+        if equal["ms_per_frame"] <= plain["ms_per_frame"]:
+            break
+        equal = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, nb, train_samples)
+    return {"restir_gi": plain["relmse"], "restir_gi_mlp_cache": same["relmse"], "pt_1spp": plain["pt_1spp"],
+            "ratio_cache_over_plain": round(same["relmse"] / plain["relmse"], 4),
+            "restir_gi_mlp_cache_equal_time": equal["relmse"],
+            "ratio_equal_time": round(equal["relmse"] / plain["relmse"], 4),
+            "detail": {"restir_gi": plain, "restir_gi_mlp_cache": same, "restir_gi_mlp_cache_equal_time": equal},
             "reference": f"FP64-accumulated plain path tracer, {ref_spp} spp, same path depth, "
                          f"at frames {list(eval_frames)} of the camera path",
-            "eps": RELMSE_EPS, "reference_seconds": round(ref_s, 2)}
+            "eps": RELMSE_EPS, "reference_seconds": round(refs.get("seconds", 0.0), 2)}
 
 
 def cpu_baseline(scene, ubos, seconds_budget: float = 20.0) -> dict:
@@ -349,7 +362,8 @@ def run_ours(args):
     # ---- e2e through the C ABI with host buffers ----
     pinned = xr.PinnedBuffer(W * H * 4)
     out = pinned.array
-    host_ubos = [L.XrUniformBufferObject.from_buffer_copy(u) for u in ubos[fi:fi + args.steps]]
+    # the same camera frames as the device-timed region
+    host_ubos = [L.XrUniformBufferObject.from_buffer_copy(u) for u in ubos[args.warmup:args.warmup + args.steps]]
     _barrier(dist, local)
     t0 = time.perf_counter()
     for u in host_ubos:

@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
     "-Xptxas", "-warn-spills",
     f"-I{ROOT / 'include'}", f"-I{CSRC}",
-]
+] + os.environ.get("XR_EXTRA_NVCC_FLAGS", "").split()   # e.g. -DXR_TRACE_MIN_BLOCKS=10 (tuning builds)
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 
 CU_SOURCES = ["bvh_build.cu", "trace.cu", "trace_noalloc.cu", "restir.cu", "nrc.cu", "cache_api.cu", "xr_api.cu"]
@@ -89,8 +89,8 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
 
 
 def build_oracle(force: bool = False) -> Path:
-    src = ORACLE_DIR / "oracle.cpp"
-    if force or _stale(ORACLE_LIB, [src, ORACLE_DIR / "xr_oracle.h"]):
+    deps = sorted(ORACLE_DIR.glob("*.cpp")) + sorted(ORACLE_DIR.glob("*.h")) + [ORACLE_DIR / "Makefile"]
+    if force or _stale(ORACLE_LIB, deps):
         _run(["make", "-s", "-C", str(ORACLE_DIR)] + (["-B"] if force else []))
     return ORACLE_LIB
 

@@ -25,6 +25,11 @@ namespace xr {
 namespace {
 
 constexpr int kBlock = 128;
+// Minimum resident CTAs per SM requested from the compiler for the traversal
+// kernels (a register budget: 8 -> 64 registers, 10 -> 48).
+#ifndef XR_TRACE_MIN_BLOCKS
+#define XR_TRACE_MIN_BLOCKS 8
+#endif
 
 struct HitPayload {
     float3 pos, normal, geo;
@@ -428,7 +433,7 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 
 // Closest hits of the paths of one bounce (TMin 1e-4, TMax 1e4,
 // ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
-__global__ void __launch_bounds__(kBlock) k_trace_paths(DeviceScene sc, const float4* __restrict__ q0,
+__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_paths(DeviceScene sc, const float4* __restrict__ q0,
                                                         const float4* __restrict__ q1, uint4* __restrict__ hits,
                                                         const uint32_t* count_ptr, uint32_t* next, uint32_t* err,
                                                         uint32_t* nonfinite) {
@@ -888,7 +893,7 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
 // Spatial reuse, step 2 of 3: any-hit traversal of the queued shadow rays
 // (ReSTIRGISpatialReuse.rgen.hlsl:44-62 with the centre pixel's visible point as
 // origin); an occluded ray sets its slot's bit in the pixel's occlusion word.
-__global__ void __launch_bounds__(kBlock) k_trace_shadow(FrameArgs fa) {
+__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_shadow(FrameArgs fa) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[32];
     trace_persistent<true>(
         fa.sc, count, &fa.counters[kCntFetchShadow],
@@ -917,7 +922,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_shadow(FrameArgs fa) {
 
 // Next-event rays of the cache's training paths (one bounce): any-hit
 // traversal; an unoccluded ray adds its contribution to its record's target.
-__global__ void __launch_bounds__(kBlock) k_trace_nee(FrameArgs fa) {
+__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_nee(FrameArgs fa) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[kCntCacheNee];
     trace_persistent<true>(
         fa.sc, count < fa.cache_t_cap ? count : fa.cache_t_cap, &fa.counters[kCntFetchNee],
