@@ -99,3 +99,15 @@ def test_camera_ubo_matches_glm_conventions():
     assert np.allclose(view @ [0.5, 1.0, 3.0, 1.0], [0, 0, 0, 1], atol=1e-6)   # camera at the origin
     u2 = xr.camera_ubo(cam, 1920, 1080, u, 1, 4)
     assert list(u2.view_prev) == list(u.view) and list(u.view_prev) == list(u.view)   # first frame: prev = current
+
+
+def test_png_roundtrip(tmp_path):
+    """Headless output (the reference's present path replaced by a PNG file)."""
+    from xvk_ray_gb300.render import read_png_rgba, write_png
+    rng = np.random.default_rng(3)
+    for w, h in ((1, 1), (7, 3), (64, 48)):
+        px = rng.integers(0, 256, (w * h, 4)).astype(np.uint8)
+        p = tmp_path / f"i{w}x{h}.png"
+        write_png(str(p), px, w, h)
+        back, bw, bh = read_png_rgba(str(p))
+        assert (bw, bh) == (w, h) and np.array_equal(back, px)
