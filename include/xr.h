@@ -262,6 +262,44 @@ xr_status xr_scene_procedural(const XrProceduralDesc* desc, XrSceneData* out);
 xr_status xr_alloc_host(size_t bytes, void** ptr);
 void xr_free_host(void* ptr);
 
+/* ---- several scenes and views in one context ----
+   No single counterpart in the reference, which renders one view of one scene per
+   Render call (ApplicationReSTIRGI.cpp:150-275): here one frame renders every view
+   of the context in the same kernel launches (one path queue, one traversal
+   launch per bounce, one launch per reservoir pass for all views).  Scenes are
+   concatenated on the device -- each keeps its own BVH, reached through its root
+   node -- so rays of a view only ever see their own scene.  Results of a view are
+   bit-identical to rendering it alone.  All views of a frame share the frame
+   index parity (the reservoir ping-pong); the learned cache needs a single scene. */
+typedef struct XrView {
+    uint32_t scene;              /* index into the xr_upload_scenes list */
+    uint32_t width, height;
+} XrView;
+
+/* Uploads n scenes and builds their BVHs (replaces xr_upload_scene + xr_build_bvh). */
+xr_status xr_upload_scenes(XrContext* ctx, const XrSceneData* scenes, uint32_t n);
+/* Views and the common parameters (params->width/height are ignored). */
+xr_status xr_set_views(XrContext* ctx, const XrView* views, uint32_t n, const XrParams* params);
+/* One frame of every view; ubos[v] is view v's camera, all with the same current_frame parity.
+   With graphs enabled the frame's launches are captured once per parity and replayed. */
+xr_status xr_render_views(XrContext* ctx, const XrUniformBufferObject* ubos);
+xr_status xr_read_view_output(XrContext* ctx, uint32_t view, uint32_t which, void* host, size_t bytes);
+xr_status xr_set_graphs(XrContext* ctx, int enabled);   /* CUDA-graph replay of frames (not with the cache) */
+
+/* Launch configuration chosen by xr_autotune: persistent CTAs per SM of the
+   traversal and shading kernels (0 = the occupancy maximum). */
+typedef struct XrTuning {
+    uint32_t trace_ctas_per_sm, shade_ctas_per_sm;
+    float ms_per_frame;          /* best measured configuration */
+    float ms_default;            /* the occupancy-maximum configuration */
+    uint32_t configs_tried;
+} XrTuning;
+/* Times `frames` frames of every candidate configuration (ubos: frames x views, in
+   frame order) and keeps the fastest for the context's later frames. */
+xr_status xr_autotune(XrContext* ctx, const XrUniformBufferObject* ubos, uint32_t frames, XrTuning* out);
+/* Applies a launch configuration (e.g. one xr_autotune chose earlier); 0 = occupancy maximum. */
+xr_status xr_set_tuning(XrContext* ctx, const XrTuning* tuning);
+
 /* ---- learned radiance cache ----
    No counterpart in the reference renderer (it has no learned component): the
    cache of Mueller et al., "Real-time Neural Radiance Caching for Path Tracing"

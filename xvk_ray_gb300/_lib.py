@@ -112,6 +112,15 @@ class XrCacheStats(C.Structure):
                 ("inv_extent", C.c_float)]
 
 
+class XrView(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class XrTuning(C.Structure):
+    _fields_ = [("trace_ctas_per_sm", C.c_uint32), ("shade_ctas_per_sm", C.c_uint32), ("ms_per_frame", C.c_float),
+                ("ms_default", C.c_float), ("configs_tried", C.c_uint32)]
+
+
 XR_CACHE_MLP, XR_CACHE_GRID, XR_CACHE_MLP_GRAD, XR_CACHE_GRID_GRAD = 0, 1, 2, 3
 XR_CACHE_MLP_M, XR_CACHE_MLP_V, XR_CACHE_GRID_M, XR_CACHE_GRID_V = 4, 5, 6, 7
 XR_CACHE_QUERIES, XR_CACHE_TRAIN_RECORDS = 8, 9
@@ -156,6 +165,13 @@ _SIGS = {
     "xr_event_elapsed": (_i32, [_P, _u32, _u32, C.POINTER(C.c_float)]),
     "xr_alloc_host": (_i32, [C.c_size_t, C.POINTER(_P)]),
     "xr_free_host": (None, [_P]),
+    "xr_upload_scenes": (_i32, [_P, _P, _u32]),
+    "xr_set_views": (_i32, [_P, _P, _u32, C.POINTER(XrParams)]),
+    "xr_render_views": (_i32, [_P, _P]),
+    "xr_read_view_output": (_i32, [_P, _u32, _u32, _P, C.c_size_t]),
+    "xr_set_graphs": (_i32, [_P, C.c_int]),
+    "xr_autotune": (_i32, [_P, _P, _u32, C.POINTER(XrTuning)]),
+    "xr_set_tuning": (_i32, [_P, C.POINTER(XrTuning)]),
     "xr_cache_params_default": (None, [C.POINTER(XrCacheParams)]),
     "xr_cache_set_params": (_i32, [_P, C.POINTER(XrCacheParams)]),
     "xr_cache_get_params": (_i32, [_P, C.POINTER(XrCacheParams)]),

@@ -148,6 +148,55 @@ class Renderer:
         self.width, self.height = p.width, p.height
 
     # -- frames --
+    # -- several scenes / views in one context --
+    def upload_scenes(self, scenes: "list[Scene]") -> None:
+        """Uploads the scenes and builds their BVHs (views then pick them by index)."""
+        keep = []
+        arr = (L.XrSceneData * len(scenes))()
+        for k, sc in enumerate(scenes):
+            v = np.ascontiguousarray(sc.vertices, np.float32)
+            i = np.ascontiguousarray(sc.global_indices(), np.uint32)
+            m = np.ascontiguousarray(sc.materials, np.float32)
+            keep += [v, i, m]
+            arr[k].vertices, arr[k].vertex_count = _ptr(v), v.shape[0]
+            arr[k].indices, arr[k].index_count = _ptr(i), i.size
+            arr[k].materials, arr[k].material_count = _ptr(m), m.shape[0]
+        self._c(self._lib.xr_upload_scenes(self.ctx, C.cast(arr, C.c_void_p), len(scenes)))
+
+    def set_views(self, views: "list[tuple[int, int, int]]", params: L.XrParams) -> None:
+        """views: (scene index, width, height) per view; params are shared (their extent is ignored)."""
+        arr = (L.XrView * len(views))(*[L.XrView(*v) for v in views])
+        self.views = list(views)
+        self._c(self._lib.xr_set_views(self.ctx, C.cast(arr, C.c_void_p), len(views), C.byref(params)))
+
+    def render_views(self, ubos: "list[L.XrUniformBufferObject]") -> None:
+        arr = (L.XrUniformBufferObject * len(ubos))(*ubos)
+        self._c(self._lib.xr_render_views(self.ctx, C.cast(arr, C.c_void_p)))
+
+    def read_view_output(self, view: int, which: int = L.XR_OUT_LDR8) -> np.ndarray:
+        _, w, h = self.views[view]
+        if which == L.XR_OUT_LDR8:
+            out = np.empty((w * h, 4), np.uint8)
+        else:
+            out = np.empty((w * h, 4), np.float32)
+        self._c(self._lib.xr_read_view_output(self.ctx, view, which, _ptr(out), out.nbytes))
+        return out
+
+    def set_graphs(self, enabled: bool) -> None:
+        self._c(self._lib.xr_set_graphs(self.ctx, 1 if enabled else 0))
+
+    def autotune(self, frames: "list[list[L.XrUniformBufferObject]]") -> L.XrTuning:
+        """frames: per frame, the UBO of every view (or a single UBO for a one-view context)."""
+        flat = [u for f in frames for u in (f if isinstance(f, (list, tuple)) else [f])]
+        arr = (L.XrUniformBufferObject * len(flat))(*flat)
+        t = L.XrTuning()
+        self._c(self._lib.xr_autotune(self.ctx, C.cast(arr, C.c_void_p), len(frames), C.byref(t)))
+        return t
+
+    def set_tuning(self, trace_ctas_per_sm: int, shade_ctas_per_sm: int) -> None:
+        t = L.XrTuning(trace_ctas_per_sm, shade_ctas_per_sm, 0.0, 0.0, 0)
+        self._c(self._lib.xr_set_tuning(self.ctx, C.byref(t)))
+
     def render(self, ubo: L.XrUniformBufferObject) -> None:
         self._c(self._lib.xr_render_frame(self.ctx, C.byref(ubo)))
 

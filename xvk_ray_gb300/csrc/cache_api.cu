@@ -242,6 +242,7 @@ xr_status xr_cache_set_params(XrContext* c, const XrCacheParams* p) {
     xr_status s = validate(c, p);
     if (s) return s;
     DeviceGuard g(c->device);
+    invalidate_graphs(c);
     c->cache.params = *p;
     if (p->enabled) return cache_alloc(c);
     return XR_OK;

@@ -58,6 +58,38 @@ __device__ __forceinline__ HitPayload closest_hit(const DeviceScene& sc, const H
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// ---- views: a pixel's view, its view-local coordinates and extent ----
+__device__ __forceinline__ uint32_t view_index(const FrameArgs& fa, uint32_t p) {
+    if (fa.n_views <= 1u) return 0u;
+    uint32_t lo = 0, hi = fa.n_views - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (fa.views[mid].pix_off <= p) lo = mid;
+        else hi = mid - 1u;
+    }
+    return lo;
+}
+struct PixView {
+    uint32_t v, x, y, W, H, base;
+};
+__device__ __forceinline__ PixView pix_view(const FrameArgs& fa, uint32_t p) {
+    PixView c;
+    if (fa.n_views <= 1u) {
+        c.v = 0u; c.base = 0u; c.W = fa.W; c.H = fa.H;
+    } else {
+        c.v = view_index(fa, p);
+        const ViewInfo vi = fa.views[c.v];
+        c.base = vi.pix_off; c.W = vi.W; c.H = vi.H;
+    }
+    const uint32_t l = p - c.base;
+    c.x = l % c.W;
+    c.y = l / c.W;
+    return c;
+}
+__device__ __forceinline__ uint32_t root_of_pixel(const FrameArgs& fa, uint32_t p) {
+    return fa.multi_root ? fa.views[view_index(fa, p)].root : 0u;
+}
+
 __device__ __forceinline__ void flag_error(const FrameArgs& fa, uint32_t bits) { atomicOr(&fa.counters[kCntError], bits); }
 
 // ---------------------------------------------------------------------------
@@ -405,19 +437,37 @@ __device__ __forceinline__ bool cache_emit(const FrameArgs& fa, const CacheEmit&
 // Camera rays (ReSTIRGIInitialSample.rgen.hlsl:41-52) for a 16 x 8 pixel tile per
 // block, appended to the queue of bounce 0 in tile order.
 template <bool COMPAT>
-__global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t nb) {
-    const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
-    const uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 4);
-    const bool inside = x < fa.W && y < fa.H;
+__global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniformBufferObject* __restrict__ ubos, uint32_t nb) {
+    // tile -> view (tiles of every view in one 1-D grid, view by view)
+    uint32_t v = 0;
+    if (fa.n_views > 1u) {
+        uint32_t lo = 0, hi = fa.n_views - 1u;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1u) >> 1;
+            if (fa.views[mid].tile_off <= blockIdx.x) lo = mid;
+            else hi = mid - 1u;
+        }
+        v = lo;
+    }
+    uint32_t VW = fa.W, VH = fa.H, base = 0u, lt = blockIdx.x;
+    if (fa.n_views > 1u) {
+        const ViewInfo vi = fa.views[v];
+        VW = vi.W; VH = vi.H; base = vi.pix_off; lt = blockIdx.x - vi.tile_off;
+    }
+    const XrUniformBufferObject* __restrict__ u = ubos + v;
+    const uint32_t tiles_x = (VW + 15u) / 16u;
+    const uint32_t x = (lt % tiles_x) * 16u + (threadIdx.x & 15u);
+    const uint32_t y = (lt / tiles_x) * 8u + (threadIdx.x >> 4);
+    const bool inside = x < VW && y < VH;
     PathState s;
     bool alive = false;
     if (inside) {
-        s.pixel = y * fa.W + x;
-        s.rng = pass_rng(COMPAT, x, y, fa.W, u->current_frame, kPassInitial, fa.seed);
+        s.pixel = base + y * VW + x;
+        s.rng = pass_rng(COMPAT, x, y, VW, u->current_frame, kPassInitial, fa.seed);
         float ox = random_float(s.rng);
         float oy = random_float(s.rng);
         float px = (float)x + ox, py = (float)y + oy;
-        float uvx = (px / (float)fa.W) * 2.0f - 1.0f, uvy = (py / (float)fa.H) * 2.0f - 1.0f;
+        float uvx = (px / (float)VW) * 2.0f - 1.0f, uvy = (py / (float)VH) * 2.0f - 1.0f;
         float4 origin = mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f));
         float4 target = mat_mul(u->projection_inverse, make_float4(uvx, uvy, 1.0f, 1.0f));
         float3 tn = normalize(xyz(target));
@@ -433,17 +483,25 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 
 // Closest hits of the paths of one bounce (TMin 1e-4, TMax 1e4,
 // ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
-__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_paths(DeviceScene sc, const float4* __restrict__ q0,
+// With several scenes each ray starts at its view's root; a path whose pixel slot
+// holds a cache training record (pixel_is_record) finds its pixel in the record.
+__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_paths(FrameArgs fa, const float4* __restrict__ q0,
                                                         const float4* __restrict__ q1, uint4* __restrict__ hits,
                                                         const uint32_t* count_ptr, uint32_t* next, uint32_t* err,
-                                                        uint32_t* nonfinite) {
+                                                        uint32_t* nonfinite, uint32_t pixel_is_record) {
     const uint32_t count = *(volatile const uint32_t*)count_ptr;
     trace_persistent<false>(
-        sc, count, next,
+        fa.sc, count, next,
         [&](uint32_t i) {
             float4 a = q0[i], b = q1[i];
             RayIn r;
             r.o = xyz(a); r.d = xyz(b); r.tmin = 0.0001f; r.tmax = 10000.0f;
+            r.root = 0u;
+            if (fa.multi_root) {
+                uint32_t p = __float_as_uint(a.w);
+                if (pixel_is_record) p = fa.cache_t[(size_t)p * 3u].w;
+                r.root = root_of_pixel(fa, p);
+            }
             return r;
         },
         [&](uint32_t i, const HitRec& h) {
@@ -475,7 +533,13 @@ __global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformB
             s.thr = xyz(c); s.pq = c.w;
             HitRec h;
             h.prim = (int32_t)hr.x; h.t = __uint_as_float(hr.y); h.b1 = __uint_as_float(hr.z); h.b2 = __uint_as_float(hr.w);
-            alive = shade_step<COMPAT>(fa, u, bounce, nb, s, h, ce);
+            const XrUniformBufferObject* __restrict__ uv = u;
+            if (fa.n_views > 1u) {
+                uint32_t p = s.pixel;
+                if (!COMPAT && fa.cache_on && bounce >= 2u) p = fa.cache_t[(size_t)p * 3u].w;
+                uv = u + view_index(fa, p);
+            }
+            alive = shade_step<COMPAT>(fa, uv, bounce, nb, s, h, ce);
         }
         if (!COMPAT && fa.cache_on && bounce == 1u) alive = cache_emit(fa, ce, alive, s);
         if (!COMPAT && fa.cache_on && bounce >= 2u) push_nee(fa, ce.nee.valid, ce.nee, s.pixel);
@@ -567,8 +631,10 @@ __device__ __forceinline__ float3 mat_albedo_over_pi(const FrameArgs& fa, uint32
 __global__ void __launch_bounds__(256) k_temporal_compat(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
-    const uint32_t x = p % fa.W, y = p / fa.W, N = fa.N;
-    uint32_t rng = pass_rng(true, x, y, fa.W, u->current_frame, kPassTemporal, fa.seed);
+    const PixView pv = pix_view(fa, p);
+    u += pv.v;
+    const uint32_t x = pv.x, y = pv.y, N = fa.N;
+    uint32_t rng = pass_rng(true, x, y, pv.W, u->current_frame, kPassTemporal, fa.seed);
     const uint32_t pp = u->current_frame % 2u;
     const uint32_t cur = pp * N, prev = (1u - pp) * N;
     float4 xv = fa.s_xv[p], nv = fa.s_nv[p], xs = fa.s_xs[p], ns = fa.s_ns[p], Lv = fa.s_L[p];
@@ -586,12 +652,12 @@ __global__ void __launch_bounds__(256) k_temporal_compat(FrameArgs fa, const XrU
     bool found = false;
     Res r_prev; res_init(r_prev);
     {
-        float2 cuv = make_float2(((float)x + 0.5f) / (float)fa.W, ((float)y + 0.5f) / (float)fa.H);
+        float2 cuv = make_float2(((float)x + 0.5f) / (float)pv.W, ((float)y + 0.5f) / (float)pv.H);
         float2 puv0 = world_to_screen_uv(xyz(xv), u->view_prev, u->projection_prev);
         float mvx = half_round(cuv.x - puv0.x), mvy = half_round(cuv.y - puv0.y);
-        float fx = (cuv.x - mvx) * (float)fa.W, fy = (cuv.y - mvy) * (float)fa.H;
-        if (fx > -1.0f && fx < (float)fa.W && fy > -1.0f && fy < (float)fa.H) {
-            uint32_t q = (uint32_t)(int)fy * fa.W + (uint32_t)(int)fx;
+        float fx = (cuv.x - mvx) * (float)pv.W, fy = (cuv.y - mvy) * (float)pv.H;
+        if (fx > -1.0f && fx < (float)pv.W && fy > -1.0f && fy < (float)pv.H) {
+            uint32_t q = pv.base + (uint32_t)(int)fy * pv.W + (uint32_t)(int)fx;
             // previous G-buffer aliases the current one: validity of this frame at q
             if (__float_as_uint(fa.s_xv[q].w) != kInvalid) {
                 load_wide(fa, fa.rw, prev + q, r_prev);
@@ -667,8 +733,10 @@ __device__ __forceinline__ float jacobian_of(float3 x_nb_view, float3 x_view, fl
 __global__ void __launch_bounds__(256) k_spatial_compat(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
-    const uint32_t x = p % fa.W, y = p / fa.W, N = fa.N;
-    uint32_t rng = pass_rng(true, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
+    const PixView pv = pix_view(fa, p);
+    u += pv.v;
+    const uint32_t x = pv.x, y = pv.y, N = fa.N;
+    uint32_t rng = pass_rng(true, x, y, pv.W, u->current_frame, kPassSpatial, fa.seed);
     const uint32_t pp = u->current_frame % 2u;
     const uint32_t read_off = pp * N, write_off = (1u - pp) * N;
     const bool reuse = u->reuse != 0u;
@@ -680,7 +748,7 @@ __global__ void __launch_bounds__(256) k_spatial_compat(FrameArgs fa, const XrUn
     Res r; res_init(r);
     res_merge(r, center, length(center.L), rng);
     for (int i = 0; i < 6; i++) {
-        uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, 5.0f, rng);
+        uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, 5.0f, rng);
         float4 nxv = fa.s_xv[nbi], nnv = fa.s_nv[nbi];
         if (length(xyz(nnv)) == 0.0f) continue;
         float3 dd = xyz(xv) - xyz(nxv);
@@ -771,7 +839,9 @@ __device__ __forceinline__ float3 shade_corrected(const PixelShading& P, const R
 __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
-    const uint32_t x = p % fa.W, y = p / fa.W;
+    const PixView pv = pix_view(fa, p);
+    u += pv.v;
+    const uint32_t x = pv.x, y = pv.y;
     float4 g = fa.gb_pos_cur[p];
     uint32_t mat = fa.gb_mat_cur[p];
     float4 a = fa.cand_a[p], b = fa.cand_b[p];
@@ -787,7 +857,7 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
         if (out_here) write_out(fa, p, valid ? f3(0, 0, 0) : xyz(b), true);
         return;
     }
-    uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassTemporal, fa.seed);
+    uint32_t rng = pass_rng(false, x, y, pv.W, u->current_frame, kPassTemporal, fa.seed);
     const float3 x_view = xyz(g);
     const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
     Res s_new;
@@ -798,9 +868,9 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     Res r_prev; res_init(r_prev);
     if (fa.temporal_on && P.reuse) {
         float2 puv = world_to_screen_uv(x_view, u->view_prev, u->projection_prev);
-        float fx = floorf(puv.x * (float)fa.W), fy = floorf(puv.y * (float)fa.H);
-        if (fx >= 0.0f && fx < (float)fa.W && fy >= 0.0f && fy < (float)fa.H) {
-            uint32_t q = (uint32_t)fy * fa.W + (uint32_t)fx;
+        float fx = floorf(puv.x * (float)pv.W), fy = floorf(puv.y * (float)pv.H);
+        if (fx >= 0.0f && fx < (float)pv.W && fy >= 0.0f && fy < (float)pv.H) {
+            uint32_t q = pv.base + (uint32_t)fy * pv.W + (uint32_t)fx;
             if (fa.gb_mat_prev[q] == mat) {
                 float4 pg = fa.gb_pos_prev[q];
                 float3 pn = oct_decode(__float_as_uint(pg.w), 16);
@@ -844,18 +914,20 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
     uint32_t nb_of[32];
     if (p < fa.N) {
         fa.occ[p] = 0u;
-        const uint32_t x = p % fa.W, y = p / fa.W;
+        const PixView pv = pix_view(fa, p);
+        const XrUniformBufferObject* __restrict__ uv = u + pv.v;
+        const uint32_t x = pv.x, y = pv.y;
         const float4 g = fa.gb_pos_cur[p];
         const uint32_t mat = fa.gb_mat_cur[p];
         const float4 b = fa.cand_b[p];
         if (mat != kInvalid && (__float_as_uint(b.w) >> 31) != 0u) {
-            uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
+            uint32_t rng = pass_rng(false, x, y, pv.W, uv->current_frame, kPassSpatial, fa.seed);
             const float3 x_view = xyz(g);
             const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
-            const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat);
+            const PixelShading P = pixel_shading(fa, uv, x_view, n_view, mat);
             (void)random_float(rng);   // the centre merge's draw
             for (uint32_t i = 0; i < (P.reuse ? fa.n_nb : 0u); i++) {
-                const uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, fa.radius, rng);
+                const uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng);
                 const uint32_t nmat = fa.gb_mat_cur[nbi];
                 if (nmat == kInvalid) continue;
                 const float4 ng = fa.gb_pos_cur[nbi];
@@ -905,6 +977,7 @@ __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_shadow(Fr
             const float3 to = xyz(fa.rt_cur0[e.y]);
             const float3 dir = to - from;
             RayIn r;
+            r.root = root_of_pixel(fa, e.x >> 5);
             r.o = from + n * 0.01f;
             r.d = normalize(dir);
             r.tmin = 0.0f;
@@ -929,6 +1002,7 @@ __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_nee(Frame
         [&](uint32_t i) {
             const float4 a = fa.cache_nee[(size_t)i * 3u], b = fa.cache_nee[(size_t)i * 3u + 1u];
             RayIn r;
+            r.root = fa.multi_root ? root_of_pixel(fa, fa.cache_t[(size_t)__float_as_uint(a.w) * 3u].w) : 0u;
             r.o = xyz(a);
             r.d = xyz(b);
             r.tmin = 0.0f;
@@ -952,7 +1026,9 @@ __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_nee(Frame
 __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
-    const uint32_t x = p % fa.W, y = p / fa.W;
+    const PixView pv = pix_view(fa, p);
+    u += pv.v;
+    const uint32_t x = pv.x, y = pv.y;
     float4 g = fa.gb_pos_cur[p];
     uint32_t mat = fa.gb_mat_cur[p];
     float4 b = fa.cand_b[p];
@@ -963,7 +1039,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
         write_out(fa, p, valid ? f3(0, 0, 0) : xyz(b), true);
         return;
     }
-    uint32_t rng = pass_rng(false, x, y, fa.W, u->current_frame, kPassSpatial, fa.seed);
+    uint32_t rng = pass_rng(false, x, y, pv.W, u->current_frame, kPassSpatial, fa.seed);
     const float3 x_view = xyz(g);
     const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
     const uint32_t occ = fa.visibility ? fa.occ[p] : 0u;
@@ -972,7 +1048,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
     Res r; res_init(r);
     res_merge(r, center, target_corrected(P, center.xs, center.L), rng);
     for (uint32_t i = 0; i < (P.reuse ? fa.n_nb : 0u); i++) {
-        uint32_t nbi = neighbor_index(x, y, fa.W, fa.H, fa.radius, rng);
+        uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng);
         uint32_t nmat = fa.gb_mat_cur[nbi];
         if (nmat == kInvalid) continue;
         float4 ng = fa.gb_pos_cur[nbi];
@@ -1163,7 +1239,7 @@ uint32_t trace_grid(int sm_count) {
 }
 
 void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
-    dim3 grid0((fa.W + 15u) / 16u, (fa.H + 7u) / 8u);
+    const uint32_t grid0 = fa.n_tiles;
     FrameArgs a = fa;
     if (fa.compat) k_raygen<true><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
     else k_raygen<false><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
@@ -1171,9 +1247,9 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
     for (uint32_t b = 0; b < nb; b++) {
         // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
-        k_trace_paths<<<fa.grid_trace, kBlock, 0, st>>>(fa.sc, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+        k_trace_paths<<<fa.grid_trace, kBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                         fa.counters + kCntFetchPath + b, fa.counters + kCntError,
-                                                        fa.counters + kCntNonFinite);
+                                                        fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u);
         const bool nee = cache && b >= 1u && b + 1u < nb;
         if (nee) cudaMemsetAsync(fa.counters + kCntCacheNee, 0, 2 * sizeof(uint32_t), st);   // count + fetch
         if (fa.compat) k_shade<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);

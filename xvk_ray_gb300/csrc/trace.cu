@@ -23,6 +23,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DeviceScene sc, const flo
         [&](uint32_t i) {
             float4 a = rays[2 * i], b = rays[2 * i + 1];
             RayIn r;
+            r.root = 0u;
             r.o = xyz(a); r.tmin = a.w; r.d = xyz(b); r.tmax = b.w;
             return r;
         },

@@ -27,6 +27,7 @@ constexpr float kMinDir = 1e-20f;                 // smallest direction componen
 struct RayIn {
     float3 o, d;
     float tmin, tmax;
+    uint32_t root;   // first node of the ray's scene (0 unless several scenes share the node array)
 };
 
 // Byte k of `word` placed in mantissa bits 8..15 of 1.0f by one byte permute:
@@ -118,8 +119,8 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     tg_mask = 0;
                     visits_left = sc.n_nodes;
                     // a virtual group whose only child is the root (node 0)
-                    ng_base = 0;
-                    ng_bits = sc.n_nodes ? (1u | ((1u << flip) << 8)) : 0u;
+                    ng_base = r.root;
+                    ng_bits = (r.root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;   // no root: a miss
                     // A non-finite origin or direction (or a zero direction) can hit
                     // nothing -- every triangle test fails -- but would make every box
                     // test pass through NaN slabs and walk the whole tree: end it as a miss.

@@ -39,6 +39,14 @@ xr_status cuda_check(Context* ctx, cudaError_t e, const char* what) {
     return fail(ctx, code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+void invalidate_graphs(Context* c) {
+    for (int i = 0; i < 2; i++) {
+        if (c->graph[i]) cudaGraphExecDestroy(c->graph[i]);
+        c->graph[i] = nullptr;
+        c->graph_bounces[i] = 0u;
+    }
+}
+
 uint32_t persistent_grid(int sm_count, bool compat);
 uint32_t trace_grid(int sm_count);
 
@@ -57,8 +65,29 @@ void free_pixels(Context* c) {
 // One allocation holds every per-pixel buffer of the selected layout.
 xr_status alloc_pixels(Context* c) {
     free_pixels(c);
+    invalidate_graphs(c);
     const XrParams& P = c->params;
-    const size_t N = (size_t)P.width * P.height;
+    // views: the xr_set_views list, else one view of scene 0 with the parameters' extent
+    std::vector<XrView> views = c->views;
+    if (views.empty()) views.push_back(XrView{0u, P.width, P.height});
+    std::vector<ViewInfo> vinfo(views.size());
+    size_t Ntot = 0;
+    uint32_t tiles = 0;
+    bool multi_root = false;
+    for (size_t v = 0; v < views.size(); v++) {
+        ViewInfo& vi = vinfo[v];
+        vi = ViewInfo{};
+        vi.pix_off = (uint32_t)Ntot;
+        vi.W = views[v].width;
+        vi.H = views[v].height;
+        vi.root = views[v].scene < c->scene_roots.size() ? c->scene_roots[views[v].scene] : 0u;
+        vi.tile_off = tiles;
+        if (vi.root != 0u) multi_root = true;
+        Ntot += (size_t)vi.W * vi.H;
+        tiles += ((vi.W + 15u) / 16u) * ((vi.H + 7u) / 8u);
+    }
+    if (Ntot >= (1ull << 31)) return fail(c, XR_ERR_INVALID_ARGUMENT, "views: more than 2^31 pixels in total");
+    const size_t N = Ntot;
     const bool compat = P.compat_reference != 0;
     struct Item { void** dst; size_t bytes; };
     std::vector<Item> items;
@@ -99,8 +128,29 @@ xr_status alloc_pixels(Context* c) {
     c->pix_bytes = total;
     if (!compat)
         for (int i = 0; i < 2; i++) cudaMemsetAsync(c->gb_mat[i], 0xFF, N * 4, c->stream);
-    c->W = P.width; c->H = P.height; c->N = (uint32_t)N;
+    c->W = views[0].width; c->H = views[0].height; c->N = (uint32_t)N;
     fa.W = c->W; fa.H = c->H; fa.N = c->N;
+    fa.n_views = (uint32_t)views.size();
+    fa.n_tiles = tiles;
+    fa.multi_root = multi_root ? 1u : 0u;
+    cudaFree(c->d_views);
+    c->d_views = nullptr;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_views, vinfo.size() * sizeof(ViewInfo)), "view table"))) return s;
+    cudaMemcpy(c->d_views, vinfo.data(), vinfo.size() * sizeof(ViewInfo), cudaMemcpyHostToDevice);
+    c->view_info = vinfo;
+    fa.views = c->d_views;
+    if (views.size() > c->ubo_cap) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->d_ubo);
+        cudaFreeHost(c->h_ubo);
+        c->d_ubo = nullptr;
+        c->h_ubo = nullptr;
+        c->ubo_cap = 0;
+        if ((s = cuda_check(c, cudaMalloc((void**)&c->d_ubo, views.size() * sizeof(XrUniformBufferObject)), "ubo")) ||
+            (s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, views.size() * sizeof(XrUniformBufferObject)), "ubo staging")))
+            return s;
+        c->ubo_cap = (uint32_t)views.size();
+    }
     fa.counters = c->d_counters;
     fa.ubo = c->d_ubo;
     for (int k = 0; k < 3; k++) { fa.q_out[k] = c->q[0][k]; fa.q_in[k] = c->q[1][k]; }
@@ -120,19 +170,42 @@ void set_frame_pointers(Context* c, uint32_t parity) {
         fa.rt_cur0 = c->rt0[parity]; fa.rt_cur1 = c->rt1[parity];
         fa.rt_prev0 = c->rt0[1 - parity]; fa.rt_prev1 = c->rt1[1 - parity];
     }
-    fa.grid_persistent = persistent_grid(c->sm_count, P.compat_reference != 0);
-    fa.grid_trace = trace_grid(c->sm_count);
+    fa.grid_persistent = c->tune_shade_ctas ? c->tune_shade_ctas * (uint32_t)c->sm_count
+                                            : persistent_grid(c->sm_count, P.compat_reference != 0);
+    fa.grid_trace = c->tune_trace_ctas ? c->tune_trace_ctas * (uint32_t)c->sm_count : trace_grid(c->sm_count);
+}
+
+// Host side of a frame's UBO upload: wait until the previous frame's transfer has
+// read the pinned staging copy, then overwrite it with the n views' UBOs.
+xr_status stage_ubos(Context* c, const XrUniformBufferObject* ubos, uint32_t n) {
+    xr_status s = cuda_check(c, cudaEventSynchronize(c->ev[5]), "ubo staging");
+    if (s) return s;
+    for (uint32_t i = 0; i < n; i++) c->h_ubo[i] = ubos[i];
+    return XR_OK;
+}
+// Records `e` on the context's stream; inside a stream capture it becomes an
+// event-record node of the graph (an external event), so the host can still
+// wait on it and time with it when the graph is replayed.
+cudaError_t record_event(Context* c, cudaEvent_t e) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t q = cudaStreamIsCapturing(c->stream, &cs);
+    if (q != cudaSuccess) return q;
+    if (cs == cudaStreamCaptureStatusActive) return cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal);
+    return cudaEventRecord(e, c->stream);
+}
+
+// Stream side: the transfer itself (also what a captured frame graph replays).
+xr_status enqueue_ubos(Context* c, uint32_t n) {
+    xr_status s = cuda_check(c, cudaMemcpyAsync(c->d_ubo, c->h_ubo, n * sizeof(XrUniformBufferObject),
+                                                cudaMemcpyHostToDevice, c->stream), "ubo upload");
+    if (s) return s;
+    return cuda_check(c, record_event(c, c->ev[5]), "ubo event");
 }
 
 xr_status upload_ubo(Context* c, const XrUniformBufferObject* ubo) {
-    // the pinned staging copy may still be read by the previous frame's transfer
-    xr_status s = cuda_check(c, cudaEventSynchronize(c->ev[5]), "ubo staging");
+    xr_status s = stage_ubos(c, ubo, 1u);
     if (s) return s;
-    *c->h_ubo = *ubo;
-    s = cuda_check(c, cudaMemcpyAsync(c->d_ubo, c->h_ubo, sizeof(XrUniformBufferObject), cudaMemcpyHostToDevice, c->stream),
-                   "ubo upload");
-    if (s) return s;
-    return cuda_check(c, cudaEventRecord(c->ev[5], c->stream), "ubo event");
+    return enqueue_ubos(c, 1u);
 }
 
 }  // namespace
@@ -171,6 +244,8 @@ xr_status validate_params(const Context* c, const XrParams* p) {
 }
 
 }  // namespace
+xr_status realloc_pixels(Context* c) { return alloc_pixels(c); }
+
 }  // namespace xr
 
 using namespace xr;
@@ -258,6 +333,8 @@ void xr_destroy(XrContext* c) {
     DeviceGuard g(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_pixels(c);
+    invalidate_graphs(c);
+    cudaFree(c->d_views);
     cache_free(c);
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
     cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo); cudaFree(c->d_work);
@@ -384,6 +461,12 @@ xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const ui
     c->nv = nv; c->ntri = ntri; c->nm = nm;
     c->scene_has_non_lambert = non_lambert;
     cache_scene_bounds(c, reinterpret_cast<const float*>(v), nv);
+    invalidate_graphs(c);
+    c->scene_roots.clear();   // a single scene, root node 0
+    if (c->views.size() > 1) {   // views of a former scene list: back to one view
+        c->views.clear();
+        if (c->pix_mem && (s = alloc_pixels(c))) return s;
+    }
     c->scene_ready = true;
     return XR_OK;
 }
@@ -392,6 +475,7 @@ xr_status xr_build_bvh(XrContext* c) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "build_bvh: null context");
     if (!c->scene_ready) return fail(c, XR_ERR_STATE, "build_bvh: upload a scene first");
     DeviceGuard g(c->device);
+    invalidate_graphs(c);
     xr_status s = build_bvh(c);
     if (s) return s;
     DeviceScene& sc = c->fa.sc;
@@ -412,8 +496,13 @@ xr_status xr_set_params(XrContext* c, const XrParams* p) {
     bool realloc = !c->pix_mem || o.width != p->width || o.height != p->height || o.compat_reference != p->compat_reference ||
                    o.write_pt != p->write_pt || o.write_hdr != p->write_hdr ||
                    (!p->compat_reference && o.n_neighbours != p->n_neighbours);
+    if (!c->views.empty()) {   // back to a single view of scene 0
+        c->views.clear();
+        realloc = true;
+    }
     c->params = *p;
     c->params_set = true;
+    invalidate_graphs(c);
     if (realloc) {
         cudaStreamSynchronize(c->stream);
         if ((s = alloc_pixels(c))) return s;
@@ -427,32 +516,191 @@ xr_status xr_get_params(XrContext* c, XrParams* p) {
     return XR_OK;
 }
 
-xr_status xr_render_frame(XrContext* c, const XrUniformBufferObject* ubo) {
-    if (!c || !ubo) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_frame: null argument");
-    if (!c->params_set) return fail(c, XR_ERR_STATE, "render_frame: set the parameters (extent) first");
-    if (!c->bvh_ready) return fail(c, XR_ERR_STATE, "render_frame: build the BVH first");
-    if (ubo->number_of_bounces > 31) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_frame: number_of_bounces must be <= 31");
-    if (c->params.compat_reference && c->scene_has_non_lambert)
-        return fail(c, XR_ERR_UNSUPPORTED, "render_frame: reference mode renders only Lambertian and DiffuseLight materials");
-    DeviceGuard g(c->device);
-    xr_status s = upload_ubo(c, ubo);
+static void* output_ptr(XrContext* c, uint32_t which, size_t* bytes);
+
+
+// Every stream operation of one frame once its UBOs are staged: the UBO transfer,
+// the per-frame counters, the three passes and the timing events.  This is the
+// sequence a frame graph captures.
+static xr_status enqueue_frame(Context* c, uint32_t n_ubo, uint32_t nb, bool reuse0) {
+    xr_status s = enqueue_ubos(c, n_ubo);
     if (s) return s;
-    set_frame_pointers(c, ubo->current_frame % 2u);
-    if ((s = cache_prepare_frame(c, ubo->current_frame))) return s;
     cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);   // keep the sticky error word
     const bool compat = c->params.compat_reference != 0;
-    cudaEventRecord(c->ev[0], c->stream);
-    launch_initial(c->fa, ubo->number_of_bounces, c->stream);
+    record_event(c, c->ev[0]);
+    launch_initial(c->fa, nb, c->stream);
     cache_after_paths(c);   // radiance-cache inference and training (when enabled)
-    cudaEventRecord(c->ev[1], c->stream);
-    bool temporal_writes_image = compat ? (ubo->reuse == 0u) : (c->params.spatial_on == 0u);
+    record_event(c, c->ev[1]);
+    bool temporal_writes_image = compat ? !reuse0 : (c->params.spatial_on == 0u);
     launch_temporal(c->fa, temporal_writes_image, c->stream);
-    cudaEventRecord(c->ev[2], c->stream);
+    record_event(c, c->ev[2]);
     if (compat || c->params.spatial_on) launch_spatial(c->fa, c->stream);
-    cudaEventRecord(c->ev[3], c->stream);
+    record_event(c, c->ev[3]);
+    return cuda_check(c, cudaGetLastError(), "render launch");
+}
+
+// One frame of the context's n views (n = 1 for xr_render_frame).
+static xr_status render_impl(Context* c, const XrUniformBufferObject* ubos, uint32_t n, const char* who) {
+    if (!c->params_set) return fail(c, XR_ERR_STATE, std::string(who) + ": set the parameters (extent) first");
+    if (!c->bvh_ready) return fail(c, XR_ERR_STATE, std::string(who) + ": build the BVH first");
+    const uint32_t nb = ubos[0].number_of_bounces;
+    if (nb > kMaxBounces) return fail(c, XR_ERR_INVALID_ARGUMENT, std::string(who) + ": number_of_bounces must be <= 31");
+    for (uint32_t i = 1; i < n; i++)
+        if (ubos[i].number_of_bounces != nb || ubos[i].current_frame % 2u != ubos[0].current_frame % 2u ||
+            ubos[i].reuse != ubos[0].reuse)
+            return fail(c, XR_ERR_INVALID_ARGUMENT,
+                        std::string(who) + ": all views of a frame share number_of_bounces, reuse and the frame parity");
+    if (c->params.compat_reference && c->scene_has_non_lambert)
+        return fail(c, XR_ERR_UNSUPPORTED, std::string(who) + ": reference mode renders only Lambertian and DiffuseLight materials");
+    DeviceGuard g(c->device);
+    xr_status s = stage_ubos(c, ubos, n);
+    if (s) return s;
+    const uint32_t parity = ubos[0].current_frame % 2u;
+    set_frame_pointers(c, parity);
+    if ((s = cache_prepare_frame(c, ubos[0].current_frame))) return s;
+    const bool reuse0 = ubos[0].reuse != 0u;
+    if (c->graphs_on && !c->fa.cache_on) {
+        if (!c->graph[parity] || c->graph_bounces[parity] != (nb | (reuse0 ? 0x100u : 0u))) {
+            if (c->graph[parity]) cudaGraphExecDestroy(c->graph[parity]);
+            c->graph[parity] = nullptr;
+            cudaGraph_t gr = nullptr;
+            if ((s = cuda_check(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "frame capture")))
+                return s;
+            const xr_status e = enqueue_frame(c, n, nb, reuse0);
+            const cudaError_t ce = cudaStreamEndCapture(c->stream, &gr);
+            if (e) { if (gr) cudaGraphDestroy(gr); return e; }
+            if ((s = cuda_check(c, ce, "frame capture end"))) return s;
+            s = cuda_check(c, cudaGraphInstantiate(&c->graph[parity], gr, 0), "frame graph instantiate");
+            cudaGraphDestroy(gr);
+            if (s) return s;
+            c->graph_bounces[parity] = nb | (reuse0 ? 0x100u : 0u);
+        }
+        if ((s = cuda_check(c, cudaGraphLaunch(c->graph[parity], c->stream), "frame graph launch"))) return s;
+    } else if ((s = enqueue_frame(c, n, nb, reuse0))) {
+        return s;
+    }
     c->frames++;
-    c->last_bounces = ubo->number_of_bounces;
-    return cuda_check(c, cudaGetLastError(), "render_frame launch");
+    c->last_bounces = nb;
+    return XR_OK;
+}
+
+xr_status xr_render_frame(XrContext* c, const XrUniformBufferObject* ubo) {
+    if (!c || !ubo) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_frame: null argument");
+    if (c->fa.n_views > 1u) return fail(c, XR_ERR_STATE, "render_frame: the context has several views (xr_render_views)");
+    return render_impl(c, ubo, 1u, "render_frame");
+}
+
+xr_status xr_render_views(XrContext* c, const XrUniformBufferObject* ubos) {
+    if (!c || !ubos) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_views: null argument");
+    return render_impl(c, ubos, c->fa.n_views, "render_views");
+}
+
+xr_status xr_set_views(XrContext* c, const XrView* views, uint32_t n, const XrParams* p) {
+    if (!c || !views || n == 0 || !p) return fail(c, XR_ERR_INVALID_ARGUMENT, "set_views: bad argument");
+    const uint32_t n_scenes = c->scene_roots.empty() ? 1u : (uint32_t)c->scene_roots.size();
+    for (uint32_t v = 0; v < n; v++) {
+        if (views[v].scene >= n_scenes) return fail(c, XR_ERR_INVALID_ARGUMENT, "set_views: scene index out of range");
+        if (views[v].width == 0 || views[v].height == 0 || views[v].width > 16384 || views[v].height > 16384)
+            return fail(c, XR_ERR_INVALID_ARGUMENT, "set_views: width/height must be in [1, 16384]");
+    }
+    XrParams q = *p;
+    q.width = views[0].width;
+    q.height = views[0].height;
+    xr_status s = validate_params(c, &q);
+    if (s) return s;
+    if (n > 1 && c->cache.params.enabled && n_scenes > 1)
+        return fail(c, XR_ERR_UNSUPPORTED, "set_views: the learned cache covers one scene");
+    DeviceGuard g(c->device);
+    cudaStreamSynchronize(c->stream);
+    c->views.assign(views, views + n);
+    c->params = q;
+    c->params_set = true;
+    return alloc_pixels(c);
+}
+
+xr_status xr_read_view_output(XrContext* c, uint32_t view, uint32_t which, void* host, size_t bytes) {
+    if (!c || !host) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_view_output: null argument");
+    if (view >= c->view_info.size()) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_view_output: view out of range");
+    size_t all;
+    char* src = (char*)output_ptr(c, which, &all);
+    if (!src) return fail(c, XR_ERR_STATE, "read_view_output: that image is not enabled (write_hdr / write_pt)");
+    const size_t bpp = all / c->N;
+    const ViewInfo& vi = c->view_info[view];
+    const size_t need = (size_t)vi.W * vi.H * bpp;
+    if (bytes < need) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_view_output: host buffer too small");
+    DeviceGuard g(c->device);
+    xr_status s = cuda_check(c, cudaMemcpyAsync(host, src + (size_t)vi.pix_off * bpp, need, cudaMemcpyDeviceToHost,
+                                                c->stream), "read_view_output copy");
+    if (s) return s;
+    return xr_sync(c);
+}
+
+xr_status xr_set_graphs(XrContext* c, int enabled) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "set_graphs: null context");
+    DeviceGuard g(c->device);
+    c->graphs_on = enabled != 0;
+    invalidate_graphs(c);
+    return XR_OK;
+}
+
+xr_status xr_set_tuning(XrContext* c, const XrTuning* t) {
+    if (!c || !t) return fail(c, XR_ERR_INVALID_ARGUMENT, "set_tuning: null argument");
+    if (t->trace_ctas_per_sm > 64 || t->shade_ctas_per_sm > 64)
+        return fail(c, XR_ERR_INVALID_ARGUMENT, "set_tuning: at most 64 CTAs per SM");
+    DeviceGuard g(c->device);
+    c->tune_trace_ctas = t->trace_ctas_per_sm;
+    c->tune_shade_ctas = t->shade_ctas_per_sm;
+    invalidate_graphs(c);
+    return XR_OK;
+}
+
+xr_status xr_autotune(XrContext* c, const XrUniformBufferObject* ubos, uint32_t frames, XrTuning* out) {
+    if (!c || !ubos || frames == 0) return fail(c, XR_ERR_INVALID_ARGUMENT, "autotune: bad argument");
+    DeviceGuard g(c->device);
+    const uint32_t n = c->fa.n_views;
+    int occ_t = 0, occ_s = 0;
+    {
+        // the occupancy maxima are what grid 0 (the default) resolves to
+        const uint32_t t0 = trace_grid(c->sm_count), s0 = persistent_grid(c->sm_count, c->params.compat_reference != 0);
+        occ_t = (int)(t0 / (uint32_t)c->sm_count);
+        occ_s = (int)(s0 / (uint32_t)c->sm_count);
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> cands;
+    for (int t : {0, occ_t * 3 / 4, occ_t / 2})
+        for (int sh : {0, occ_s / 2})
+            if ((t == 0 || t >= 1) && (sh == 0 || sh >= 1)) cands.push_back({(uint32_t)t, (uint32_t)sh});
+    float best = 1e30f, dflt = 0.0f;
+    std::pair<uint32_t, uint32_t> pick{0u, 0u};
+    xr_status s = XR_OK;
+    for (const auto& cand : cands) {
+        c->tune_trace_ctas = cand.first;
+        c->tune_shade_ctas = cand.second;
+        invalidate_graphs(c);
+        // one untimed frame (graph capture, caches), then the timed frames
+        if ((s = render_impl(c, ubos, n, "autotune"))) break;
+        cudaEventRecord(c->user_ev[6], c->stream);
+        for (uint32_t f = 0; f < frames && !s; f++) s = render_impl(c, ubos + (size_t)f * n, n, "autotune");
+        if (s) break;
+        cudaEventRecord(c->user_ev[7], c->stream);
+        if ((s = xr_sync(c))) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, c->user_ev[6], c->user_ev[7]);
+        ms /= (float)frames;
+        if (cand.first == 0 && cand.second == 0) dflt = ms;
+        if (ms < best) { best = ms; pick = cand; }
+    }
+    c->tune_trace_ctas = pick.first;
+    c->tune_shade_ctas = pick.second;
+    invalidate_graphs(c);
+    if (s) return s;
+    if (out) {
+        out->trace_ctas_per_sm = pick.first ? pick.first : (uint32_t)occ_t;
+        out->shade_ctas_per_sm = pick.second ? pick.second : (uint32_t)occ_s;
+        out->ms_per_frame = best;
+        out->ms_default = dflt;
+        out->configs_tried = (uint32_t)cands.size();
+    }
+    return XR_OK;
 }
 
 xr_status xr_render_reference(XrContext* c, const XrUniformBufferObject* ubo, uint32_t frame0, uint32_t spp,

@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <string>
+#include <vector>
 
 #include "../../include/xr.h"
 
@@ -89,10 +90,24 @@ struct DeviceScene {
     uint32_t n_lights;
 };
 
+// One view of a multi-view context: its pixels are [pix_off, pix_off + W H) of the
+// per-pixel buffers, its camera rays start at BVH node `root` (the first node of
+// its scene in the concatenated node array), its 16x8 raygen tiles follow tile_off.
+struct ViewInfo {
+    uint32_t pix_off;
+    uint32_t W, H;
+    uint32_t root;
+    uint32_t tile_off;
+    uint32_t pad[3];
+};
+
 struct FrameArgs {
     DeviceScene sc;
-    const XrUniformBufferObject* ubo;   // device copy of this frame's UBO
-    uint32_t W, H, N;
+    const XrUniformBufferObject* ubo;   // device copies of this frame's UBOs, one per view
+    uint32_t W, H, N;                   // single view: its extent; several: W = H = 0, N = all pixels
+    const ViewInfo* views;              // n_views entries (device)
+    uint32_t n_views, n_tiles;
+    uint32_t multi_root;                // views over more than one scene
     uint32_t compat, temporal_on, spatial_on, visibility, write_pt, seed;
     uint32_t m_cap_t, m_cap_s, n_nb;
     float radius;
@@ -211,7 +226,24 @@ struct Context {
     cudaEvent_t user_ev[8] = {};
     XrStats stats{};
     CacheState cache;
+
+    // views (xr_set_views; empty: one view of scene 0 with the parameters' extent)
+    std::vector<XrView> views;
+    std::vector<ViewInfo> view_info;      // host copy of the device view table
+    ViewInfo* d_views = nullptr;
+    uint32_t ubo_cap = 1;                 // UBOs d_ubo / h_ubo hold
+    std::vector<uint32_t> scene_roots;    // first node of each scene (kNoRoot: empty scene)
+    // CUDA graphs of one frame per parity of the frame index (xr_render_views)
+    bool graphs_on = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    uint32_t graph_bounces[2] = {0, 0};
+    // launch configuration (xr_autotune): persistent CTAs per SM, 0 = occupancy maximum
+    uint32_t tune_trace_ctas = 0, tune_shade_ctas = 0;
 };
+
+constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
+void invalidate_graphs(Context* c);
+xr_status realloc_pixels(Context* c);   // per-pixel buffers and view table for the current views / params
 
 xr_status fail(const Context* ctx, xr_status code, const std::string& msg);
 xr_status cuda_check(Context* ctx, cudaError_t e, const char* what);
