@@ -89,6 +89,7 @@ def test_gradients_match_oracle():
 def test_adam_step_bit_exact():
     r, oc = _pair(6)
     rng = np.random.default_rng(2)
+    p1 = p2 = np.float32(1.0)
     with r:
         for step in (1, 2):
             gw = rng.standard_normal(17408).astype(np.float32)
@@ -101,8 +102,9 @@ def test_adam_step_bit_exact():
             oc.param(ob.NRC_MLP_GRAD)[:] = gw
             oc.param(ob.NRC_GRID_GRAD)[:] = gg
             p = r.cache.params()
-            b1, b2 = float(np.float32(p.beta1)), float(np.float32(p.beta2))
-            bc1, bc2 = np.float32(1.0 - b1 ** step), np.float32(1.0 - b2 ** step)
+            # bias correction as the device keeps it: FP32 running powers of beta
+            p1, p2 = np.float32(p1 * np.float32(p.beta1)), np.float32(p2 * np.float32(p.beta2))
+            bc1, bc2 = np.float32(np.float32(1.0) - p1), np.float32(np.float32(1.0) - p2)
             oc.adam(p.learning_rate, p.beta1, p.beta2, p.epsilon, bc1, bc2)
             for which, ow in ((L.XR_CACHE_MLP, ob.NRC_MLP), (L.XR_CACHE_MLP_M, ob.NRC_MLP_M),
                               (L.XR_CACHE_MLP_V, ob.NRC_MLP_V), (L.XR_CACHE_GRID, ob.NRC_GRID),

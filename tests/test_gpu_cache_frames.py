@@ -105,3 +105,28 @@ def test_reference_mode_rejects_cache():
         r.cache.set_params(_cache_params(256))
         with pytest.raises(xr.XrError):
             r.render(camera_sequence(scene, W, H, 1, 4)[0])
+
+
+def test_cache_frames_replayed_from_graphs():
+    """Training and inference inside replayed frame graphs: one Adam step per frame
+    (bias correction advanced on the device), images as with direct launches up to
+    the float-order nondeterminism of the gradient atomics."""
+    scene = xr.Scene.procedural(seed=3, n_objects=256, n_lights=8, extent=8.0)
+    W, H = 96, 64
+    ubos = camera_sequence(scene, W, H, 6, 4)
+    out = []
+    for graphs in (False, True):
+        with xr.Renderer(W, H) as r:
+            r.set_params(xr.params_default(W, H, write_hdr=1))
+            r.upload_scene(scene)
+            r.build_bvh()
+            r.cache.set_params(_cache_params(1024))
+            r.cache.reset(2)
+            r.set_graphs(graphs)
+            for u in ubos:
+                r.render(u)
+            cs = r.cache.stats()
+            assert cs.steps == len(ubos) and np.isfinite(cs.loss) and cs.train_samples > 0
+            out.append(r.read_output(L.XR_OUT_HDR)[:, :3].astype(np.float64))
+    d = np.abs(out[0] - out[1]).mean() / max(out[0].mean(), 1e-9)
+    assert d < 0.05, d

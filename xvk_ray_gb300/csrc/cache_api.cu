@@ -74,6 +74,7 @@ xr_status cache_init(Context* c, uint32_t seed) {
     cs.step = 0;
     cs.grads_dirty = false;
     launch_cache_init(cs, seed, c->stream);
+    launch_cache_adam_reset(cs, c->stream);
     s = cuda_check(c, cudaGetLastError(), "cache init launch");
     if (s) return s;
     return cuda_check(c, cudaStreamSynchronize(c->stream), "cache init");
@@ -95,6 +96,7 @@ xr_status cache_alloc(Context* c) {
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.w_fwd, nrc::kImageBytes), "cache alloc"))) return s;
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.w_bwd, nrc::kImageBytes), "cache alloc"))) return s;
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.loss, sizeof(float)), "cache alloc"))) return s;
+    if ((s = cuda_check(c, cudaMalloc((void**)&cs.adam, 4 * sizeof(float)), "cache alloc"))) return s;
     cs.allocated = true;
     return cache_init(c, cs.params.seed);
 }
@@ -151,7 +153,7 @@ xr_status upload_samples(Context* c, const XrCacheSample* s, uint32_t n, uint32_
 void cache_free(Context* c) {
     CacheState& cs = c->cache;
     void* ptrs[] = {cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.grid, cs.grid_grad, cs.grid_m, cs.grid_v,
-                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.queries, cs.train, cs.nee};
+                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.adam, cs.queries, cs.train, cs.nee};
     for (void* p : ptrs) cudaFree(p);
     cs = CacheState{};
 }
@@ -200,7 +202,7 @@ xr_status cache_prepare_frame(Context* c, uint32_t frame) {
     fa.cache_nee = cs.nee;
     fa.cache_t_cap = tcap;
     fa.cache_sel_n = tcap < c->N ? tcap : c->N;
-    fa.cache_sel_off = (uint32_t)(((uint64_t)frame * 2654435761ull) % (uint64_t)c->N);
+    (void)frame;
     cs.frame_used = true;
     cs.frame_trained = tcap > 0;
     return XR_OK;
@@ -210,10 +212,10 @@ void cache_after_paths(Context* c) {
     CacheState& cs = c->cache;
     if (!c->fa.cache_on) return;
     uint32_t* err = c->d_counters + kCntError;
-    cudaEventRecord(c->ev[6], c->stream);
+    record_event(c, c->ev[6]);
     launch_cache_infer(cs, cs.queries, c->d_counters + kCntCacheQuery, 0u, nullptr, c->fa.cand_b, err, c->sm_count,
                        c->stream);
-    cudaEventRecord(c->ev[7], c->stream);
+    record_event(c, c->ev[7]);
     if (cs.frame_trained)
         launch_cache_train(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap, true, err, c->sm_count,
                            c->stream);
@@ -304,6 +306,7 @@ xr_status xr_cache_train(XrContext* c, const XrCacheSample* smp, uint32_t n, int
     cudaMemsetAsync(cs.mlp_grad, 0, (size_t)nrc::kMlpParams * 4, c->stream);
     cudaMemsetAsync(cs.grid_grad, 0, nrc::kGridParams * 4, c->stream);
     launch_cache_train(cs, cs.train, nullptr, n, n, apply != 0, c->d_counters + kCntError, c->sm_count, c->stream);
+    if (apply) cs.step++;
     s = cuda_check(c, cudaGetLastError(), "cache train launch");
     float l = 0.0f;
     if (!s) s = cuda_check(c, cudaMemcpyAsync(&l, cs.loss, 4, cudaMemcpyDeviceToHost, c->stream), "cache loss");
@@ -320,6 +323,7 @@ xr_status xr_cache_step(XrContext* c) {
     xr_status s = cache_alloc(c);
     if (s) return s;
     launch_cache_adam(c->cache, c->stream);
+    c->cache.step++;
     c->cache.grads_dirty = false;
     if ((s = cuda_check(c, cudaGetLastError(), "cache step launch"))) return s;
     return xr_sync(c);

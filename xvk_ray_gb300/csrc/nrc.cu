@@ -375,14 +375,33 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict_
 // Adam (Kingma and Ba 2015) and weight images
 // ---------------------------------------------------------------------------
 struct AdamArgs {
-    float lr, b1, b2, eps, bc1, bc2;
+    float lr, b1, b2, eps;
+    const float* state;   // {beta1^t, beta2^t, bc1 = 1 - beta1^t, bc2 = 1 - beta2^t} of the current step
 };
 
-__device__ __forceinline__ void adam_step(float& w, float& m, float& v, float g, const AdamArgs& a) {
+__device__ __forceinline__ void adam_step(float& w, float& m, float& v, float g, const AdamArgs& a, float bc1,
+                                          float bc2) {
     m = a.b1 * m + (1.0f - a.b1) * g;
     v = a.b2 * v + (1.0f - a.b2) * (g * g);
-    const float mh = m / a.bc1, vh = v / a.bc2;
+    const float mh = m / bc1, vh = v / bc2;
     w = w - a.lr * mh / (sqrtf(vh) + a.eps);
+}
+
+// One step of the bias-correction powers: beta^t = beta^(t-1) * beta in FP32, kept
+// on the device so that a replayed frame graph advances them.
+__global__ void k_cache_adam_advance(float* state, float b1, float b2) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const float p1 = state[0] * b1, p2 = state[1] * b2;
+        state[0] = p1;
+        state[1] = p2;
+        state[2] = 1.0f - p1;
+        state[3] = 1.0f - p2;
+    }
+}
+__global__ void k_cache_adam_state_reset(float* state) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        state[0] = 1.0f; state[1] = 1.0f; state[2] = 0.0f; state[3] = 0.0f;
+    }
 }
 
 __device__ __forceinline__ void write_images(uint32_t i, float w, uint8_t* w_fwd, uint8_t* w_bwd) {
@@ -400,7 +419,7 @@ __global__ void k_cache_adam_mlp(float* w, float* g, float* m, float* v, uint8_t
     float wi = w[i];
     if (apply) {
         float mi = m[i], vi = v[i];
-        adam_step(wi, mi, vi, g[i], a);
+        adam_step(wi, mi, vi, g[i], a, a.state[2], a.state[3]);
         w[i] = wi; m[i] = mi; v[i] = vi;
         g[i] = 0.0f;
     }
@@ -414,8 +433,9 @@ __global__ void k_cache_adam_grid(float2* w, float2* g, float2* m, float2* v, __
     const float2 gr = g[e];
     if (gr.x == 0.0f && gr.y == 0.0f) return;
     float2 wi = w[e], mi = m[e], vi = v[e];
-    if (gr.x != 0.0f) adam_step(wi.x, mi.x, vi.x, gr.x, a);
-    if (gr.y != 0.0f) adam_step(wi.y, mi.y, vi.y, gr.y, a);
+    const float bc1 = a.state[2], bc2 = a.state[3];
+    if (gr.x != 0.0f) adam_step(wi.x, mi.x, vi.x, gr.x, a, bc1, bc2);
+    if (gr.y != 0.0f) adam_step(wi.y, mi.y, vi.y, gr.y, a, bc1, bc2);
     w[e] = wi; m[e] = mi; v[e] = vi;
     g[e] = make_float2(0.0f, 0.0f);
     table[e] = __floats2half2_rn(wi.x, wi.y);
@@ -464,8 +484,7 @@ static nrc::AdamArgs adam_args(const CacheState& cs) {
     a.b1 = cs.params.beta1;
     a.b2 = cs.params.beta2;
     a.eps = cs.params.epsilon;
-    a.bc1 = (float)(1.0 - std::pow((double)cs.params.beta1, (double)cs.step));
-    a.bc2 = (float)(1.0 - std::pow((double)cs.params.beta2, (double)cs.step));
+    a.state = cs.adam;
     return a;
 }
 
@@ -536,9 +555,13 @@ void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_
     if (apply) launch_cache_adam(cs, st);
 }
 
+void launch_cache_adam_reset(CacheState& cs, cudaStream_t st) {
+    k_cache_adam_state_reset<<<1, 32, 0, st>>>(cs.adam);
+}
+
 void launch_cache_adam(CacheState& cs, cudaStream_t st) {
-    cs.step++;
     const nrc::AdamArgs a = adam_args(cs);
+    k_cache_adam_advance<<<1, 32, 0, st>>>(cs.adam, cs.params.beta1, cs.params.beta2);
     k_cache_adam_mlp<<<(kMlpParams + 255) / 256, 256, 0, st>>>(cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.w_fwd,
                                                                 cs.w_bwd, a, 1);
     const uint32_t n2 = (uint32_t)(kGridParams / 2);

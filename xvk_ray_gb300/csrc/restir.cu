@@ -222,9 +222,13 @@ struct CacheEmit {
     NeeRay nee;        // training paths: the next-event ray of this vertex
 };
 
+// Training pixels of a frame: (pixel * (2^31 - 1) + off) mod N < cache_sel_n with
+// off = frame * 2654435761 mod N -- a permutation of the pixels that changes every
+// frame (the frame index is read on the device, so a replayed graph follows it).
 __device__ __forceinline__ bool cache_training_pixel(const FrameArgs& fa, uint32_t pixel) {
     if (fa.cache_sel_n == 0u) return false;
-    const uint64_t k = ((uint64_t)pixel * 2147483647ull + fa.cache_sel_off) % (uint64_t)fa.N;
+    const uint64_t off = ((uint64_t)fa.ubo[0].current_frame * 2654435761ull) % (uint64_t)fa.N;
+    const uint64_t k = ((uint64_t)pixel * 2147483647ull + off) % (uint64_t)fa.N;
     return k < fa.cache_sel_n;
 }
 

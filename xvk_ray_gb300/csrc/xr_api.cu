@@ -186,6 +186,8 @@ xr_status stage_ubos(Context* c, const XrUniformBufferObject* ubos, uint32_t n) 
 // Records `e` on the context's stream; inside a stream capture it becomes an
 // event-record node of the graph (an external event), so the host can still
 // wait on it and time with it when the graph is replayed.
+}  // namespace
+
 cudaError_t record_event(Context* c, cudaEvent_t e) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaError_t q = cudaStreamIsCapturing(c->stream, &cs);
@@ -193,6 +195,8 @@ cudaError_t record_event(Context* c, cudaEvent_t e) {
     if (cs == cudaStreamCaptureStatusActive) return cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal);
     return cudaEventRecord(e, c->stream);
 }
+
+namespace {
 
 // Stream side: the transfer itself (also what a captured frame graph replays).
 xr_status enqueue_ubos(Context* c, uint32_t n) {
@@ -559,7 +563,7 @@ static xr_status render_impl(Context* c, const XrUniformBufferObject* ubos, uint
     set_frame_pointers(c, parity);
     if ((s = cache_prepare_frame(c, ubos[0].current_frame))) return s;
     const bool reuse0 = ubos[0].reuse != 0u;
-    if (c->graphs_on && !c->fa.cache_on) {
+    if (c->graphs_on) {
         if (!c->graph[parity] || c->graph_bounces[parity] != (nb | (reuse0 ? 0x100u : 0u))) {
             if (c->graph[parity]) cudaGraphExecDestroy(c->graph[parity]);
             c->graph[parity] = nullptr;
@@ -579,6 +583,7 @@ static xr_status render_impl(Context* c, const XrUniformBufferObject* ubos, uint
     } else if ((s = enqueue_frame(c, n, nb, reuse0))) {
         return s;
     }
+    if (c->cache.frame_trained) c->cache.step++;   // one Adam step per trained frame (the bias correction advances on the device)
     c->frames++;
     c->last_bounces = nb;
     return XR_OK;

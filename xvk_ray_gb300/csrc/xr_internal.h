@@ -138,8 +138,7 @@ struct FrameArgs {
     uint4* cache_q;           // query records, 2 uint4 each (capacity N)
     uint4* cache_t;           // training records, 3 uint4 each (capacity cache_t_cap)
     uint32_t cache_t_cap;
-    uint32_t cache_sel_n;     // training pixels: (pixel * 2^31-1 + cache_sel_off) mod N < cache_sel_n
-    uint32_t cache_sel_off;
+    uint32_t cache_sel_n;     // training pixels per frame (selection in restir.cu: cache_training_pixel)
     float4* cache_nee;        // next-event rays: 3 float4 each {o, record}, {d, tmax}, {contribution, 0}
 };
 
@@ -163,6 +162,7 @@ struct CacheState {
     float* grid_m = nullptr;
     float* grid_v = nullptr;
     float* loss = nullptr;           // mean loss of the last training launch
+    float* adam = nullptr;           // device Adam state {beta1^t, beta2^t, 1 - beta1^t, 1 - beta2^t}
     uint4* queries = nullptr;        // query records (capacity query_cap)
     uint4* train = nullptr;          // training records (capacity train_cap)
     float4* nee = nullptr;           // next-event rays of one bounce (capacity train_cap)
@@ -243,6 +243,8 @@ struct Context {
 
 constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
 void invalidate_graphs(Context* c);
+// Records `e` on the context's stream (an external event node when the stream is being captured).
+cudaError_t record_event(Context* c, cudaEvent_t e);
 xr_status realloc_pixels(Context* c);   // per-pixel buffers and view table for the current views / params
 
 xr_status fail(const Context* ctx, xr_status code, const std::string& msg);
@@ -293,7 +295,8 @@ void launch_cache_infer(CacheState& cs, const uint4* rec, const uint32_t* count_
                         float4* cand_b, uint32_t* err, int sm_count, cudaStream_t st);
 void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
                         uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st);
-void launch_cache_adam(CacheState& cs, cudaStream_t st);   // one Adam step (cs.step incremented) on the gradients
+void launch_cache_adam(CacheState& cs, cudaStream_t st);   // one Adam step on the gradients (bias correction on the device)
+void launch_cache_adam_reset(CacheState& cs, cudaStream_t st);
 // ---- cache_api.cu ----
 xr_status cache_prepare_frame(Context* c, uint32_t frame);   // capacities; sets the FrameArgs cache fields
 void cache_after_paths(Context* c);           // inference (+ training) after the bounce loop
