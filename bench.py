@@ -524,6 +524,119 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+# 4K workload: the 1080p scene's generator scaled to 32,768 objects and 64
+# emissive quads (extent grown to keep the object density), four 3840x2160
+# camera streams (yaw 0/90/180/270 degrees) rendered per launch.
+SCENE_4K = dict(seed=1, n_objects=32768, n_lights=64, extent=40.0 * 8.0 ** 0.5, sphere_subdiv=2)
+RES_4K = (3840, 2160)
+STREAMS_4K = 4
+MLP_FLOP_PER_QUERY = 2 * (4 * 64 * 64 + 16 * 64)          # 34,816 (forward)
+
+
+def run_4k(args):
+    """ms/frame of 4 x 3840x2160 streams of an 8M-triangle scene, plain ReSTIR GI
+    and ReSTIR GI + learned cache, both replayed from frame graphs; relMSE of both
+    against the FP64 reference of the last frame."""
+    import ctypes as C
+
+    import numpy as np
+    dist, rank, ws, local = _dist()
+    import xvk_ray_gb300 as xr
+    from xvk_ray_gb300 import _build
+    _build.build_library()
+    L = xr._lib
+    lib = L.load()
+    scene = xr.Scene.procedural(**SCENE_4K)
+    w, h = RES_4K
+    views = [(0, w, h)] * STREAMS_4K
+    n_frames = args.warmup + args.steps
+    cams = []
+    for k in range(STREAMS_4K):
+        cam = L.XrCamera.from_buffer_copy(scene.camera)
+        cam.yaw_deg += 90.0 * k
+        cams.append(cam)
+    frames, prev = [], [None] * STREAMS_4K
+    for f in range(n_frames):
+        row = []
+        for k in range(STREAMS_4K):
+            cams[k].position[2] -= 0.01
+            cams[k].yaw_deg += 0.2
+            u = xr.camera_ubo(cams[k], w, h, prev[k], f, BOUNCES, sky=False, reuse=True)
+            prev[k] = u
+            row.append(u)
+        frames.append(row)
+    peaks = _peaks()
+    out, ref = {}, None
+    for variant in ("restir_gi", "restir_gi_mlp_cache"):
+        r = xr.Renderer(8, 8, device=local)
+        r.upload_scenes([scene])
+        r.set_views(views, xr.params_default(8, 8, write_hdr=1, write_pt=1))
+        if variant == "restir_gi_mlp_cache":
+            cp = xr.cache_params_default()
+            cp.enabled = 1
+            cp.train_samples = 65536
+            r.cache.set_params(cp)
+        r.set_graphs(True)
+        for f in range(args.warmup):
+            r.render_views(frames[f])
+        r.sync()
+        _barrier(dist, local)
+        clocks = ClockSampler(local)
+        clocks.start()
+        L.check(lib.xr_event_record(r.ctx, 0), r.ctx)
+        for f in range(args.warmup, n_frames):
+            r.render_views(frames[f])
+        L.check(lib.xr_event_record(r.ctx, 1), r.ctx)
+        ms = C.c_float()
+        L.check(lib.xr_event_elapsed(r.ctx, 0, 1, C.byref(ms)), r.ctx)
+        clk = clocks.stop()
+        st = r.stats()
+        N = w * h * STREAMS_4K
+        entry = {"ms_per_frame": round(_max_over_ranks(dist, float(ms.value), f"cuda:{local}") / args.steps, 4),
+                 "passes_ms": {"initial_sample": round(st.ms_initial, 4), "temporal": round(st.ms_temporal, 4),
+                               "spatial": round(st.ms_spatial, 4)},
+                 "rays_per_frame": int(st.rays_traced + st.shadow_rays),
+                 "temporal_hbm_gbs": round(TEMPORAL_BYTES_PER_PX * N / (st.ms_temporal * 1e-3) / 1e9, 1),
+                 "clocks": clk}
+        entry["rays_per_s"] = round(entry["rays_per_frame"] / (entry["ms_per_frame"] * 1e-3), 1)
+        if variant == "restir_gi_mlp_cache":
+            cs = r.cache.stats()
+            flops = cs.queries * MLP_FLOP_PER_QUERY
+            entry["cache"] = {"queries": cs.queries, "train_samples": cs.train_samples, "loss": round(cs.loss, 4),
+                              "ms_infer": round(cs.ms_infer, 4), "ms_train": round(cs.ms_train, 4),
+                              "inference_tflops": round(flops / (cs.ms_infer * 1e-3) / 1e12, 2),
+                              "inference_tensor_frac_of_measured_bf16_peak":
+                                  round(flops / (cs.ms_infer * 1e-3) / 1e12 / peaks["bf16_tflops"], 4)
+                                  if peaks.get("bf16_tflops") else None}
+        hdr = [r.read_view_output(v, L.XR_OUT_HDR) for v in range(STREAMS_4K)]
+        if ref is None and args.relmse_spp > 0:
+            ref = r.render_reference_views(frames[-1], 1_000_000, max(1, args.relmse_spp // 8))
+            pt = [r.read_view_output(v, L.XR_OUT_PT) for v in range(STREAMS_4K)]
+            out["pt_1spp"] = float(np.mean([relmse(p, q) for p, q in zip(pt, ref)]))
+        if ref is not None:
+            entry["relmse"] = float(np.mean([relmse(p, q) for p, q in zip(hdr, ref)]))
+        out[variant] = entry
+        r.close()
+    if rank != 0:
+        return
+    plain, cached = out["restir_gi"], out["restir_gi_mlp_cache"]
+    line = {
+        "metric": "ms/frame, 4 camera streams x 3840x2160, 8M triangles, ReSTIR GI + learned cache (one launch set per frame, CUDA graph)",
+        "value": cached["ms_per_frame"], "unit": "ms/frame", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": cached["ms_per_frame"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (bf16 MLP)", "data": "synthetic (procedural scene, seed 1, 32768 objects, 64 emissive quads)",
+        "config": {"workload": f"{STREAMS_4K} x {w}x{h}, {scene.n_triangles} triangles, {n_frames}-frame camera sweep, "
+                               "corrected ReSTIR GI (M cap 20, 5 neighbours, 30 px, shadow rays) + learned cache, depth 4",
+                   "parallelism": f"replicas x{ws}", "l2": "working set far larger than L2"},
+        "restir_gi": plain, "restir_gi_mlp_cache": cached, "pt_1spp_relmse": out.get("pt_1spp"),
+        "relmse_ratio_cache_over_plain": (round(cached["relmse"] / plain["relmse"], 4) if "relmse" in plain else None),
+        "reference": (f"FP64-accumulated plain path tracer, {max(1, args.relmse_spp // 8)} spp, last frame"
+                      if args.relmse_spp > 0 else None),
+        "gpu_launches": FRAME_LAUNCHES * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -536,8 +649,9 @@ def main():
     ap.add_argument("--width", type=int, default=1920, help="smaller extents are for profiling only")
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--objects", type=int, default=4096, help="scene objects (4096 -> 998,442 triangles)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch"],
-                    help="frame: 1080p / 1M triangles (the headline); batch: 64 views over 8 scenes")
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "4k"],
+                    help="frame: 1080p / 1M triangles (the headline); batch: 64 views over 8 scenes; "
+                         "4k: 4 x 3840x2160 streams, 8M triangles, learned cache")
     args = ap.parse_args()
     global W, H
     W, H = args.width, args.height
@@ -548,6 +662,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "4k":
+        run_4k(args)
     else:
         run_ours(args)
 

@@ -284,6 +284,9 @@ xr_status xr_set_views(XrContext* ctx, const XrView* views, uint32_t n, const Xr
    With graphs enabled the frame's launches are captured once per parity and replayed. */
 xr_status xr_render_views(XrContext* ctx, const XrUniformBufferObject* ubos);
 xr_status xr_read_view_output(XrContext* ctx, uint32_t view, uint32_t which, void* host, size_t bytes);
+/* xr_render_reference for every view: host_rgb holds 3 doubles per pixel of all views, view by view. */
+xr_status xr_render_reference_views(XrContext* ctx, const XrUniformBufferObject* ubos, uint32_t frame0, uint32_t spp,
+                                    double* host_rgb);
 xr_status xr_set_graphs(XrContext* ctx, int enabled);   /* CUDA-graph replay of frames (not with the cache) */
 
 /* Launch configuration chosen by xr_autotune: persistent CTAs per SM of the

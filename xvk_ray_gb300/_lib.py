@@ -169,6 +169,7 @@ _SIGS = {
     "xr_set_views": (_i32, [_P, _P, _u32, C.POINTER(XrParams)]),
     "xr_render_views": (_i32, [_P, _P]),
     "xr_read_view_output": (_i32, [_P, _u32, _u32, _P, C.c_size_t]),
+    "xr_render_reference_views": (_i32, [_P, _P, _u32, _u32, _P]),
     "xr_set_graphs": (_i32, [_P, C.c_int]),
     "xr_autotune": (_i32, [_P, _P, _u32, C.POINTER(XrTuning)]),
     "xr_set_tuning": (_i32, [_P, C.POINTER(XrTuning)]),

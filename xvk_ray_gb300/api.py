@@ -182,6 +182,18 @@ class Renderer:
         self._c(self._lib.xr_read_view_output(self.ctx, view, which, _ptr(out), out.nbytes))
         return out
 
+    def render_reference_views(self, ubos: "list[L.XrUniformBufferObject]", frame0: int, spp: int) -> "list[np.ndarray]":
+        """FP64 reference of every view (list of (W*H, 3) float64 arrays)."""
+        arr = (L.XrUniformBufferObject * len(ubos))(*ubos)
+        n = sum(w * h for _, w, h in self.views)
+        out = np.empty((n, 3), np.float64)
+        self._c(self._lib.xr_render_reference_views(self.ctx, C.cast(arr, C.c_void_p), frame0, spp, _ptr(out)))
+        res, off = [], 0
+        for _, w, h in self.views:
+            res.append(out[off:off + w * h])
+            off += w * h
+        return res
+
     def set_graphs(self, enabled: bool) -> None:
         self._c(self._lib.xr_set_graphs(self.ctx, 1 if enabled else 0))
 

@@ -708,30 +708,32 @@ xr_status xr_autotune(XrContext* c, const XrUniformBufferObject* ubos, uint32_t 
     return XR_OK;
 }
 
-xr_status xr_render_reference(XrContext* c, const XrUniformBufferObject* ubo, uint32_t frame0, uint32_t spp,
-                              double* host_rgb) {
-    if (!c || !ubo || !host_rgb || spp == 0) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_reference: bad argument");
-    if (!c->params_set || !c->bvh_ready) return fail(c, XR_ERR_STATE, "render_reference: parameters and BVH required");
-    if (!c->params.write_pt) return fail(c, XR_ERR_STATE, "render_reference: set write_pt in the parameters");
-    if (ubo->number_of_bounces > kMaxBounces) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_reference: too many bounces");
+// FP64 accumulation of spp samples of the plain path tracer for the n views.
+static xr_status render_reference_impl(XrContext* c, const XrUniformBufferObject* ubos, uint32_t n, uint32_t frame0,
+                                       uint32_t spp, double* host_rgb, const char* who) {
+    if (!c->params_set || !c->bvh_ready) return fail(c, XR_ERR_STATE, std::string(who) + ": parameters and BVH required");
+    if (!c->params.write_pt) return fail(c, XR_ERR_STATE, std::string(who) + ": set write_pt in the parameters");
+    for (uint32_t i = 0; i < n; i++)
+        if (ubos[i].number_of_bounces != ubos[0].number_of_bounces || ubos[i].number_of_bounces > kMaxBounces)
+            return fail(c, XR_ERR_INVALID_ARGUMENT, std::string(who) + ": number_of_bounces must be equal and <= 31");
     if (c->params.compat_reference && c->scene_has_non_lambert)
-        return fail(c, XR_ERR_UNSUPPORTED, "render_reference: reference mode renders only Lambertian and DiffuseLight materials");
+        return fail(c, XR_ERR_UNSUPPORTED, std::string(who) + ": reference mode renders only Lambertian and DiffuseLight materials");
     DeviceGuard g(c->device);
     const size_t n3 = (size_t)c->N * 3;
     double* acc = nullptr;
     xr_status s = cuda_check(c, cudaMalloc((void**)&acc, n3 * sizeof(double)), "render_reference alloc");
     if (s) return s;
     cudaMemsetAsync(acc, 0, n3 * sizeof(double), c->stream);
-    XrUniformBufferObject u = *ubo;
+    std::vector<XrUniformBufferObject> u(ubos, ubos + n);
     for (uint32_t k = 0; k < spp && !s; k++) {
-        u.current_frame = frame0 + k;
-        if ((s = upload_ubo(c, &u))) break;
-        set_frame_pointers(c, u.current_frame % 2u);
+        for (auto& x : u) x.current_frame = frame0 + k;
+        if ((s = stage_ubos(c, u.data(), n)) || (s = enqueue_ubos(c, n))) break;
+        set_frame_pointers(c, u[0].current_frame % 2u);
         c->fa.cache_on = 0;   // the converged reference is the plain path tracer
         c->fa.cache_sel_n = 0;
         c->cache.frame_used = false;
         cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);
-        launch_initial(c->fa, u.number_of_bounces, c->stream);
+        launch_initial(c->fa, u[0].number_of_bounces, c->stream);
         launch_accumulate_sample(c->fa, acc, c->stream);
         s = cuda_check(c, cudaGetLastError(), "render_reference launch");
     }
@@ -742,6 +744,19 @@ xr_status xr_render_reference(XrContext* c, const XrUniformBufferObject* ubo, ui
     if (s) return s;
     for (size_t i = 0; i < n3; i++) host_rgb[i] /= (double)spp;
     return XR_OK;
+}
+
+xr_status xr_render_reference(XrContext* c, const XrUniformBufferObject* ubo, uint32_t frame0, uint32_t spp,
+                              double* host_rgb) {
+    if (!c || !ubo || !host_rgb || spp == 0) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_reference: bad argument");
+    if (c->fa.n_views > 1u) return fail(c, XR_ERR_STATE, "render_reference: the context has several views");
+    return render_reference_impl(c, ubo, 1u, frame0, spp, host_rgb, "render_reference");
+}
+
+xr_status xr_render_reference_views(XrContext* c, const XrUniformBufferObject* ubos, uint32_t frame0, uint32_t spp,
+                                    double* host_rgb) {
+    if (!c || !ubos || !host_rgb || spp == 0) return fail(c, XR_ERR_INVALID_ARGUMENT, "render_reference_views: bad argument");
+    return render_reference_impl(c, ubos, c->fa.n_views, frame0, spp, host_rgb, "render_reference_views");
 }
 
 xr_status xr_sync(XrContext* c) {
