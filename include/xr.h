@@ -262,6 +262,22 @@ xr_status xr_scene_procedural(const XrProceduralDesc* desc, XrSceneData* out);
 xr_status xr_alloc_host(size_t bytes, void** ptr);
 void xr_free_host(void* ptr);
 
+/* ---- base-colour textures: replaces the reference's per-model image upload
+        (src/Asset/Scene.cpp:56-72, src/Asset/TextureImage.cpp:25 -- R8G8B8A8_UNORM)
+        and its sampler (src/Vulkan/XVKSampler.h:11-27: linear, clamp to edge).
+   RGBA8 texels, row 0 = texture coordinate v = 0; a material whose
+   base_color_texture_index >= 0 takes the bilinearly filtered texture RGB instead of
+   its base colour (BSDF.hlsl:22-23).  Upload the textures before the scene(s) that
+   use them; the texture list is shared by all scenes of the context. */
+typedef struct XrTexture {
+    uint32_t width, height;
+    const uint8_t* rgba8;        /* width * height * 4 bytes */
+} XrTexture;
+xr_status xr_upload_textures(XrContext* ctx, const XrTexture* textures, uint32_t n);
+/* PNG scanline reconstruction for the scene loader (filters None/Sub/Up/Average/Paeth):
+   filtered = rows x (1 filter byte + row_bytes), bpp = bytes per pixel (1..8); no GPU. */
+xr_status xr_png_unfilter(const uint8_t* filtered, uint32_t rows, uint32_t row_bytes, uint32_t bpp, uint8_t* out);
+
 /* ---- several scenes and views in one context ----
    No single counterpart in the reference, which renders one view of one scene per
    Render call (ApplicationReSTIRGI.cpp:150-275): here one frame renders every view

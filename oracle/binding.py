@@ -33,6 +33,7 @@ def load():
             "or_oct_roundtrip": (None, [P, u32, u32, P, P]),
             "or_scene_create": (P, [P, u32, P, u32, P, u32]),
             "or_scene_destroy": (None, [P]),
+            "or_scene_set_textures": (None, [P, P, u32, P]),
             "or_trace": (None, [P, P, u32, C.c_int, P, P, P]),
             "or_renderer_create": (P, [P, P]),
             "or_renderer_destroy": (None, [P]),
@@ -103,7 +104,13 @@ class OracleScene:
 
     @staticmethod
     def from_scene(scene) -> "OracleScene":
-        return OracleScene(scene.vertices, scene.global_indices(), scene.materials)
+        o = OracleScene(scene.vertices, scene.global_indices(), scene.materials)
+        textures = getattr(scene, "textures", None) or []
+        if textures:
+            sizes = np.array([[t.shape[1], t.shape[0]] for t in textures], np.uint32)
+            texels = np.concatenate([np.ascontiguousarray(t, np.uint8).reshape(-1) for t in textures])
+            load().or_scene_set_textures(o.h, _p(sizes), len(textures), _p(texels))
+        return o
 
     def trace(self, rays: np.ndarray, any_hit: bool = False):
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)

@@ -130,6 +130,9 @@ struct Scene {
     std::vector<BNode> nodes;
     std::vector<uint32_t> order;
     bool brute = true;
+    // base-colour textures: per texture {first texel, width, height}, RGBA8 texels
+    std::vector<uint32_t> tex_info;
+    std::vector<uint32_t> texels;
     // emissive triangles (next-event estimation of the radiance cache's training paths)
     std::vector<uint32_t> light_prim;
     std::vector<float> light_cdf, light_pmf, prim_light_pdf;
@@ -549,6 +552,45 @@ inline uint8_t to_unorm8(float v) {
     return (uint8_t)(int)(v * 255.0f + 0.5f);
 }
 
+// Bilinear sampling with clamp to edge of an RGBA8 UNORM texture (the reference's
+// sampler, src/Vulkan/XVKSampler.h:11-27, on R8G8B8A8_UNORM images), the same
+// operations in the same order as the kernels' tex_bilinear.
+inline f3 tex_bilinear(const Scene& s, uint32_t t, f2 uv) {
+    const uint32_t off = s.tex_info[3 * (size_t)t], wu = s.tex_info[3 * (size_t)t + 1], hu = s.tex_info[3 * (size_t)t + 2];
+    const int w = (int)wu, h = (int)hu;
+    float x = uv.x * (float)w - 0.5f, y = uv.y * (float)h - 0.5f;
+    if (!std::isfinite(x)) x = 0.0f;
+    if (!std::isfinite(y)) y = 0.0f;
+    x = fminf(fmaxf(x, -1.0f), (float)w);
+    y = fminf(fmaxf(y, -1.0f), (float)h);
+    const float x0f = floorf(x), y0f = floorf(y);
+    const float fx = x - x0f, fy = y - y0f;
+    const int x0 = (int)x0f, y0 = (int)y0f;
+    const int xa = std::min(std::max(x0, 0), w - 1), xb = std::min(std::max(x0 + 1, 0), w - 1);
+    const int ya = std::min(std::max(y0, 0), h - 1), yb = std::min(std::max(y0 + 1, 0), h - 1);
+    auto texel = [&](int xx, int yy, int ch) {
+        const uint32_t v = s.texels[off + (size_t)yy * w + xx];
+        return (float)((v >> (8 * ch)) & 255u) / 255.0f;
+    };
+    const float gx = 1.0f - fx, gy = 1.0f - fy;
+    float c[3];
+    for (int ch = 0; ch < 3; ch++)
+        c[ch] = (texel(xa, ya, ch) * gx + texel(xb, ya, ch) * fx) * gy + (texel(xa, yb, ch) * gx + texel(xb, yb, ch) * fx) * fy;
+    return f3{c[0], c[1], c[2]};
+}
+
+// Material m at texture coordinate uv: a base-colour texture replaces the base
+// colour's RGB (BSDF.hlsl:22-23).
+inline Material resolve_material(const Scene& s, uint32_t m, f2 uv) {
+    Material r = s.mat[m];
+    const uint32_t n_tex = (uint32_t)(s.tex_info.size() / 3);
+    if (r.tex >= 0 && (uint32_t)r.tex < n_tex) {
+        const f3 c = tex_bilinear(s, (uint32_t)r.tex, uv);
+        r.base[0] = c.x; r.base[1] = c.y; r.base[2] = c.z;
+    }
+    return r;
+}
+
 void build_lights(Scene& s) {
     std::vector<float> area, power;
     for (uint32_t t = 0; t < s.ntri; t++) {
@@ -616,7 +658,13 @@ f3 next_event(const Scene& sc, const Material& mat, f3 x, f3 n, f3 g, f3 wo, f3 
     if (!(wil.z > 0.0f)) return zero;
     const Lobe lb = eval_material(mat, to_local(wo, T, B, n), wil);
     const float pdf_l = sc.prim_light_pdf[prim] * dist2 / cos_l;
-    const Material& lm = sc.mat[vert_mat(sc, sc.idx[(size_t)prim * 3])];
+    const uint32_t li0 = sc.idx[(size_t)prim * 3], li1 = sc.idx[(size_t)prim * 3 + 1], li2 = sc.idx[(size_t)prim * 3 + 2];
+    f2 luv{0.0f, 0.0f};
+    if (!sc.tex_info.empty()) {
+        const f2 t0 = vert_uv(sc, li0), t1 = vert_uv(sc, li1), t2 = vert_uv(sc, li2);
+        luv = f2{t0.x * b0 + t1.x * b1 + t2.x * b2, t0.y * b0 + t1.y * b1 + t2.y * b2};
+    }
+    const Material lm = resolve_material(sc, (uint32_t)vert_mat(sc, li0), luv);
     const f3 Le = f3{lm.base[0], lm.base[1], lm.base[2]} * 4.0f;
     const f3 contrib = thr * Le * lb.f * (wil.z / (pdf_l + lb.pdf));
     if (!(contrib.x + contrib.y + contrib.z > 0.0f)) return zero;
@@ -642,6 +690,7 @@ struct Renderer {
     std::vector<uint32_t> prev_code, prev_mat;
     std::vector<f3> le0, thr0;
     std::vector<f4> hdr, pt;
+    std::vector<f2> gb_uv;                // texture coordinate of the visible point (textured scenes)
     std::vector<uint8_t> ldr;
     std::vector<uint32_t> written;
     // learned radiance cache (corrected mode, or_renderer_set_cache): per pixel the
@@ -722,7 +771,8 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
             }
             break;
         }
-        const Material& mat = sc.mat[pl.mat];
+        const Material mat = resolve_material(sc, (uint32_t)pl.mat, pl.uv);
+        if (bounce == 0 && !sc.tex_info.empty()) R.gb_uv[p] = pl.uv;
         if (!compat) {
             f3 wo = -direction;
             if (dot(pl.geo_normal, wo) < 0.0f) pl.geo_normal = -pl.geo_normal;
@@ -874,19 +924,19 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
 constexpr float kReuseMinRoughness = 0.25f;
 
 struct PixelShading {
-    const Material* m;
+    Material m;
     f3 x, n, wo, T, B;
     bool reuse;
 };
-inline PixelShading pixel_shading(const Renderer& R, const Sample& s, const OrUBO& u) {
+inline PixelShading pixel_shading(const Renderer& R, const Sample& s, const OrUBO& u, uint32_t p) {
     PixelShading P;
-    P.m = &R.sc->mat[s.materialID];
+    P.m = resolve_material(*R.sc, s.materialID, R.sc->tex_info.empty() ? f2{0.0f, 0.0f} : R.gb_uv[p]);
     P.x = s.x_view;
     P.n = s.n_view;
     f3 cam = xyz(mul(u.view_inverse, f4{0, 0, 0, 1}));
     P.wo = normalize(cam - P.x);
     branchless_onb(P.n, &P.T, &P.B);
-    const bool glossy = (P.m->model == MAT_METALLIC || P.m->model == MAT_PLASTIC) && P.m->fuzz < kReuseMinRoughness;
+    const bool glossy = (P.m.model == MAT_METALLIC || P.m.model == MAT_PLASTIC) && P.m.fuzz < kReuseMinRoughness;
     P.reuse = !glossy;
     return P;
 }
@@ -894,7 +944,7 @@ inline float target_corrected(const PixelShading& P, f3 xs, f3 L) {
     f3 wi = normalize(xs - P.x);
     float c = dot(P.n, wi);
     if (c <= 0.0f) return 0.0f;
-    f3 f = eval_material(*P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n)).f;
+    f3 f = eval_material(P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n)).f;
     return length(L * f * c);
 }
 
@@ -912,8 +962,8 @@ void shade_output(Renderer& R, uint32_t p, const Reservoir& r, const Sample& s_n
             // at that one direction (the sampled direction left from a point offset
             // along the normal, and in a sharp lobe f alone varies by orders of
             // magnitude over that angle)
-            const PixelShading P = pixel_shading(R, s_new, u);
-            const Lobe lb = eval_material(*P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n));
+            const PixelShading P = pixel_shading(R, s_new, u, p);
+            const Lobe lb = eval_material(P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n));
             if (P.reuse) color = r.s.L_out * r.W * lb.f * cos_theta;
             else if (lb.pdf > 0.0f) color = r.s.L_out * lb.f * (cos_theta / lb.pdf);
             write_output(R, p, color, true);
@@ -967,7 +1017,7 @@ void temporal_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u, bool ou
             }
         }
         if (!R.P.temporal_on) found = false;
-    } else if (R.P.temporal_on && pixel_shading(R, s_new, u).reuse) {
+    } else if (R.P.temporal_on && pixel_shading(R, s_new, u, p).reuse) {
         f2 puv = world_to_screen_uv(s_new.x_view, u.view_prev, u.projection_prev);
         float fx = floorf(puv.x * (float)R.W), fy = floorf(puv.y * (float)R.H);
         if (fx >= 0.0f && fx < (float)R.W && fy >= 0.0f && fy < (float)R.H) {
@@ -982,7 +1032,7 @@ void temporal_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u, bool ou
     f3 x_curr = s_new.x_view;
     f3 n_curr = normalize(s_new.n_view);
     PixelShading P{};
-    if (!compat) P = pixel_shading(R, s_new, u);
+    if (!compat) P = pixel_shading(R, s_new, u, p);
     auto target = [&](const Sample& smp) {
         return compat ? eval_target(smp, x_curr, n_curr) : target_corrected(P, smp.x_sample, smp.L_out);
     };
@@ -1050,7 +1100,7 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
     Reservoir center = R.temporal[read_off + p];
     Reservoir r_s = init_reservoir();
     PixelShading P{};
-    if (!compat) P = pixel_shading(R, s_new, u);
+    if (!compat) P = pixel_shading(R, s_new, u, p);
     auto target = [&](const Sample& smp) {
         return compat ? p_hat_of(smp.L_out) : target_corrected(P, smp.x_sample, smp.L_out);
     };
@@ -1167,6 +1217,24 @@ void* or_scene_create(const float* vertices, uint32_t nv, const uint32_t* indice
 }
 void or_scene_destroy(void* scene) { delete (Scene*)scene; }
 
+// Base-colour textures (n; sizes as width, height pairs; texels RGBA8 concatenated,
+// row 0 = v 0) -- the layout of xr_upload_textures.
+void or_scene_set_textures(void* scene, const uint32_t* sizes2, uint32_t n, const uint8_t* rgba8) {
+    Scene& s = *(Scene*)scene;
+    s.tex_info.clear();
+    s.texels.clear();
+    size_t off = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t w = sizes2[2 * i], h = sizes2[2 * i + 1];
+        s.tex_info.push_back((uint32_t)off);
+        s.tex_info.push_back(w);
+        s.tex_info.push_back(h);
+        off += (size_t)w * h;
+    }
+    s.texels.resize(off);
+    if (off) std::memcpy(s.texels.data(), rgba8, off * 4);
+}
+
 void or_trace(void* scene, const float* rays, uint32_t n, int any_hit, int32_t* prim, float* t,
               float* bary) {
     const Scene& s = *(const Scene*)scene;
@@ -1205,6 +1273,7 @@ void* or_renderer_create(void* scene, const OrParams* params) {
     R->pt.assign(N, f4{0, 0, 0, 0});
     R->ldr.assign(4 * (size_t)N, 0);
     R->written.assign(N, 0);
+    R->gb_uv.assign(N, f2{0.0f, 0.0f});
     return R;
 }
 void or_renderer_destroy(void* r) { delete (Renderer*)r; }

@@ -83,6 +83,8 @@ void or_oct_roundtrip(const float* n3, uint32_t count, uint32_t bits, float* out
 void* or_scene_create(const float* vertices, uint32_t nv, const uint32_t* indices, uint32_t ntri,
                       const float* materials, uint32_t nm);
 void or_scene_destroy(void* scene);
+/* Base-colour textures: n sizes (width, height pairs) and the RGBA8 texels concatenated. */
+void or_scene_set_textures(void* scene, const uint32_t* sizes2, uint32_t n, const uint8_t* rgba8);
 /* rays: n x 8 floats (o.xyz, tmin, d.xyz, tmax). any_hit=1 stops at the first hit.
    prim: -1 on miss.  t, bary (b1, b2) are written on hit. */
 void or_trace(void* scene, const float* rays, uint32_t n, int any_hit,

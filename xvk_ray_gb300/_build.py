@@ -34,7 +34,7 @@ NVCC_FLAGS = ARCH + [
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 
 CU_SOURCES = ["bvh_build.cu", "trace.cu", "trace_noalloc.cu", "restir.cu", "nrc.cu", "cache_api.cu", "batch.cu", "xr_api.cu"]
-CXX_SOURCES = ["scene_gen.cpp"]
+CXX_SOURCES = ["scene_gen.cpp", "image_io.cpp"]
 
 
 def _nvcc() -> str:

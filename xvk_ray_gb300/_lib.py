@@ -112,6 +112,10 @@ class XrCacheStats(C.Structure):
                 ("inv_extent", C.c_float)]
 
 
+class XrTexture(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgba8", C.POINTER(C.c_uint8))]
+
+
 class XrView(C.Structure):
     _fields_ = [("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32)]
 
@@ -165,6 +169,8 @@ _SIGS = {
     "xr_event_elapsed": (_i32, [_P, _u32, _u32, C.POINTER(C.c_float)]),
     "xr_alloc_host": (_i32, [C.c_size_t, C.POINTER(_P)]),
     "xr_free_host": (None, [_P]),
+    "xr_upload_textures": (_i32, [_P, _P, _u32]),
+    "xr_png_unfilter": (_i32, [_P, _u32, _u32, _u32, _P]),
     "xr_upload_scenes": (_i32, [_P, _P, _u32]),
     "xr_set_views": (_i32, [_P, _P, _u32, C.POINTER(XrParams)]),
     "xr_render_views": (_i32, [_P, _P]),

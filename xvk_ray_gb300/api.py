@@ -5,7 +5,7 @@ Every call goes through libxr.so; numpy holds host arrays only.
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -31,6 +31,7 @@ class Scene:
     materials: np.ndarray
     ranges: np.ndarray
     camera: L.XrCamera
+    textures: list = field(default_factory=list)   # (height, width, 4) uint8 RGBA, row 0 = v 0
 
     @property
     def n_triangles(self) -> int:
@@ -132,7 +133,18 @@ class Renderer:
         self.close()
 
     # -- scene / BVH --
+    def upload_textures(self, textures: "list[np.ndarray]") -> None:
+        """RGBA8 textures, each (height, width, 4) uint8 with row 0 at v = 0."""
+        keep = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        arr = (L.XrTexture * max(len(keep), 1))()
+        for k, t in enumerate(keep):
+            arr[k].width, arr[k].height = t.shape[1], t.shape[0]
+            arr[k].rgba8 = C.cast(_ptr(t), C.POINTER(C.c_uint8))
+        self._c(self._lib.xr_upload_textures(self.ctx, C.cast(arr, C.c_void_p), len(keep)))
+
     def upload_scene(self, scene: Scene) -> None:
+        if scene.textures:
+            self.upload_textures(scene.textures)
         v = np.ascontiguousarray(scene.vertices, np.float32)
         i = np.ascontiguousarray(scene.indices, np.uint32)
         m = np.ascontiguousarray(scene.materials, np.float32)

@@ -70,6 +70,7 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
     for (uint32_t k = 0; k < n && !s; k++) {
         const XrSceneData& sd = scenes[k];
         if ((s = xr_create(&dd, &parts[k]))) break;
+        parts[k]->n_tex = c->n_tex;   // texture indices are checked against the context's texture list
         if ((s = xr_upload_scene(parts[k], (const XrVertex*)sd.vertices, sd.vertex_count, (const uint32_t*)sd.indices,
                                  sd.index_count, (const XrMaterial*)sd.materials, sd.material_count, nullptr, 0)))
             break;
@@ -95,15 +96,16 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
     }
     cudaStreamSynchronize(c->stream);
     invalidate_graphs(c);
-    cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
+    cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats); cudaFree(c->d_vuv);
     cudaFree(c->d_nodes); cudaFree(c->d_tris);
-    c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr;
+    c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr; c->d_vuv = nullptr;
     c->d_nodes = nullptr; c->d_tris = nullptr;
     c->scene_ready = false;
     c->bvh_ready = false;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_tri_idx, std::max<size_t>(ntri, 1) * 16), "scene alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_vpos, std::max<size_t>(nv, 1) * 16), "scene alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_vnrm, std::max<size_t>(nv, 1) * 16), "scene alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_vuv, std::max<size_t>(nv, 1) * 8), "scene alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_mats, std::max<size_t>(nm, 1) * sizeof(XrMaterial)), "scene alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_nodes, std::max<size_t>(nodes, 1) * sizeof(WideNode)), "bvh alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_tris, std::max<size_t>(slots, 1) * 48), "bvh alloc"))) {
@@ -121,6 +123,7 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
         if (p->nv) {
             cudaMemcpyAsync(c->d_vpos + ov, p->d_vpos, (size_t)p->nv * 16, cudaMemcpyDeviceToDevice, c->stream);
             cudaMemcpyAsync(c->d_vnrm + ov, p->d_vnrm, (size_t)p->nv * 16, cudaMemcpyDeviceToDevice, c->stream);
+            cudaMemcpyAsync(c->d_vuv + ov, p->d_vuv, (size_t)p->nv * 8, cudaMemcpyDeviceToDevice, c->stream);
         }
         if (p->nm)
             cudaMemcpyAsync(c->d_mats + om, p->d_mats, (size_t)p->nm * sizeof(XrMaterial), cudaMemcpyDeviceToDevice,
@@ -162,6 +165,7 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
     sc.mats = c->d_mats; sc.n_mats = c->nm; sc.ntri = c->ntri;
     sc.light_prim = c->d_light_prim; sc.light_cdf = c->d_light_cdf; sc.light_pmf = c->d_light_pmf;
     sc.prim_light_pdf = c->d_prim_light_pdf; sc.n_lights = c->n_lights;
+    sc.vuv = c->d_vuv; sc.tex_info = c->d_tex_info; sc.texels = c->d_texels; sc.n_tex = c->n_tex;
     // the views' roots follow the new scene list
     if (c->pix_mem) {
         cudaStreamSynchronize(c->stream);

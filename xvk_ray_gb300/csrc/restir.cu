@@ -19,6 +19,7 @@
 
 #include "bsdf.cuh"
 #include "nrc.cuh"
+#include "texture.cuh"
 #include "wavefront_trace.cuh"
 
 namespace xr {
@@ -33,6 +34,7 @@ constexpr int kBlock = 128;
 
 struct HitPayload {
     float3 pos, normal, geo;
+    float2 uv;
     int32_t mat;
     float t;
 };
@@ -48,6 +50,11 @@ __device__ __forceinline__ HitPayload closest_hit(const DeviceScene& sc, const H
     float3 normal = normalize(nm);
     float3 v0 = xyz(__ldg(sc.vpos + id.x)), v1 = xyz(__ldg(sc.vpos + id.y)), v2 = xyz(__ldg(sc.vpos + id.z));
     pl.pos = v0 * bx + v1 * by + v2 * bz;
+    pl.uv = make_float2(0.0f, 0.0f);
+    if (sc.n_tex) {
+        const float2 u0 = __ldg(sc.vuv + id.x), u1 = __ldg(sc.vuv + id.y), u2 = __ldg(sc.vuv + id.z);
+        pl.uv = make_float2(u0.x * bx + u1.x * by + u2.x * bz, u0.y * bx + u1.y * by + u2.y * bz);
+    }
     float3 e0 = v2 - v0, e1 = v1 - v0;
     pl.geo = normalize(cross(e0, e1));
     pl.normal = normalize(normal);
@@ -201,7 +208,12 @@ __device__ __forceinline__ NeeRay next_event(const DeviceScene& sc, const XrMate
     if (!(wil.z > 0.0f)) return r;
     const Lobe lb = eval_material(mat, to_local(wo, T, B, n), wil);
     const float pdf_l = sc.prim_light_pdf[prim] * dist2 / cos_l;
-    const XrMaterial& lm = sc.mats[id.w];
+    float2 luv = make_float2(0.0f, 0.0f);
+    if (sc.n_tex) {
+        const float2 t0 = __ldg(sc.vuv + id.x), t1 = __ldg(sc.vuv + id.y), t2 = __ldg(sc.vuv + id.z);
+        luv = make_float2(t0.x * b0 + t1.x * b1 + t2.x * b2, t0.y * b0 + t1.y * b1 + t2.y * b2);
+    }
+    const XrMaterial lm = resolve_material(sc, id.w, luv);
     const float3 Le = f3(lm.base_color[0], lm.base_color[1], lm.base_color[2]) * 4.0f;
     r.contrib = thr * Le * lb.f * (wil.z / (pdf_l + lb.pdf));
     if (!(r.contrib.x + r.contrib.y + r.contrib.z > 0.0f)) return r;
@@ -263,7 +275,8 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
         else if (bounce == 1) write_sample<COMPAT>(fa, p, f3(0, 0, 0), f3(0, 0, 1), f3(0, 0, 0), s.pq);
         return false;
     }
-    const XrMaterial mat = fa.sc.mats[pl.mat];
+    const XrMaterial mat = resolve_material(fa.sc, (uint32_t)pl.mat, pl.uv);
+    if (bounce == 0 && fa.sc.n_tex) fa.gb_uv[p] = pl.uv;
     if (!COMPAT) {
         float3 wo = -s.d;
         if (dot(pl.geo, wo) < 0.0f) pl.geo = -pl.geo;
@@ -625,9 +638,9 @@ __device__ __forceinline__ void write_out(const FrameArgs& fa, uint32_t p, float
     }
 }
 
-__device__ __forceinline__ float3 mat_albedo_over_pi(const FrameArgs& fa, uint32_t m) {
+__device__ __forceinline__ float3 mat_albedo_over_pi(const FrameArgs& fa, uint32_t m, uint32_t p) {
     if (m >= fa.sc.n_mats) return f3(0.0f, 0.0f, 0.0f);
-    const XrMaterial& mm = fa.sc.mats[m];
+    const XrMaterial mm = resolve_material(fa.sc, m, fa.sc.n_tex ? fa.gb_uv[p] : make_float2(0.0f, 0.0f));
     return f3(mm.base_color[0], mm.base_color[1], mm.base_color[2]) * XR_INV_PI_F;
 }
 
@@ -674,7 +687,7 @@ __global__ void __launch_bounds__(256) k_temporal_compat(FrameArgs fa, const XrU
     }
     if (!fa.temporal_on) found = false;
     Res s_new;
-    s_new.xs = xyz(xs); s_new.L = xyz(Lv); s_new.ns = xyz(ns); s_new.f = mat_albedo_over_pi(fa, mat); s_new.code = 0u;
+    s_new.xs = xyz(xs); s_new.L = xyz(Lv); s_new.ns = xyz(ns); s_new.f = mat_albedo_over_pi(fa, mat, p); s_new.code = 0u;
     const float3 x_curr = xyz(xv);
     const float3 n_curr = normalize(xyz(nv));
     Res r; res_init(r);
@@ -800,9 +813,9 @@ struct PixelShading {
     bool reuse;
 };
 __device__ __forceinline__ PixelShading pixel_shading(const FrameArgs& fa, const XrUniformBufferObject* __restrict__ u,
-                                                      float3 x, float3 n, uint32_t mat) {
+                                                      float3 x, float3 n, uint32_t mat, uint32_t p) {
     PixelShading P;
-    P.m = fa.sc.mats[mat];
+    P.m = resolve_material(fa.sc, mat, fa.sc.n_tex ? fa.gb_uv[p] : make_float2(0.0f, 0.0f));
     P.x = x;
     P.n = n;
     const float3 cam = xyz(mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));
@@ -867,7 +880,7 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     Res s_new;
     s_new.xs = xyz(a); s_new.L = xyz(b); s_new.code = bw & 0x00FFFFFFu; s_new.ns = oct_decode(s_new.code, 12);
     s_new.f = f3(0, 0, 0);
-    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat);
+    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat, p);
     bool found = false;
     Res r_prev; res_init(r_prev);
     if (fa.temporal_on && P.reuse) {
@@ -928,7 +941,7 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
             uint32_t rng = pass_rng(false, x, y, pv.W, uv->current_frame, kPassSpatial, fa.seed);
             const float3 x_view = xyz(g);
             const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
-            const PixelShading P = pixel_shading(fa, uv, x_view, n_view, mat);
+            const PixelShading P = pixel_shading(fa, uv, x_view, n_view, mat, p);
             (void)random_float(rng);   // the centre merge's draw
             for (uint32_t i = 0; i < (P.reuse ? fa.n_nb : 0u); i++) {
                 const uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng);
@@ -1047,7 +1060,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
     const float3 x_view = xyz(g);
     const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
     const uint32_t occ = fa.visibility ? fa.occ[p] : 0u;
-    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat);
+    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat, p);
     Res center; load_packed(fa.rt_cur0, fa.rt_cur1, p, center);
     Res r; res_init(r);
     res_merge(r, center, target_corrected(P, center.xs, center.L), rng);
@@ -1118,7 +1131,7 @@ __global__ void k_export_samples(FrameArgs fa, uint32_t* __restrict__ out) {
         put3(8, xyz(xs)); w[11] = __float_as_uint(xs.w);
         put3(12, xyz(ns));
         put3(16, xyz(L));
-        if (mat != kInvalid && mat < fa.sc.n_mats) put3(20, mat_albedo_over_pi(fa, mat));
+        if (mat != kInvalid && mat < fa.sc.n_mats) put3(20, mat_albedo_over_pi(fa, mat, p));
     } else {
         float4 g = fa.gb_pos_cur[p], a = fa.cand_a[p], b = fa.cand_b[p];
         uint32_t mat = fa.gb_mat_cur[p], bw = __float_as_uint(b.w);

@@ -106,6 +106,7 @@ xr_status alloc_pixels(Context* c) {
         add((void**)&fa.rs0, N * 16); add((void**)&fa.rs1, N * 16);
     }
     if (P.write_pt) { add((void**)&fa.thr0, N * 16); add((void**)&fa.out_pt, N * 16); }
+    add((void**)&fa.gb_uv, N * 8);   // written and read only when the scene has textures
     if (!compat) {
         add((void**)&fa.occ, N * 4);
         add((void**)&fa.shadow_q, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
@@ -342,6 +343,7 @@ void xr_destroy(XrContext* c) {
     cache_free(c);
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
     cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo); cudaFree(c->d_work);
+    cudaFree(c->d_vuv); cudaFree(c->d_tex_info); cudaFree(c->d_texels);
     free_lights(c);
     if (c->h_ubo) cudaFreeHost(c->h_ubo);
     for (int i = 0; i < 8; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -407,6 +409,36 @@ static xr_status upload_lights(Context* c, const std::vector<uint4>& tri, const 
     return XR_OK;
 }
 
+xr_status xr_upload_textures(XrContext* c, const XrTexture* t, uint32_t n) {
+    if (!c || (n && !t)) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload_textures: null argument");
+    size_t total = 0;
+    std::vector<uint4> info(n);
+    for (uint32_t i = 0; i < n; i++) {
+        if (!t[i].rgba8 || t[i].width == 0 || t[i].height == 0 || t[i].width > 16384 || t[i].height > 16384)
+            return fail(c, XR_ERR_INVALID_ARGUMENT, "upload_textures: each texture needs texels and a size in [1, 16384]");
+        info[i] = make_uint4((uint32_t)total, t[i].width, t[i].height, 0u);
+        total += (size_t)t[i].width * t[i].height;
+        if (total >= (1ull << 32)) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload_textures: more than 2^32 texels");
+    }
+    DeviceGuard g(c->device);
+    cudaStreamSynchronize(c->stream);
+    invalidate_graphs(c);
+    cudaFree(c->d_tex_info); cudaFree(c->d_texels);
+    c->d_tex_info = nullptr; c->d_texels = nullptr; c->n_tex = 0;
+    xr_status s;
+    if ((s = cuda_check(c, cudaMalloc((void**)&c->d_tex_info, std::max<size_t>(n, 1) * 16), "texture alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_texels, std::max<size_t>(total, 1) * 4), "texture alloc")))
+        return s;
+    if (n) cudaMemcpy(c->d_tex_info, info.data(), (size_t)n * 16, cudaMemcpyHostToDevice);
+    for (uint32_t i = 0; i < n; i++)
+        cudaMemcpy(c->d_texels + info[i].x, t[i].rgba8, (size_t)t[i].width * t[i].height * 4, cudaMemcpyHostToDevice);
+    if ((s = cuda_check(c, cudaGetLastError(), "texture upload"))) return s;
+    c->n_tex = n;
+    DeviceScene& sc = c->fa.sc;
+    sc.tex_info = c->d_tex_info; sc.texels = c->d_texels; sc.n_tex = c->n_tex;
+    return XR_OK;
+}
+
 xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const uint32_t* idx, uint32_t ni,
                           const XrMaterial* m, uint32_t nm, const XrMeshRange* ranges, uint32_t nranges) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "upload: null context");
@@ -432,33 +464,37 @@ xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const ui
     }
     bool non_lambert = false;
     for (uint32_t i = 0; i < nm; i++) {
-        if (m[i].base_color_texture_index >= 0)
-            return fail(c, XR_ERR_UNSUPPORTED, "upload: base-colour textures are not supported by this build");
+        if (m[i].base_color_texture_index >= (int32_t)c->n_tex)
+            return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: base-colour texture index out of range (upload the textures first)");
         uint32_t mm = m[i].material_model;
         if (mm != XR_MAT_LAMBERTIAN && mm != XR_MAT_DIFFUSE_LIGHT) non_lambert = true;
         if (mm > XR_MAT_PLASTIC) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: unknown material model");
     }
     std::vector<float4> pos(nv), nrm(nv);
+    std::vector<float2> uv(nv);
     for (uint32_t i = 0; i < nv; i++) {
         pos[i] = make_float4(v[i].pos[0], v[i].pos[1], v[i].pos[2], 0.0f);
         nrm[i] = make_float4(v[i].normal[0], v[i].normal[1], v[i].normal[2], 0.0f);
+        uv[i] = make_float2(v[i].tex_coord[0], v[i].tex_coord[1]);
         if (!std::isfinite(v[i].pos[0]) || !std::isfinite(v[i].pos[1]) || !std::isfinite(v[i].pos[2]))
             return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: non-finite vertex position");
     }
     cudaStreamSynchronize(c->stream);
-    cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats);
-    c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr;
+    cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats); cudaFree(c->d_vuv);
+    c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr; c->d_vuv = nullptr;
     free_lights(c);
     c->scene_ready = false; c->bvh_ready = false;
     xr_status s;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_tri_idx, std::max<size_t>(ntri, 1) * 16), "scene alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_vpos, std::max<size_t>(nv, 1) * 16), "scene alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_vnrm, std::max<size_t>(nv, 1) * 16), "scene alloc")) ||
-        (s = cuda_check(c, cudaMalloc((void**)&c->d_mats, std::max<size_t>(nm, 1) * sizeof(XrMaterial)), "scene alloc")))
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_mats, std::max<size_t>(nm, 1) * sizeof(XrMaterial)), "scene alloc")) ||
+        (s = cuda_check(c, cudaMalloc((void**)&c->d_vuv, std::max<size_t>(nv, 1) * 8), "scene alloc")))
         return s;
     if (ntri) cudaMemcpy(c->d_tri_idx, tri.data(), (size_t)ntri * 16, cudaMemcpyHostToDevice);
     if (nv) { cudaMemcpy(c->d_vpos, pos.data(), (size_t)nv * 16, cudaMemcpyHostToDevice);
-              cudaMemcpy(c->d_vnrm, nrm.data(), (size_t)nv * 16, cudaMemcpyHostToDevice); }
+              cudaMemcpy(c->d_vnrm, nrm.data(), (size_t)nv * 16, cudaMemcpyHostToDevice);
+              cudaMemcpy(c->d_vuv, uv.data(), (size_t)nv * 8, cudaMemcpyHostToDevice); }
     if (nm) cudaMemcpy(c->d_mats, m, (size_t)nm * sizeof(XrMaterial), cudaMemcpyHostToDevice);
     if ((s = upload_lights(c, tri, pos, m, nm))) return s;
     if ((s = cuda_check(c, cudaGetLastError(), "scene upload"))) return s;
@@ -488,6 +524,7 @@ xr_status xr_build_bvh(XrContext* c) {
     sc.mats = c->d_mats; sc.n_mats = c->nm; sc.ntri = c->ntri;
     sc.light_prim = c->d_light_prim; sc.light_cdf = c->d_light_cdf; sc.light_pmf = c->d_light_pmf;
     sc.prim_light_pdf = c->d_prim_light_pdf; sc.n_lights = c->n_lights;
+    sc.vuv = c->d_vuv; sc.tex_info = c->d_tex_info; sc.texels = c->d_texels; sc.n_tex = c->n_tex;
     return XR_OK;
 }
 

@@ -88,6 +88,11 @@ struct DeviceScene {
     const float* light_pmf;          // probability of light k (power / total power)
     const float* prim_light_pdf;     // per primitive: pmf / area (0: not a sampled light)
     uint32_t n_lights;
+    // base-colour textures (texture.cuh)
+    const float2* vuv;               // per vertex texture coordinate
+    const uint4* tex_info;           // per texture {first texel, width, height, 0}
+    const uint32_t* texels;          // RGBA8 texels of all textures, row 0 = v 0
+    uint32_t n_tex;
 };
 
 // One view of a multi-view context: its pixels are [pix_off, pix_off + W H) of the
@@ -124,6 +129,7 @@ struct FrameArgs {
     float4* rsw[4];           // spatial reservoirs, 2N entries per plane
     // shared
     float4* thr0;             // bounce-0 throughput (write_pt)
+    float2* gb_uv;            // texture coordinate of the visible point (read only when the scene has textures)
     float4* le0;              // directly seen emission (write_pt, compat)
     uchar4* out_ldr; float4* out_hdr; float4* out_pt;
     // wavefront
@@ -184,6 +190,10 @@ struct Context {
     uint4* d_tri_idx = nullptr;
     float4* d_vpos = nullptr;
     float4* d_vnrm = nullptr;
+    float2* d_vuv = nullptr;
+    uint4* d_tex_info = nullptr;
+    uint32_t* d_texels = nullptr;
+    uint32_t n_tex = 0;
     XrMaterial* d_mats = nullptr;
     bool scene_ready = false;
     bool scene_has_non_lambert = false;

@@ -75,6 +75,7 @@ def camera_path(scene: Scene, width: int, height: int, frames: int, bounces: int
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--scene", choices=["procedural", "cornell"], default="procedural")
+    ap.add_argument("--gltf", default=None, help="render this glTF 2.0 file (.gltf / .glb) instead")
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--frames", type=int, default=12)
@@ -83,7 +84,11 @@ def main(argv=None) -> int:
     ap.add_argument("--cache", action="store_true", help="enable the learned radiance cache")
     ap.add_argument("--png", default=None, help="write the last frame's tone-mapped image here")
     a = ap.parse_args(argv)
-    scene = Scene.procedural(**PROCEDURAL_1M) if a.scene == "procedural" else Scene.cornell()
+    if a.gltf:
+        from .gltf import load_gltf
+        scene = load_gltf(a.gltf)
+    else:
+        scene = Scene.procedural(**PROCEDURAL_1M) if a.scene == "procedural" else Scene.cornell()
     ubos = camera_path(scene, a.width, a.height, a.frames, a.bounces, not a.static)
     with Renderer(a.width, a.height) as r:
         r.set_params(params_default(a.width, a.height))
