@@ -108,25 +108,43 @@ def test_reference_mode_rejects_cache():
 
 
 def test_cache_frames_replayed_from_graphs():
-    """Training and inference inside replayed frame graphs: one Adam step per frame
-    (bias correction advanced on the device), images as with direct launches up to
-    the float-order nondeterminism of the gradient atomics."""
+    """Training and inference inside replayed frame graphs.  With a learning rate
+    of 1e-30 every update is below half an ulp of the FP32 weights (and the FP16 /
+    BF16 inference images round it away), so graph replay and direct launches must give
+    bit-identical images and records (one Adam step counted per frame either way).
+    With the default rate the float-order nondeterminism of the gradient atomics
+    makes the two trajectories drift apart, so the check is on the size of the
+    updates: bias correction advanced on the device gives the same mean weight
+    change as the host-driven path (a stuck correction would roughly double it)."""
     scene = xr.Scene.procedural(seed=3, n_objects=256, n_lights=8, extent=8.0)
     W, H = 96, 64
     ubos = camera_sequence(scene, W, H, 6, 4)
-    out = []
-    for graphs in (False, True):
+
+    def run(graphs, lr):
         with xr.Renderer(W, H) as r:
             r.set_params(xr.params_default(W, H, write_hdr=1))
             r.upload_scene(scene)
             r.build_bvh()
-            r.cache.set_params(_cache_params(1024))
+            cp = _cache_params(1024)
+            cp.learning_rate = lr
+            r.cache.set_params(cp)
             r.cache.reset(2)
+            w0 = r.cache.read(L.XR_CACHE_MLP)
             r.set_graphs(graphs)
             for u in ubos:
                 r.render(u)
             cs = r.cache.stats()
             assert cs.steps == len(ubos) and np.isfinite(cs.loss) and cs.train_samples > 0
-            out.append(r.read_output(L.XR_OUT_HDR)[:, :3].astype(np.float64))
-    d = np.abs(out[0] - out[1]).mean() / max(out[0].mean(), 1e-9)
-    assert d < 0.05, d
+            return (r.read_output(L.XR_OUT_HDR)[:, :3].copy(), r.cache.read(L.XR_CACHE_QUERIES),
+                    r.cache.read(L.XR_CACHE_MLP) - w0)
+
+    img_d, q_d, _ = run(False, 1e-30)
+    img_g, q_g, _ = run(True, 1e-30)
+    assert np.array_equal(img_d.view(np.uint32), img_g.view(np.uint32))
+    assert np.array_equal(q_d, q_g)
+
+    _, _, dw_d = run(False, 1e-2)
+    _, _, dw_g = run(True, 1e-2)
+    step_d, step_g = np.abs(dw_d).mean(), np.abs(dw_g).mean()
+    assert step_d > 1e-4
+    assert 0.9 < step_g / step_d < 1.1, (step_g, step_d)

@@ -14,7 +14,8 @@
 //      children by repeatedly opening the child of largest surface area
 //      (subtrees of more than 3 triangles first), children of <= 3 triangles
 //      become leaves, slots are assigned by octant of the child centre so that a
-//      ray visits near children first, boxes are quantised to 8 bits.
+//      ray visits near children first, boxes are quantised to 8 bits (rounded
+//      outwards, plus the slack of kBoxSlackCells).
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -27,6 +28,15 @@ namespace xr {
 namespace {
 
 constexpr uint32_t kLeafBit = 0x80000000u;
+// Slack of the quantised child boxes, per side: the larger of kBoxSlackCells of the
+// node's cell and one cell of the finest grid (2^emin >= 2^-17 of the largest
+// coordinate).  The first covers the box test's own rounding (the plane constants
+// of traversal are rounded at 32768 cells, 2^-9 of a cell, and the quantisation
+// below adds 2^-16 of a cell); the second covers the watertight triangle
+// test, whose hits can lie a few ulps of |v - o| (<= 2^-21 of the largest
+// coordinate) outside the exact triangle.  The box test also widens every far t by
+// a relative 2e-6, so a box is never rejected while it can hold a reported hit.
+constexpr float kBoxSlackCells = 1.0f / 32.0f;
 
 __device__ __forceinline__ uint32_t f2o(float f) {
     uint32_t u = __float_as_uint(f);
@@ -375,8 +385,9 @@ __global__ void k_collapse(CollapseArgs a) {
         float cl[3] = {clo[c].x, clo[c].y, clo[c].z}, ch[3] = {chi[c].x, chi[c].y, chi[c].z};
         for (int k = 0; k < 3; k++) {
             float inv = ldexpf(1.0f, -e[k]);
-            float l = floorf((cl[k] - p3[k]) * inv) - 1.0f;
-            float h = ceilf((ch[k] - p3[k]) * inv) + 1.0f;
+            const float slack = fmaxf(kBoxSlackCells, ldexpf(1.0f, a.emin - e[k]));
+            float l = floorf((cl[k] - p3[k]) * inv - slack);
+            float h = ceilf((ch[k] - p3[k]) * inv + slack);
             ql[k][s] = (uint8_t)fminf(fmaxf(l, 0.0f), 255.0f);
             qh[k][s] = (uint8_t)fminf(fmaxf(h, 0.0f), 255.0f);
         }

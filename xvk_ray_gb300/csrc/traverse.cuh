@@ -10,11 +10,13 @@
 // double-precision recomputation when an edge function is exactly zero.
 //
 // Node test: child boxes are stored quantised to 8 bits against a power-of-two
-// grid with one cell of slack on every side, and the slab test runs on
-// t = q * (2^e / d) + (p - o) / d with one fused multiply-add per plane.  The
-// slack (>= 2^-18 of the scene's largest coordinate) exceeds every rounding
-// error of that arithmetic, so a box is never rejected while it can contain a
-// hit at t <= the current closest t; traversal order only changes speed.
+// grid, rounded outwards with a slack of max(1/32 cell, 2^-17 of the scene's
+// largest coordinate) on every side, and the slab test runs on
+// t = q * (2^e / d) + (p - o) / d with one fused multiply-add per plane and a
+// relative widening of 2e-6 of the far planes.  Together they exceed every
+// rounding error of that arithmetic and of the watertight triangle test, so a box
+// is never rejected while it can contain a hit at t <= the current closest t;
+// traversal order only changes speed.
 #pragma once
 #include "device_math.cuh"
 #include "xr_internal.h"

@@ -21,7 +21,7 @@
 namespace xr {
 
 constexpr uint32_t kTriGroupBit = 0x80000000u;   // stack entry holds a triangle group
-constexpr int kPostponeBelow = 12;                // lanes; fewer testing triangles -> postpone
+constexpr int kPostponeBelow = 8;                 // lanes; fewer testing triangles -> postpone
 constexpr float kMinDir = 1e-20f;                 // smallest direction component seen by the box test
 
 struct RayIn {
@@ -34,7 +34,7 @@ struct RayIn {
 // the result is exactly 1 + q / 32768.  A plane at q cells is then
 // t = q s + a = fma(1 + q / 32768, 32768 s, a - 32768 s), one instruction per
 // plane after the per-node constants; the extra rounding of a - 32768 s is
-// below 2^-9 of a cell, far inside the one-cell slack of the stored boxes.
+// below 2^-9 of a cell, inside the 1/32-cell slack of the stored boxes.
 __device__ __forceinline__ float qplane(uint32_t word, uint32_t k) {
     return __uint_as_float(__byte_perm(word, 0x3F800000u, 0x7604u | (k << 4)));
 }
@@ -105,7 +105,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     // plane constants below is NaN, which drops that axis from every slab
                     // test and walks the whole tree.  The box test then follows a ray that
                     // departs from the true one by at most kMinDir * t, far inside the
-                    // one-cell slack of the stored boxes, so no box holding a hit is culled;
+                    // slack of the stored boxes, so no box holding a hit is culled;
                     // the triangle test uses the true direction.
                     idx = 1.0f / copysignf(fmaxf(fabsf(r.d.x), kMinDir), r.d.x);
                     idy = 1.0f / copysignf(fmaxf(fabsf(r.d.y), kMinDir), r.d.y);
