@@ -1104,11 +1104,17 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
     auto target = [&](const Sample& smp) {
         return compat ? p_hat_of(smp.L_out) : target_corrected(P, smp.x_sample, smp.L_out);
     };
-    merge_reservoir(r_s, center, target(center.s), rng);
     const uint32_t nn = compat ? 6u : (P.reuse ? R.P.n_neighbours : 0u);
     const float radius = compat ? 5.0f : R.P.radius_px;
+    // reference: one stream, each pick followed by its merge's draw; corrected:
+    // the first 2 nn draws pick the neighbours and the merges draw after them
+    uint32_t rng_pick = rng;
+    if (!compat)
+        for (uint32_t k = 0; k < 2u * nn; k++) next_random(rng);
+    uint32_t& pick = compat ? rng : rng_pick;
+    merge_reservoir(r_s, center, target(center.s), rng);
     for (uint32_t i = 0; i < nn; i++) {
-        uint32_t nb = neighbor_index(x, y, R.W, R.H, radius, rng);
+        uint32_t nb = neighbor_index(x, y, R.W, R.H, radius, pick);
         const Sample& s_nb = R.samples[nb];
         if (compat) {
             if (length(s_nb.n_view) == 0.0f || !is_similar(s_new, s_nb)) continue;

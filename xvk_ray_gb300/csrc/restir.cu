@@ -613,8 +613,7 @@ __device__ __forceinline__ void store_wide(float4* const* planes, uint32_t i, co
     planes[2][i] = f4(r.ns, __uint_as_float(r.m));
     planes[3][i] = f4(r.f, 0.0f);
 }
-__device__ __forceinline__ void load_packed(const float4* p0, const float4* p1, uint32_t i, Res& r) {
-    float4 a = p0[i], b = p1[i];
+__device__ __forceinline__ void decode_packed(float4 a, float4 b, Res& r) {
     uint32_t w = __float_as_uint(b.w);
     r.xs = xyz(a); r.W = a.w;
     r.L = xyz(b);
@@ -623,6 +622,9 @@ __device__ __forceinline__ void load_packed(const float4* p0, const float4* p1, 
     r.ns = oct_decode(r.code, 12);
     r.f = f3(0, 0, 0);
     r.w_sum = 0.0f;
+}
+__device__ __forceinline__ void load_packed(const float4* p0, const float4* p1, uint32_t i, Res& r) {
+    decode_packed(p0[i], p1[i], r);
 }
 __device__ __forceinline__ void store_packed(float4* p0, float4* p1, uint32_t i, const Res& r) {
     p0[i] = f4(r.xs, r.W);
@@ -853,6 +855,13 @@ __device__ __forceinline__ float3 shade_corrected(const PixelShading& P, const R
     return c;
 }
 
+// Neighbours of the corrected spatial pass: the first 2 n draws of the pixel's
+// spatial stream pick the n neighbours (two per pick, in order) and the merges
+// draw after them.
+__device__ __forceinline__ void rng_skip(uint32_t& st, uint32_t n) {
+    for (uint32_t k = 0; k < n; k++) st = st * 747796405u + 2891336453u;   // the state step of next_random
+}
+
 __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
@@ -880,23 +889,33 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     Res s_new;
     s_new.xs = xyz(a); s_new.L = xyz(b); s_new.code = bw & 0x00FFFFFFu; s_new.ns = oct_decode(s_new.code, 12);
     s_new.f = f3(0, 0, 0);
-    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat, p);
-    bool found = false;
-    Res r_prev; res_init(r_prev);
-    if (fa.temporal_on && P.reuse) {
+    // Reprojection first, and every previous-frame word of the reprojected pixel
+    // gathered at once (material, position, reservoir): one memory round trip
+    // instead of three dependent ones; the tests below decide what is used.
+    bool in_prev = false;
+    uint32_t pmat = kInvalid;
+    float4 pg = make_float4(0, 0, 0, 0), rp0 = pg, rp1 = pg;
+    if (fa.temporal_on) {
         float2 puv = world_to_screen_uv(x_view, u->view_prev, u->projection_prev);
         float fx = floorf(puv.x * (float)pv.W), fy = floorf(puv.y * (float)pv.H);
         if (fx >= 0.0f && fx < (float)pv.W && fy >= 0.0f && fy < (float)pv.H) {
-            uint32_t q = pv.base + (uint32_t)fy * pv.W + (uint32_t)fx;
-            if (fa.gb_mat_prev[q] == mat) {
-                float4 pg = fa.gb_pos_prev[q];
-                float3 pn = oct_decode(__float_as_uint(pg.w), 16);
-                float3 dd = x_view - xyz(pg);
-                if (!(dot(n_view, pn) < 0.8f) && !(dot(dd, dd) > 0.1f)) {
-                    load_packed(fa.rt_prev0, fa.rt_prev1, q, r_prev);
-                    found = true;
-                }
-            }
+            const uint32_t q = pv.base + (uint32_t)fy * pv.W + (uint32_t)fx;
+            pmat = fa.gb_mat_prev[q];
+            pg = fa.gb_pos_prev[q];
+            rp0 = fa.rt_prev0[q];
+            rp1 = fa.rt_prev1[q];
+            in_prev = true;
+        }
+    }
+    const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat, p);
+    bool found = false;
+    Res r_prev; res_init(r_prev);
+    if (in_prev && P.reuse && pmat == mat) {
+        float3 pn = oct_decode(__float_as_uint(pg.w), 16);
+        float3 dd = x_view - xyz(pg);
+        if (!(dot(n_view, pn) < 0.8f) && !(dot(dd, dd) > 0.1f)) {
+            decode_packed(rp0, rp1, r_prev);
+            found = true;
         }
     }
     Res r; res_init(r);
@@ -919,11 +938,12 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     if (out_here) write_out(fa, p, shade_corrected(P, r), true);
 }
 
-// Spatial reuse, step 1 of 3 (corrected mode with shadow rays): replays the
-// neighbour picks of the resolve step (same RNG stream: one draw for the centre
-// merge, two per pick, one per accepted neighbour's merge) and queues one
-// shadow ray {pixel << 5 | slot, neighbour} per neighbour whose sample would
-// get a non-zero weight.  Every pixel clears its occlusion bits.
+// Spatial reuse, step 1 of 3 (corrected mode): picks each pixel's neighbours,
+// tests their similarity, evaluates the target of each similar neighbour's
+// sample at the pixel times the Jacobian of the reconnection (p-hat) and stores
+// {neighbour, p-hat} per slot for the resolve step; with shadow rays on, queues
+// one ray {pixel << 5 | slot, neighbour} per neighbour with p-hat > 0.  Every
+// pixel clears its occlusion bits.
 __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = lane_id();
@@ -938,25 +958,27 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
         const uint32_t mat = fa.gb_mat_cur[p];
         const float4 b = fa.cand_b[p];
         if (mat != kInvalid && (__float_as_uint(b.w) >> 31) != 0u) {
-            uint32_t rng = pass_rng(false, x, y, pv.W, uv->current_frame, kPassSpatial, fa.seed);
+            uint32_t rng_pick = pass_rng(false, x, y, pv.W, uv->current_frame, kPassSpatial, fa.seed);
             const float3 x_view = xyz(g);
             const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
             const PixelShading P = pixel_shading(fa, uv, x_view, n_view, mat, p);
-            (void)random_float(rng);   // the centre merge's draw
-            for (uint32_t i = 0; i < (P.reuse ? fa.n_nb : 0u); i++) {
-                const uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng);
+            const uint32_t nn = P.reuse ? fa.n_nb : 0u;
+            for (uint32_t i = 0; i < nn; i++) {
+                uint2 slot = make_uint2(kInvalid, 0u);
+                const uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng_pick);
                 const uint32_t nmat = fa.gb_mat_cur[nbi];
-                if (nmat == kInvalid) continue;
-                const float4 ng = fa.gb_pos_cur[nbi];
-                const float3 dd = x_view - xyz(ng);
-                if (dot(dd, dd) > 0.1f) continue;
-                if (dot(n_view, oct_decode(__float_as_uint(ng.w), 16)) < 0.8f) continue;
-                if (mat != nmat) continue;
-                Res rn;
-                load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
-                const float ph = target_corrected(P, rn.xs, rn.L) * jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
-                (void)random_float(rng);   // the merge's draw
-                if (ph > 0.0f) { emit_mask |= 1u << i; nb_of[i] = nbi; }
+                if (nmat != kInvalid && nmat == mat) {
+                    const float4 ng = fa.gb_pos_cur[nbi];
+                    const float3 dd = x_view - xyz(ng);
+                    if (!(dot(dd, dd) > 0.1f) && !(dot(n_view, oct_decode(__float_as_uint(ng.w), 16)) < 0.8f)) {
+                        Res rn;
+                        load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
+                        const float ph = target_corrected(P, rn.xs, rn.L) * jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
+                        slot = make_uint2(nbi, __float_as_uint(ph));
+                        if (fa.visibility && ph > 0.0f) { emit_mask |= 1u << i; nb_of[i] = nbi; }
+                    }
+                }
+                fa.nb_slot[(size_t)i * fa.N + p] = slot;
             }
         }
     }
@@ -1039,7 +1061,8 @@ __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_nee(Frame
 }
 
 // Spatial reuse, step 3 of 3: the merge of ReSTIRGISpatialReuse.rgen.hlsl:91-176
-// with the visibility of step 2, M cap, W, shading and tone mapping.
+// over the similar neighbours and p-hat values of step 1, with the visibility of
+// step 2, M cap, W, shading and tone mapping.
 __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
@@ -1062,20 +1085,16 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
     const uint32_t occ = fa.visibility ? fa.occ[p] : 0u;
     const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat, p);
     Res center; load_packed(fa.rt_cur0, fa.rt_cur1, p, center);
+    const uint32_t nn = P.reuse ? fa.n_nb : 0u;   // the neighbours k_spatial_select picked and tested
+    rng_skip(rng, 2u * nn);                         // the merges draw after the picks
     Res r; res_init(r);
     res_merge(r, center, target_corrected(P, center.xs, center.L), rng);
-    for (uint32_t i = 0; i < (P.reuse ? fa.n_nb : 0u); i++) {
-        uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng);
-        uint32_t nmat = fa.gb_mat_cur[nbi];
-        if (nmat == kInvalid) continue;
-        float4 ng = fa.gb_pos_cur[nbi];
-        float3 dd = x_view - xyz(ng);
-        if (dot(dd, dd) > 0.1f) continue;
-        if (dot(n_view, oct_decode(__float_as_uint(ng.w), 16)) < 0.8f) continue;
-        if (mat != nmat) continue;
-        Res rn; load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
-        float jac = jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
-        float ph = target_corrected(P, rn.xs, rn.L) * jac;
+    for (uint32_t i = 0; i < nn; i++) {
+        const uint2 slot = fa.nb_slot[(size_t)i * fa.N + p];
+        if (slot.x == kInvalid) continue;   // not similar: no merge, no draw
+        Res rn;
+        load_packed(fa.rt_cur0, fa.rt_cur1, slot.x, rn);
+        float ph = __uint_as_float(slot.y);
         const bool occluded = ph > 0.0f && ((occ >> i) & 1u);
         if (occluded) ph = 0.0f;
         res_merge(r, rn, ph, rng);
@@ -1312,10 +1331,8 @@ void launch_spatial(const FrameArgs& fa, cudaStream_t st) {
         k_spatial_compat<<<blocks, 256, 0, st>>>(fa, fa.ubo);
         return;
     }
-    if (fa.visibility) {
-        k_spatial_select<<<blocks, 256, 0, st>>>(fa, fa.ubo);
-        k_trace_shadow<<<fa.grid_trace, kBlock, 0, st>>>(fa);
-    }
+    k_spatial_select<<<blocks, 256, 0, st>>>(fa, fa.ubo);
+    if (fa.visibility) k_trace_shadow<<<fa.grid_trace, kBlock, 0, st>>>(fa);
     k_spatial_resolve<<<blocks, 256, 0, st>>>(fa, fa.ubo);
 }
 

@@ -110,6 +110,7 @@ xr_status alloc_pixels(Context* c) {
     if (!compat) {
         add((void**)&fa.occ, N * 4);
         add((void**)&fa.shadow_q, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
+        add((void**)&fa.nb_slot, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
     }
     add((void**)&fa.hits, N * 16);
     add((void**)&fa.out_ldr, N * 4);

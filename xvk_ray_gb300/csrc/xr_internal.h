@@ -137,6 +137,8 @@ struct FrameArgs {
     uint4* hits;              // closest-hit record per queue slot {prim, t, b1, b2}
     uint2* shadow_q;          // corrected spatial pass: {pixel << 5 | slot, neighbour pixel}
     uint32_t* occ;            // per pixel: occluded neighbour slots
+    uint2* nb_slot;           // corrected spatial pass, plane per slot: {neighbour pixel, target * Jacobian}
+                              // of a similar neighbour, {kInvalid, 0} otherwise
     uint32_t* counters;       // [b] paths entering bounce b, then the kCnt* words above
     uint32_t grid_persistent, grid_trace;
     // learned radiance cache (corrected mode): paths end at x_s unless selected for training
