@@ -326,6 +326,7 @@ def run_ours(args):
     r.set_params(xr.params_default(W, H))
     r.upload_scene(scene)
     r.build_bvh()
+    r.set_graphs(True)   # each frame's launches replayed from a CUDA graph (one per frame parity)
     st = r.stats()
     bvh = {"nodes": st.bvh_nodes, "triangles": st.bvh_triangles, "depth": st.bvh_depth,
            "build_ms": round(st.ms_bvh_build, 2)}
@@ -395,7 +396,7 @@ def run_ours(args):
         "config": {"workload": workload(args.steps),
                    "resolution": [W, H], "triangles": scene.n_triangles, "bounces": BOUNCES,
                    "l2": "per-frame working set 0.66 GB > 129 MB L2 (no flush needed); BVH stays L2-resident",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}", "launch": "frame graphs (xr_set_graphs)"},
         "passes_ms": {"initial_sample": round(ms_init, 4), "temporal": round(ms_temp, 4), "spatial": round(ms_spat, 4)},
         "rays_per_frame": rays_pf, "shadow_rays_per_frame": shadow_pf,
         "rays_per_s": (rays_pf + shadow_pf) / ((ms_init + ms_spat) * 1e-3),

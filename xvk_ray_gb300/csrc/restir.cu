@@ -963,12 +963,25 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
             const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
             const PixelShading P = pixel_shading(fa, uv, x_view, n_view, mat, p);
             const uint32_t nn = P.reuse ? fa.n_nb : 0u;
+            // the picks do not depend on the merges: the next neighbour's G-buffer
+            // words are gathered while this one is tested and evaluated
+            uint32_t nx_i = 0u, nx_mat = kInvalid;
+            float4 nx_g = make_float4(0, 0, 0, 0);
+            if (nn) {
+                nx_i = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng_pick);
+                nx_mat = fa.gb_mat_cur[nx_i];
+                nx_g = fa.gb_pos_cur[nx_i];
+            }
             for (uint32_t i = 0; i < nn; i++) {
                 uint2 slot = make_uint2(kInvalid, 0u);
-                const uint32_t nbi = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng_pick);
-                const uint32_t nmat = fa.gb_mat_cur[nbi];
+                const uint32_t nbi = nx_i, nmat = nx_mat;
+                const float4 ng = nx_g;
+                if (i + 1u < nn) {
+                    nx_i = pv.base + neighbor_index(x, y, pv.W, pv.H, fa.radius, rng_pick);
+                    nx_mat = fa.gb_mat_cur[nx_i];
+                    nx_g = fa.gb_pos_cur[nx_i];
+                }
                 if (nmat != kInvalid && nmat == mat) {
-                    const float4 ng = fa.gb_pos_cur[nbi];
                     const float3 dd = x_view - xyz(ng);
                     if (!(dot(dd, dd) > 0.1f) && !(dot(n_view, oct_decode(__float_as_uint(ng.w), 16)) < 0.8f)) {
                         Res rn;
