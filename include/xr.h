@@ -129,6 +129,10 @@ typedef struct XrStats {
     uint64_t query_node_visits;  /* BVH nodes visited by those rays */
     uint64_t query_tri_tests;    /* triangle tests of those rays */
     uint64_t nonfinite_rays;     /* rays of the last frame ended as misses for a non-finite origin/direction */
+    uint32_t instances;          /* instances of xr_set_instances (0: none) */
+    uint32_t tlas_nodes;         /* nodes of the top-level BVH */
+    float ms_tlas_build;         /* last top-level BVH build */
+    float ms_refit;              /* last xr_update_vertices refit */
 } XrStats;
 enum { XR_DEVFLAG_STACK_OVERFLOW = 1u, XR_DEVFLAG_QUEUE_OVERFLOW = 2u, XR_DEVFLAG_BAD_INDEX = 4u,
        XR_DEVFLAG_MMA_TIMEOUT = 8u /* a tensor-core completion wait of the radiance cache gave up (1 s) */ };
@@ -318,6 +322,40 @@ typedef struct XrTuning {
 xr_status xr_autotune(XrContext* ctx, const XrUniformBufferObject* ubos, uint32_t frames, XrTuning* out);
 /* Applies a launch configuration (e.g. one xr_autotune chose earlier); 0 = occupancy maximum. */
 xr_status xr_set_tuning(XrContext* ctx, const XrTuning* tuning);
+
+/* ---- instances, dynamic top-level BVH and refit ----
+   Replaces the reference's top-level acceleration structure over one identity
+   instance per model (ApplicationRT.cpp:226-258, XVKTLAccelerationStructure.cpp:88)
+   and the ObjectToWorld / WorldToObject mapping of its closest-hit shader
+   (Ray.rchit.hlsl:46-55).  The scenes of xr_upload_scenes (or the one of
+   xr_upload_scene + xr_build_bvh) are the bottom-level BVHs; instances place
+   transformed copies of them.  A top-level 8-wide BVH over the instances' world
+   boxes is built on the device; a ray enters an instance's BVH in its object
+   space (origin and direction mapped by world-to-object, t stays the world
+   ray's) and its hit is mapped back: position by object-to-world, shading and
+   geometric normals by the inverse transpose.  Closest hit: smallest t, then the
+   lowest instance, then the lowest primitive.  With instances set, every view
+   renders the instanced world; the learned cache is not available. */
+typedef struct XrInstance {
+    uint32_t scene;                  /* bottom-level BVH: index into the uploaded scenes */
+    uint32_t reserved;               /* 0 */
+    float object_to_world[12];       /* row-major 3 x 4: world = M (x, y, z, 1) */
+} XrInstance;                        /* 56 bytes */
+/* Replaces the instance list (n = 0: back to the scenes without instances) and
+   rebuilds the top-level BVH; call again whenever transforms change (e.g. each frame). */
+xr_status xr_set_instances(XrContext* ctx, const XrInstance* instances, uint32_t n);
+/* 24 floats per instance: object-to-world, then world-to-object (its inverse, computed
+   in double precision and rounded to float), row-major 3 x 4, as traversal uses them. */
+xr_status xr_get_instance_transforms(XrContext* ctx, float* out, uint32_t n);
+/* No counterpart in the reference (its geometry is static).  New vertices of scene
+   `scene` (same count, indices and materials as uploaded), then a refit of its BVH
+   on the device: triangle slots take the new positions, node boxes are recomputed
+   level by level from the deepest and requantised, the topology is kept; with
+   instances set, the top-level BVH is rebuilt over the new bounds. */
+xr_status xr_update_vertices(XrContext* ctx, uint32_t scene, const XrVertex* vertices, uint32_t count);
+/* xr_trace_rays that also reports each hit's instance (-1 on a miss or without instances). */
+xr_status xr_trace_rays_instanced(XrContext* ctx, const float* rays, uint32_t n, int32_t any_hit, int32_t* prim,
+                                  int32_t* instance, float* t, float* bary);
 
 /* ---- learned radiance cache ----
    No counterpart in the reference renderer (it has no learned component): the

@@ -35,6 +35,11 @@ def load():
             "or_scene_destroy": (None, [P]),
             "or_scene_set_textures": (None, [P, P, u32, P]),
             "or_trace": (None, [P, P, u32, C.c_int, P, P, P]),
+            "or_world_create": (P, [P, u32]),
+            "or_world_set_instances": (C.c_int, [P, P, P, u32]),
+            "or_world_transforms": (None, [P, P]),
+            "or_world_update_vertices": (C.c_int, [P, u32, P, u32]),
+            "or_trace_inst": (None, [P, P, u32, C.c_int, P, P, P, P]),
             "or_renderer_create": (P, [P, P]),
             "or_renderer_destroy": (None, [P]),
             "or_renderer_set_cache": (C.c_int, [P, C.c_int, u32, P]),
@@ -131,6 +136,47 @@ class OracleScene:
             self.close()
         except Exception:
             pass
+
+
+class OracleWorld(OracleScene):
+    """Scenes concatenated as xr_upload_scenes does, traced and rendered through
+    instances (or_world_*); usable wherever an OracleScene is."""
+
+    def __init__(self, scenes: "list[OracleScene]"):
+        self._parts = list(scenes)   # keep the sources alive while copying
+        arr = (C.c_void_p * len(scenes))(*[sc.h for sc in scenes])
+        self.h = load().or_world_create(C.cast(arr, C.c_void_p), len(scenes))
+        self._n_inst = 0
+
+    def set_instances(self, instances) -> None:
+        """instances: (scene index, 3x4 object-to-world) pairs."""
+        n = len(instances)
+        part = np.array([int(k) for k, _ in instances], np.uint32)
+        m = np.array([np.asarray(x, np.float32).reshape(12) for _, x in instances], np.float32).reshape(n, 12)
+        if load().or_world_set_instances(self.h, _p(part), _p(m), n) != 0:
+            raise ValueError("bad instance list (unknown scene or singular transform)")
+        self._n_inst = n
+
+    def transforms(self) -> np.ndarray:
+        out = np.empty((self._n_inst, 24), np.float32)
+        if self._n_inst:
+            load().or_world_transforms(self.h, _p(out))
+        return out.reshape(self._n_inst, 2, 3, 4)
+
+    def update_vertices(self, part: int, vertices: np.ndarray) -> None:
+        v = np.ascontiguousarray(vertices, np.float32)
+        if load().or_world_update_vertices(self.h, part, _p(v), v.shape[0]) != 0:
+            raise ValueError("bad vertex update")
+
+    def trace_instanced(self, rays: np.ndarray, any_hit: bool = False):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        inst = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        bary = np.empty((n, 2), np.float32)
+        load().or_trace_inst(self.h, _p(rays), n, 1 if any_hit else 0, _p(prim), _p(inst), _p(t), _p(bary))
+        return prim, inst, t, bary
 
 
 def _bytes_of(struct) -> C.c_void_p:

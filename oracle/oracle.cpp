@@ -136,6 +136,14 @@ struct Scene {
     // emissive triangles (next-event estimation of the radiance cache's training paths)
     std::vector<uint32_t> light_prim;
     std::vector<float> light_cdf, light_pmf, prim_light_pdf;
+    // A world of instanced scenes (or_world_*): the arrays above hold the scenes
+    // concatenated (indices and material indices relocated, as xr_upload_scenes
+    // does); parts are the scenes themselves (local primitive ids, own BVHs),
+    // part_prim0 the first primitive of each in the concatenation.
+    struct Inst { uint32_t part; float o2w[12], w2o[12]; };
+    std::vector<Scene> parts;
+    std::vector<uint32_t> part_prim0;
+    std::vector<Inst> inst;
 };
 
 // Light-sampling tables: power = area * luminance(4 * base colour) per
@@ -274,10 +282,53 @@ inline bool box_test(const BNode& n, const double o[3], const double d[3], doubl
     return t0 <= t1 * (1.0 + 1e-7) + 1e-12;
 }
 
-struct Hit { int32_t prim; float t, b1, b2; };
+struct Hit { int32_t prim; float t, b1, b2; int32_t inst = -1; };
+
+// 3 x 4 row-major transforms, one product at a time in the order written
+// (instances.cu / traverse.cuh evaluate the same expressions).
+inline f3 xform_point(const float* m, f3 p) {
+    return f3{((m[0] * p.x + m[1] * p.y) + m[2] * p.z) + m[3], ((m[4] * p.x + m[5] * p.y) + m[6] * p.z) + m[7],
+              ((m[8] * p.x + m[9] * p.y) + m[10] * p.z) + m[11]};
+}
+inline f3 xform_dir(const float* m, f3 d) {
+    return f3{(m[0] * d.x + m[1] * d.y) + m[2] * d.z, (m[4] * d.x + m[5] * d.y) + m[6] * d.z,
+              (m[8] * d.x + m[9] * d.y) + m[10] * d.z};
+}
+// transpose of the linear part of m (the rows of world-to-object): normals
+inline f3 xform_normal(const float* m, f3 v) {
+    return f3{(m[0] * v.x + m[4] * v.y) + m[8] * v.z, (m[1] * v.x + m[5] * v.y) + m[9] * v.z,
+              (m[2] * v.x + m[6] * v.y) + m[10] * v.z};
+}
+
+Hit trace(const Scene& s, f3 o, f3 d, float tmin, float tmax, bool any_hit);
+
+// Closest hit over instances: each instance's scene is traced with the ray in
+// its object space (t is the world ray's); smallest t wins, then the lowest
+// instance (visited first here), then the lowest primitive (within the scene).
+Hit trace_instanced(const Scene& s, f3 o, f3 d, float tmin, float tmax, bool any_hit) {
+    Hit best{-1, tmax, 0.0f, 0.0f};
+    for (uint32_t i = 0; i < (uint32_t)s.inst.size(); i++) {
+        const Scene::Inst& I = s.inst[i];
+        const Scene& P = s.parts[I.part];
+        if (P.ntri == 0) continue;
+        const f3 oo = xform_point(I.w2o, o), od = xform_dir(I.w2o, d);
+        const float chk = oo.x + oo.y + oo.z + od.x + od.y + od.z;
+        if (!std::isfinite(chk) || (od.x == 0.0f && od.y == 0.0f && od.z == 0.0f)) continue;
+        Hit h = trace(P, oo, od, tmin, best.t, any_hit);
+        if (h.prim < 0) continue;
+        if (best.prim < 0 || h.t < best.t) {
+            best = h;
+            best.prim = (int32_t)(s.part_prim0[I.part] + (uint32_t)h.prim);
+            best.inst = (int32_t)i;
+            if (any_hit) return best;
+        }
+    }
+    return best;
+}
 
 // Closest hit (ties: lowest primitive id) or, with any_hit, the first hit found.
 Hit trace(const Scene& s, f3 o, f3 d, float tmin, float tmax, bool any_hit) {
+    if (!s.inst.empty()) return trace_instanced(s, o, d, tmin, tmax, any_hit);
     Hit h{-1, tmax, 0.0f, 0.0f};
     RayPre r = prep_ray(o, d);
     auto test = [&](uint32_t t) -> bool {
@@ -333,7 +384,15 @@ Payload closest_hit(const Scene& s, const Hit& h) {
     f3 v0 = vert_pos(s, i0), v1 = vert_pos(s, i1), v2 = vert_pos(s, i2);
     f3 pos = v0 * bx + v1 * by + v2 * bz;
     f3 e0 = v2 - v0, e1 = v1 - v0;
-    pl.geo_normal = normalize(cross(e0, e1));
+    f3 geo = cross(e0, e1);
+    if (h.inst >= 0 && !s.inst.empty()) {
+        // Ray.rchit.hlsl:46-55: position by object-to-world, normals by its inverse transpose
+        const Scene::Inst& I = s.inst[h.inst];
+        pos = xform_point(I.o2w, pos);
+        normal = xform_normal(I.w2o, normal);
+        geo = xform_normal(I.w2o, geo);
+    }
+    pl.geo_normal = normalize(geo);
     pl.pos = pos;
     pl.normal = normalize(normal);
     pl.uv = uv;
@@ -1223,6 +1282,112 @@ void* or_scene_create(const float* vertices, uint32_t nv, const uint32_t* indice
 }
 void or_scene_destroy(void* scene) { delete (Scene*)scene; }
 
+// Inverse of a 3 x 4 affine map: adjugate over determinant in double precision,
+// rounded to float (the expressions and order of instances.cu).
+static bool invert_affine(const float m[12], float out[12]) {
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+    const double A = e * i - f * h, B = f * g - d * i, C = d * h - e * g;
+    const double det = a * A + b * B + c * C;
+    if (!std::isfinite(det) || det == 0.0) return false;
+    const double r = 1.0 / det;
+    const double inv[9] = {A * r, (c * h - b * i) * r, (b * f - c * e) * r,
+                           B * r, (a * i - c * g) * r, (c * d - a * f) * r,
+                           C * r, (b * g - a * h) * r, (a * e - b * d) * r};
+    const double tx = m[3], ty = m[7], tz = m[11];
+    for (int k = 0; k < 3; k++) {
+        out[4 * k + 0] = (float)inv[3 * k + 0];
+        out[4 * k + 1] = (float)inv[3 * k + 1];
+        out[4 * k + 2] = (float)inv[3 * k + 2];
+        out[4 * k + 3] = (float)(-((inv[3 * k + 0] * tx + inv[3 * k + 1] * ty) + inv[3 * k + 2] * tz));
+    }
+    for (int k = 0; k < 12; k++)
+        if (!std::isfinite(out[k])) return false;
+    return true;
+}
+
+static void world_concat(Scene& w) {
+    w.vert.clear(); w.idx.clear(); w.mat.clear(); w.part_prim0.clear();
+    uint32_t vo = 0, mo = 0, po = 0;
+    for (const Scene& p : w.parts) {
+        w.part_prim0.push_back(po);
+        for (uint32_t v = 0; v < p.nv; v++) {
+            const float* src = &p.vert[(size_t)v * 9];
+            float q[9];
+            memcpy(q, src, sizeof(q));
+            int32_t mi;
+            memcpy(&mi, &q[8], 4);
+            if (mi >= 0) mi += (int32_t)mo;
+            memcpy(&q[8], &mi, 4);
+            w.vert.insert(w.vert.end(), q, q + 9);
+        }
+        for (uint32_t k = 0; k < p.ntri * 3; k++) w.idx.push_back(p.idx[k] + vo);
+        w.mat.insert(w.mat.end(), p.mat.begin(), p.mat.end());
+        vo += p.nv; mo += p.nm; po += p.ntri;
+    }
+    w.nv = vo; w.nm = mo; w.ntri = po;
+    // without instances the world is traced as one scene (brute force)
+    w.p0.resize(po); w.p1.resize(po); w.p2.resize(po);
+    for (uint32_t t = 0; t < po; t++) {
+        w.p0[t] = vert_pos(w, w.idx[3 * (size_t)t]);
+        w.p1[t] = vert_pos(w, w.idx[3 * (size_t)t + 1]);
+        w.p2[t] = vert_pos(w, w.idx[3 * (size_t)t + 2]);
+    }
+}
+
+// A world of n scenes (copied), concatenated as xr_upload_scenes does; trace and
+// render it after or_world_set_instances.
+void* or_world_create(void* const* scenes, uint32_t n) {
+    Scene* w = new Scene();
+    for (uint32_t k = 0; k < n; k++) {
+        w->parts.push_back(*(const Scene*)scenes[k]);
+        w->parts.back().tex_info.clear();
+        w->parts.back().texels.clear();
+    }
+    world_concat(*w);
+    w->brute = true;
+    return w;
+}
+
+// Instances: n x {part, 3 x 4 object-to-world}.  Returns 0, or -1 for a bad part
+// or a singular transform.
+int or_world_set_instances(void* world, const uint32_t* part, const float* o2w12, uint32_t n) {
+    Scene& w = *(Scene*)world;
+    std::vector<Scene::Inst> v(n);
+    for (uint32_t i = 0; i < n; i++) {
+        if (part[i] >= w.parts.size()) return -1;
+        v[i].part = part[i];
+        memcpy(v[i].o2w, o2w12 + 12 * (size_t)i, 48);
+        if (!invert_affine(v[i].o2w, v[i].w2o)) return -1;
+    }
+    w.inst = v;
+    return 0;
+}
+
+// 24 floats per instance: object-to-world, world-to-object.
+void or_world_transforms(void* world, float* out24) {
+    const Scene& w = *(const Scene*)world;
+    for (size_t i = 0; i < w.inst.size(); i++) {
+        memcpy(out24 + 24 * i, w.inst[i].o2w, 48);
+        memcpy(out24 + 24 * i + 12, w.inst[i].w2o, 48);
+    }
+}
+
+// New vertices of one part (same count); its BVH is rebuilt from scratch.
+int or_world_update_vertices(void* world, uint32_t part, const float* vertices9, uint32_t nv) {
+    Scene& w = *(Scene*)world;
+    if (part >= w.parts.size() || w.parts[part].nv != nv) return -1;
+    Scene& p = w.parts[part];
+    p.vert.assign(vertices9, vertices9 + (size_t)nv * 9);
+    for (uint32_t t = 0; t < p.ntri; t++) {
+        p.p0[t] = vert_pos(p, p.idx[3 * (size_t)t]);
+        p.p1[t] = vert_pos(p, p.idx[3 * (size_t)t + 1]);
+        p.p2[t] = vert_pos(p, p.idx[3 * (size_t)t + 2]);
+    }
+    if (!p.brute) build_bvh(p);
+    world_concat(w);
+    return 0;
+}
+
 // Base-colour textures (n; sizes as width, height pairs; texels RGBA8 concatenated,
 // row 0 = v 0) -- the layout of xr_upload_textures.
 void or_scene_set_textures(void* scene, const uint32_t* sizes2, uint32_t n, const uint8_t* rgba8) {
@@ -1249,6 +1414,21 @@ void or_trace(void* scene, const float* rays, uint32_t n, int any_hit, int32_t* 
         const float* r = rays + 8 * i;
         Hit h = trace(s, f3{r[0], r[1], r[2]}, f3{r[4], r[5], r[6]}, r[3], r[7], any_hit != 0);
         prim[i] = h.prim;
+        t[i] = h.prim >= 0 ? h.t : -1.0f;
+        bary[2 * i] = h.b1;
+        bary[2 * i + 1] = h.b2;
+    }
+}
+
+void or_trace_inst(void* scene, const float* rays, uint32_t n, int any_hit, int32_t* prim, int32_t* inst, float* t,
+                   float* bary) {
+    const Scene& s = *(const Scene*)scene;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        const float* r = rays + 8 * i;
+        Hit h = trace(s, f3{r[0], r[1], r[2]}, f3{r[4], r[5], r[6]}, r[3], r[7], any_hit != 0);
+        prim[i] = h.prim;
+        inst[i] = h.prim >= 0 ? h.inst : -1;
         t[i] = h.prim >= 0 ? h.t : -1.0f;
         bary[2 * i] = h.b1;
         bary[2 * i + 1] = h.b2;

@@ -90,6 +90,17 @@ void or_scene_set_textures(void* scene, const uint32_t* sizes2, uint32_t n, cons
 void or_trace(void* scene, const float* rays, uint32_t n, int any_hit,
               int32_t* prim, float* t, float* bary);
 
+/* ---- instances (instances.cu; Ray.rchit.hlsl:46-55) ----
+   A world of n scenes (copied), concatenated as xr_upload_scenes does, traced and
+   rendered through its instances: each scene traced with the ray in the instance's
+   object space; closest hit by t, then instance, then primitive.  Returns 0 / -1. */
+void* or_world_create(void* const* scenes, uint32_t n);
+int or_world_set_instances(void* world, const uint32_t* part, const float* o2w12, uint32_t n);
+void or_world_transforms(void* world, float* out24);
+int or_world_update_vertices(void* world, uint32_t part, const float* vertices9, uint32_t nv);
+void or_trace_inst(void* scene, const float* rays, uint32_t n, int any_hit, int32_t* prim, int32_t* inst,
+                   float* t, float* bary);
+
 /* ---- the frame pipeline ---- */
 void* or_renderer_create(void* scene, const OrParams* params);
 void or_renderer_destroy(void* r);

@@ -46,3 +46,94 @@ def camera_sequence(scene, w, h, frames, bounces, move=None, sky=False, reuse=Tr
 def diff_words(a: np.ndarray, b: np.ndarray, cols: slice) -> int:
     """Number of rows whose words in `cols` differ bit-wise."""
     return int(np.sum(np.any(a[:, cols] != b[:, cols], axis=1)))
+
+
+def box_scene(rng: np.random.Generator, n_boxes: int, extent: float, step: float = 1.0 / 16.0,
+              light: bool = True) -> "xr.Scene":
+    """Axis-aligned boxes (and an emissive quad above them) whose coordinates are
+    multiples of `step`: translating the scene by multiples of `step` is exact in
+    float, so instanced and baked copies trace bit-identically."""
+    verts, idx, mats = [], [], []
+    mats.append([0.7, 0.6, 0.5, 1.0, 0.0, 0.0, 0.0, 0.0])     # Lambertian
+    mats.append([0.3, 0.5, 0.8, 1.0, 0.0, 0.4, 0.0, 0.0])     # Lambertian, other colour
+    # corner k has x = hi if bit 0 is set, y if bit 1, z if bit 2
+    faces = [((0, 2, 6, 4), (-1, 0, 0)), ((1, 3, 7, 5), (1, 0, 0)), ((0, 1, 5, 4), (0, -1, 0)),
+             ((2, 6, 7, 3), (0, 1, 0)), ((0, 1, 3, 2), (0, 0, -1)), ((4, 6, 7, 5), (0, 0, 1))]
+
+    def q(v):
+        return np.round(np.asarray(v, np.float64) / step) * step
+
+    def add_quad(p4, n, m):
+        base = len(verts)
+        for p in p4:
+            verts.append([p[0], p[1], p[2], n[0], n[1], n[2], 0.0, 0.0, 0.0])
+            verts[-1][8] = np.array([m], np.int32).view(np.float32)[0]
+        idx.extend([base, base + 1, base + 2, base, base + 2, base + 3])
+
+    for b in range(n_boxes):
+        c = q(rng.uniform(-extent, extent, 3))
+        h = q(rng.uniform(0.25, 1.0, 3) * extent / 4.0) + step
+        lo, hi = c - h, c + h
+        corners = [[(hi if (k >> a) & 1 else lo)[a] for a in range(3)] for k in range(8)]
+        for f, n in faces:
+            add_quad([corners[i] for i in f], n, b % 2)
+    if light:
+        mats.append([4.0, 4.0, 4.0, 1.0, 0.0, 0.0, 0.0, 0.0])
+        mats[-1][7] = np.array([3], np.uint32).view(np.float32)[0]   # DiffuseLight
+        y = extent * 1.5
+        s = q(extent / 3.0)
+        add_quad([[-s, y, -s], [-s, y, s], [s, y, s], [s, y, -s]], (0, -1, 0), len(mats) - 1)
+    m = np.array(mats, np.float32)
+    m[:, 4] = np.array([-1] * m.shape[0], np.int32).view(np.float32)   # no base-colour texture
+    v = np.array(verts, np.float32)
+    cam = xr._lib.XrCamera()
+    cam.position[:] = [0.0, 0.0, extent * 3.0]
+    cam.yaw_deg, cam.pitch_deg, cam.fov_deg = 0.0, 0.0, 60.0
+    return xr.Scene(v, np.array(idx, np.uint32), m, np.zeros((1, 2), np.uint32), cam)
+
+
+def rotation(axis, deg: float) -> np.ndarray:
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    t = np.radians(deg)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(t) * K + (1 - np.cos(t)) * K @ K
+
+
+def affine(R, t) -> np.ndarray:
+    """3x4 object-to-world matrix [R | t] (float32 values)."""
+    m = np.zeros((3, 4), np.float64)
+    m[:, :3] = R
+    m[:, 3] = t
+    return m.astype(np.float32)
+
+
+def bake_instances(scenes, instances) -> "tuple[xr.Scene, np.ndarray, np.ndarray]":
+    """One flat scene holding every instance's triangles in world space (float64
+    transform, rounded to float).  Also returns, per baked primitive, its instance
+    and its primitive in the concatenation of `scenes`."""
+    verts, idx, mats, inst_of, prim_of = [], [], [], [], []
+    prim0 = np.cumsum([0] + [s.n_triangles for s in scenes])
+    mat0 = np.cumsum([0] + [s.materials.shape[0] for s in scenes])
+    for s in scenes:
+        mats.append(s.materials)
+    nv = 0
+    for i, (k, m) in enumerate(instances):
+        s = scenes[k]
+        m = np.asarray(m, np.float64).reshape(3, 4)
+        v = s.vertices.copy()
+        p = s.vertices[:, 0:3].astype(np.float64)
+        v[:, 0:3] = (p @ m[:, :3].T + m[:, 3]).astype(np.float32)
+        n = s.vertices[:, 3:6].astype(np.float64) @ np.linalg.inv(m[:, :3])
+        v[:, 3:6] = (n / np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-30)).astype(np.float32)
+        mi = s.vertices[:, 8].view(np.int32).copy()
+        mi[mi >= 0] += int(mat0[k])
+        v[:, 8] = mi.view(np.float32)
+        verts.append(v)
+        idx.append(s.global_indices() + nv)
+        nv += v.shape[0]
+        inst_of.append(np.full(s.n_triangles, i, np.int32))
+        prim_of.append(np.arange(s.n_triangles, dtype=np.int32) + int(prim0[k]))
+    sc = xr.Scene(np.concatenate(verts), np.concatenate(idx).astype(np.uint32), np.concatenate(mats),
+                  np.zeros((1, 2), np.uint32), scenes[0].camera)
+    return sc, np.concatenate(inst_of), np.concatenate(prim_of)

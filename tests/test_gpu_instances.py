@@ -1,0 +1,145 @@
+"""Instances, the top-level BVH and refit on the GPU against the oracle: hits of
+the two-level traversal bit-exact (primitive, instance, t, barycentrics), frames
+of instanced worlds bit-exact (moving instances included), identity instances
+rendering exactly like the scene itself, and refitted BVHs tracing exactly like
+the oracle on the moved vertices."""
+import numpy as np
+import pytest
+
+import xvk_ray_gb300 as xr
+from oracle import binding as ob
+from tests.helpers import affine, box_scene, camera_sequence, random_rays, rotation
+from tests.test_gpu_frames import _compare_frame
+
+pytestmark = pytest.mark.gpu
+
+XR = xr._lib
+
+
+def _instances(t=0.0):
+    return [(0, affine(np.eye(3), [0, 0, 0])),
+            (1, affine(rotation([0, 1, 0], 30 + 40 * t) * 1.5, [2.0, -1.0 + t, 0.5])),
+            (0, affine(rotation([1, 1, 0], -75) @ np.diag([0.5, 2.0, 1.0]), [-3.0, 0.25, 4.0 - 2 * t])),
+            (1, affine(rotation([0, 0, 1], 10), [0.0, 3.0, -5.0]))]
+
+
+def _scenes(seed=7):
+    rng = np.random.default_rng(seed)
+    return box_scene(rng, 24, 3.0), box_scene(rng, 12, 2.0, light=False)
+
+
+def _world(scenes, inst):
+    w = ob.OracleWorld([ob.OracleScene.from_scene(s) for s in scenes])
+    w.set_instances(inst)
+    return w
+
+
+def test_instanced_trace_matches_oracle():
+    scenes = _scenes()
+    inst = _instances()
+    world = _world(scenes, inst)
+    rays = random_rays(np.random.default_rng(1), 50000, -8.0, 8.0)
+    with xr.Renderer(64, 64) as r:
+        r.upload_scenes(list(scenes))
+        r.set_instances(inst)
+        assert np.array_equal(r.instance_transforms(len(inst)).view(np.uint32), world.transforms().view(np.uint32))
+        st = r.stats()
+        assert st.instances == len(inst) and st.tlas_nodes >= 1
+        g = r.trace_instanced(rays)
+        c = world.trace_instanced(rays)
+        assert (c[0] >= 0).mean() > 0.1
+        for name, x, y in zip(("prim", "instance", "t", "bary"), g, c):
+            assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32)), name
+        ga = r.trace_instanced(rays, any_hit=True)
+        ca = world.trace_instanced(rays, any_hit=True)
+        assert np.array_equal(ga[0] >= 0, ca[0] >= 0)
+        # the plain query reports the same primitives
+        p, t, _ = r.trace(rays)
+        assert np.array_equal(p, g[0])
+
+
+def test_identity_instance_renders_like_the_scene():
+    scene = xr.Scene.procedural(seed=3, n_objects=200, n_lights=6, extent=8.0)
+    W, H = 96, 64
+    ubos = camera_sequence(scene, W, H, 4, 4)
+    out = []
+    for use_inst in (False, True):
+        with xr.Renderer(W, H) as r:
+            r.set_params(xr.params_default(W, H, write_hdr=1))
+            r.upload_scene(scene)
+            r.build_bvh()
+            if use_inst:
+                r.set_instances([(0, affine(np.eye(3), [0, 0, 0]))])
+            for u in ubos:
+                r.render(u)
+            out.append(r.read_output(XR.XR_OUT_HDR).copy())
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
+@pytest.mark.parametrize("moving", [False, True])
+def test_instanced_frames_match_oracle(moving):
+    scenes = _scenes(11)
+    W, H = 96, 72
+    cam = xr._lib.XrCamera()
+    cam.position[:] = [0.0, 1.0, 12.0]
+    cam.yaw_deg, cam.pitch_deg, cam.fov_deg = 0.0, -5.0, 60.0
+    view = xr.Scene(scenes[0].vertices, scenes[0].indices, scenes[0].materials, scenes[0].ranges, cam)
+    ubos = camera_sequence(view, W, H, 5, 4)
+    p = xr.params_default(W, H, write_hdr=1, write_pt=1)
+    world = _world(scenes, _instances(0.0))
+    o = ob.OracleRenderer(world, p)
+    with xr.Renderer(W, H) as r:
+        r.set_params(p)
+        r.upload_scenes(list(scenes))
+        for f, u in enumerate(ubos):
+            inst = _instances(0.1 * f if moving else 0.0)
+            if moving or f == 0:
+                r.set_instances(inst)
+                world.set_instances(inst)
+            r.render(u)
+            o.render(u)
+            _compare_frame(r, o, False, f"frame {f}")
+
+
+def test_refit_traces_like_the_moved_scene():
+    scene = xr.Scene.procedural(seed=9, n_objects=300, n_lights=4, extent=8.0)
+    rng = np.random.default_rng(5)
+    rays = random_rays(rng, 50000, -8.0, 8.0)
+    v = scene.vertices.copy()
+    v[:, 1] += 0.3 * np.sin(0.7 * v[:, 0]) * np.cos(0.5 * v[:, 2])
+    moved = xr.Scene(v, scene.indices, scene.materials, scene.ranges, scene.camera)
+    oracle = ob.OracleScene.from_scene(moved)
+    with xr.Renderer(64, 64) as r:
+        r.upload_scene(scene)
+        r.build_bvh()
+        r.update_vertices(0, v)
+        assert r.stats().ms_refit > 0.0
+        g = r.trace(rays)
+        c = oracle.trace(rays)
+        assert (c[0] >= 0).mean() > 0.2
+        for name, x, y in zip(("prim", "t", "bary"), g, c):
+            assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32)), name
+        # and under an instance
+        inst = [(0, affine(rotation([0, 1, 0], 25), [0.5, 0.0, -1.0]))]
+        r.set_instances(inst)
+        world = ob.OracleWorld([oracle])
+        world.set_instances(inst)
+        g = r.trace_instanced(rays)
+        c = world.trace_instanced(rays)
+        for name, x, y in zip(("prim", "instance", "t", "bary"), g, c):
+            assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32)), name
+
+
+def test_instance_errors():
+    scenes = _scenes()
+    with xr.Renderer(32, 32) as r:
+        r.upload_scenes(list(scenes))
+        with pytest.raises(xr.XrError):
+            r.set_instances([(2, affine(np.eye(3), [0, 0, 0]))])
+        with pytest.raises(xr.XrError):
+            r.set_instances([(0, affine(np.diag([1.0, 0.0, 1.0]), [0, 0, 0]))])
+        r.set_instances([(0, affine(np.eye(3), [0, 0, 0]))])
+        r.set_instances([])
+        assert r.stats().instances == 0
+        p, inst, t, _ = r.trace_instanced(random_rays(np.random.default_rng(0), 100, -3, 3))
+        assert np.all(inst == -1)

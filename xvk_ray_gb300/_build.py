@@ -33,7 +33,8 @@ NVCC_FLAGS = ARCH + [
 ] + os.environ.get("XR_EXTRA_NVCC_FLAGS", "").split()   # e.g. -DXR_TRACE_MIN_BLOCKS=10 (tuning builds)
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 
-CU_SOURCES = ["bvh_build.cu", "trace.cu", "trace_noalloc.cu", "restir.cu", "nrc.cu", "cache_api.cu", "batch.cu", "xr_api.cu"]
+CU_SOURCES = ["bvh_build.cu", "trace.cu", "trace_noalloc.cu", "restir.cu", "nrc.cu", "cache_api.cu", "batch.cu",
+              "instances.cu", "xr_api.cu"]
 CXX_SOURCES = ["scene_gen.cpp", "image_io.cpp"]
 
 

@@ -76,7 +76,12 @@ class XrStats(C.Structure):
                 ("rays_traced", C.c_uint64), ("shadow_rays", C.c_uint64), ("bvh_nodes", C.c_uint32),
                 ("bvh_triangles", C.c_uint32), ("bvh_depth", C.c_uint32), ("ms_bvh_build", C.c_float),
                 ("query_rays", C.c_uint64), ("query_node_visits", C.c_uint64), ("query_tri_tests", C.c_uint64),
-                ("nonfinite_rays", C.c_uint64)]
+                ("nonfinite_rays", C.c_uint64), ("instances", C.c_uint32), ("tlas_nodes", C.c_uint32),
+                ("ms_tlas_build", C.c_float), ("ms_refit", C.c_float)]
+
+
+class XrInstance(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("reserved", C.c_uint32), ("object_to_world", C.c_float * 12)]
 
 
 class XrCamera(C.Structure):
@@ -172,6 +177,10 @@ _SIGS = {
     "xr_upload_textures": (_i32, [_P, _P, _u32]),
     "xr_png_unfilter": (_i32, [_P, _u32, _u32, _u32, _P]),
     "xr_upload_scenes": (_i32, [_P, _P, _u32]),
+    "xr_set_instances": (_i32, [_P, _P, _u32]),
+    "xr_get_instance_transforms": (_i32, [_P, _P, _u32]),
+    "xr_update_vertices": (_i32, [_P, _u32, _P, _u32]),
+    "xr_trace_rays_instanced": (_i32, [_P, _P, _u32, _i32, _P, _P, _P, _P]),
     "xr_set_views": (_i32, [_P, _P, _u32, C.POINTER(XrParams)]),
     "xr_render_views": (_i32, [_P, _P]),
     "xr_read_view_output": (_i32, [_P, _u32, _u32, _P, C.c_size_t]),

@@ -276,6 +276,37 @@ class Renderer:
                                         _ptr(bary)))
         return prim, t, bary
 
+    def trace_instanced(self, rays: np.ndarray, any_hit: bool = False):
+        """trace() that also returns each hit's instance (-1: miss or no instances)."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        inst = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        bary = np.empty((n, 2), np.float32)
+        self._c(self._lib.xr_trace_rays_instanced(self.ctx, _ptr(rays), n, 1 if any_hit else 0, _ptr(prim),
+                                                  _ptr(inst), _ptr(t), _ptr(bary)))
+        return prim, inst, t, bary
+
+    def set_instances(self, instances) -> None:
+        """instances: (scene index, 3x4 object-to-world matrix) pairs; [] clears them."""
+        arr = (L.XrInstance * max(len(instances), 1))()
+        for k, (scene, m) in enumerate(instances):
+            arr[k].scene = int(scene)
+            arr[k].object_to_world[:] = [float(x) for x in np.asarray(m, np.float64).reshape(12)]
+        self._c(self._lib.xr_set_instances(self.ctx, C.cast(arr, C.c_void_p), len(instances)))
+
+    def instance_transforms(self, n: int) -> np.ndarray:
+        """(n, 2, 3, 4): object-to-world and world-to-object of the first n instances."""
+        out = np.empty((n, 24), np.float32)
+        self._c(self._lib.xr_get_instance_transforms(self.ctx, _ptr(out), n))
+        return out.reshape(n, 2, 3, 4)
+
+    def update_vertices(self, scene: int, vertices: np.ndarray) -> None:
+        """New vertices (same count and layout as uploaded) of a scene, then a refit of its BVH."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        self._c(self._lib.xr_update_vertices(self.ctx, int(scene), _ptr(v), v.shape[0]))
+
 
 # host layout of XrCacheSample (72 B)
 CACHE_SAMPLE_DTYPE = np.dtype([("pos", "<f4", 3), ("normal", "<f4", 3), ("wo", "<f4", 3), ("albedo", "<f4", 3),

@@ -96,6 +96,8 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
     }
     cudaStreamSynchronize(c->stream);
     invalidate_graphs(c);
+    free_instances(c);   // instances refer to the former scenes
+    c->parts.clear();
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats); cudaFree(c->d_vuv);
     cudaFree(c->d_nodes); cudaFree(c->d_tris);
     c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr; c->d_vuv = nullptr;
@@ -113,10 +115,18 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
         return s;
     }
     std::vector<uint32_t> roots(n);
+    std::vector<ScenePart> plist(n);
     size_t ov = 0, ot = 0, om = 0, on = 0, os = 0;
     for (uint32_t k = 0; k < n; k++) {
         Context* p = parts[k];
         roots[k] = p->n_nodes ? (uint32_t)on : kNoRoot;
+        ScenePart& sp = plist[k];
+        sp.vert_off = (uint32_t)ov; sp.nv = p->nv; sp.prim_off = (uint32_t)ot; sp.ntri = p->ntri;
+        sp.mat_off = (uint32_t)om; sp.nm = p->nm; sp.node_off = (uint32_t)on; sp.n_nodes = p->n_nodes;
+        sp.slot_off = (uint32_t)os; sp.n_slots = p->n_tri_slots;
+        sp.levels = p->bvh_levels;
+        sp.emin = p->bvh_emin;
+        for (int a = 0; a < 3; a++) { sp.lo[a] = p->scene_lo[a]; sp.hi[a] = p->scene_hi[a]; }
         if (p->ntri)
             k_relocate_prims<<<blocks(p->ntri), 256, 0, c->stream>>>(c->d_tri_idx + ot, p->d_tri_idx, p->ntri,
                                                                      (uint32_t)ov, (uint32_t)om);
@@ -157,6 +167,7 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
     c->n_nodes = (uint32_t)nodes; c->n_tri_slots = (uint32_t)slots; c->bvh_depth = depth;
     c->scene_has_non_lambert = non_lambert;
     c->scene_roots = roots;
+    c->parts = plist;
     c->scene_ready = true;
     c->bvh_ready = true;
     DeviceScene& sc = c->fa.sc;

@@ -54,15 +54,23 @@ __host__ __device__ __forceinline__ float o2f(uint32_t u) {
 }
 
 // bounds[0..2] centroid min, [3..5] centroid max, [6] largest |coordinate|
+// Primitive boxes: triangles from their vertices, or given boxes (box_lo non-null).
 __global__ void k_tri_prep(const uint4* __restrict__ tri_idx, const float4* __restrict__ vpos, uint32_t ntri,
+                           const float4* __restrict__ box_lo, const float4* __restrict__ box_hi,
                            float4* __restrict__ tri_lo, float4* __restrict__ tri_hi, uint32_t* __restrict__ bounds) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY}, amax = 0.0f;
     if (t < ntri) {
-        uint4 id = tri_idx[t];
-        float4 a = vpos[id.x], b = vpos[id.y], c = vpos[id.z];
-        float3 lo = f3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
-        float3 hi = f3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+        float3 lo, hi;
+        if (box_lo) {
+            lo = xyz(box_lo[t]);
+            hi = xyz(box_hi[t]);
+        } else {
+            uint4 id = tri_idx[t];
+            float4 a = vpos[id.x], b = vpos[id.y], c = vpos[id.z];
+            lo = f3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+            hi = f3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+        }
         tri_lo[t] = make_float4(lo.x, lo.y, lo.z, 0.0f);
         tri_hi[t] = make_float4(hi.x, hi.y, hi.z, 0.0f);
         float cx = (lo.x + hi.x) * 0.5f, cy = (lo.y + hi.y) * 0.5f, cz = (lo.z + hi.z) * 0.5f;
@@ -261,6 +269,7 @@ struct CollapseArgs {
     const float4* nlo; const float4* nhi; const float4* tlo; const float4* thi;
     const uint32_t* sorted;           // sorted primitive ids
     const uint4* tri_idx; const float4* vpos;
+    const float4* records;            // non-null: leaves copy 4 float4 per primitive from here (instances)
     const uint32_t* task_in; const uint32_t* task_wide_in; uint32_t n_tasks;
     uint32_t* task_out; uint32_t* task_wide_out;
     uint32_t* counters;               // [0] wide nodes, [1] tri slots, [2] next task count
@@ -280,6 +289,40 @@ __device__ __forceinline__ int ceil_log2f(float v) {   // smallest e with 2^e >=
     int e;
     float m = frexpf(v, &e);                           // v = m 2^e, m in [0.5, 1)
     return (m == 0.5f) ? e - 1 : e;
+}
+
+// Quantisation grid of a node over its box: p = lo - one cell, cells of 2^e per
+// axis with extent / 2^e <= 250 (at least 2^emin).
+__device__ __forceinline__ void node_grid(float4 plo, float4 phi, int emin, float p3[3], int e[3]) {
+    const float lo3[3] = {plo.x, plo.y, plo.z}, hi3[3] = {phi.x, phi.y, phi.z};
+    for (int k = 0; k < 3; k++) {
+        const float ext = hi3[k] - lo3[k];
+        int ek = ext > 0.0f ? ceil_log2f(ext / 250.0f) : emin;
+        ek = max(ek, emin);
+        e[k] = ek;
+        p3[k] = lo3[k] - ldexpf(1.0f, ek);
+    }
+}
+// A child box on its parent's grid, rounded outwards plus the slack of kBoxSlackCells.
+__device__ __forceinline__ void child_q(float4 clo, float4 chi, const float p3[3], const int e[3], int emin,
+                                        uint8_t ql[3], uint8_t qh[3]) {
+    const float cl[3] = {clo.x, clo.y, clo.z}, ch[3] = {chi.x, chi.y, chi.z};
+    for (int k = 0; k < 3; k++) {
+        const float inv = ldexpf(1.0f, -e[k]);
+        const float slack = fmaxf(kBoxSlackCells, ldexpf(1.0f, emin - e[k]));
+        const float l = floorf((cl[k] - p3[k]) * inv - slack);
+        const float h = ceilf((ch[k] - p3[k]) * inv + slack);
+        ql[k] = (uint8_t)fminf(fmaxf(l, 0.0f), 255.0f);
+        qh[k] = (uint8_t)fminf(fmaxf(h, 0.0f), 255.0f);
+    }
+}
+__device__ __forceinline__ void pack_q(const uint8_t ql[3][8], const uint8_t qh[3][8], uint32_t q[12]) {
+    for (int k = 0; k < 3; k++) {
+        q[2 * k] = ql[k][0] | (ql[k][1] << 8) | (ql[k][2] << 16) | ((uint32_t)ql[k][3] << 24);
+        q[2 * k + 1] = ql[k][4] | (ql[k][5] << 8) | (ql[k][6] << 16) | ((uint32_t)ql[k][7] << 24);
+        q[6 + 2 * k] = qh[k][0] | (qh[k][1] << 8) | (qh[k][2] << 16) | ((uint32_t)qh[k][3] << 24);
+        q[6 + 2 * k + 1] = qh[k][4] | (qh[k][5] << 8) | (qh[k][6] << 16) | ((uint32_t)qh[k][7] << 24);
+    }
 }
 
 __global__ void k_collapse(CollapseArgs a) {
@@ -358,17 +401,10 @@ __global__ void k_collapse(CollapseArgs a) {
         atomicOr(&a.counters[3], 1u);   // inconsistent tree: reported by the host, nothing written
         return;
     }
-    // quantisation grid: p = lo - one cell, cells of 2^e with extent / 2^e <= 250
     WideNode nd;
     int e[3];
-    float lo3[3] = {plo.x, plo.y, plo.z}, hi3[3] = {phi.x, phi.y, phi.z}, p3[3];
-    for (int k = 0; k < 3; k++) {
-        float ext = hi3[k] - lo3[k];
-        int ek = ext > 0.0f ? ceil_log2f(ext / 250.0f) : a.emin;
-        ek = max(ek, a.emin);
-        e[k] = ek;
-        p3[k] = lo3[k] - ldexpf(1.0f, ek);
-    }
+    float p3[3];
+    node_grid(plo, phi, a.emin, p3, e);
     nd.px = p3[0]; nd.py = p3[1]; nd.pz = p3[2];
     nd.exyz_imask = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
     nd.child_base = child_base;
@@ -382,15 +418,9 @@ __global__ void k_collapse(CollapseArgs a) {
         int c = -1;
         for (int cc = 0; cc < nc; cc++) if (slot_of[cc] == s) c = cc;
         if (c < 0) continue;
-        float cl[3] = {clo[c].x, clo[c].y, clo[c].z}, ch[3] = {chi[c].x, chi[c].y, chi[c].z};
-        for (int k = 0; k < 3; k++) {
-            float inv = ldexpf(1.0f, -e[k]);
-            const float slack = fmaxf(kBoxSlackCells, ldexpf(1.0f, a.emin - e[k]));
-            float l = floorf((cl[k] - p3[k]) * inv - slack);
-            float h = ceilf((ch[k] - p3[k]) * inv + slack);
-            ql[k][s] = (uint8_t)fminf(fmaxf(l, 0.0f), 255.0f);
-            qh[k][s] = (uint8_t)fminf(fmaxf(h, 0.0f), 255.0f);
-        }
+        uint8_t cql[3], cqh[3];
+        child_q(clo[c], chi[c], p3, e, a.emin, cql, cqh);
+        for (int k = 0; k < 3; k++) { ql[k][s] = cql[k]; qh[k][s] = cqh[k]; }
         uint32_t r = refs[c];
         if (imask & (1u << s)) {
             meta[s] = (uint8_t)(0x20u | (24u + (uint32_t)s));   // one bit, at 24 + slot
@@ -417,6 +447,11 @@ __global__ void k_collapse(CollapseArgs a) {
             meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | off);   // cnt bits, at the triangle offset
             for (uint32_t j = 0; j < cnt; j++) {
                 uint32_t prim = prims[j];
+                if (a.records) {   // an instance record: world-to-object rows, {instance, root}
+                    float4* dst = a.tris + 4u * (tri_base + off + j);
+                    for (int w = 0; w < 4; w++) dst[w] = a.records[4u * prim + w];
+                    continue;
+                }
                 uint4 id = a.tri_idx[prim];
                 float4 v0 = a.vpos[id.x], v1 = a.vpos[id.y], v2 = a.vpos[id.z];
                 float4* dst = a.tris + 3u * (tri_base + off + j);
@@ -429,13 +464,76 @@ __global__ void k_collapse(CollapseArgs a) {
     }
     nd.meta[0] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | ((uint32_t)meta[3] << 24);
     nd.meta[1] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | ((uint32_t)meta[7] << 24);
-    auto pack = [&](const uint8_t* q8, uint32_t* w) {
-        w[0] = q8[0] | (q8[1] << 8) | (q8[2] << 16) | ((uint32_t)q8[3] << 24);
-        w[1] = q8[4] | (q8[5] << 8) | (q8[6] << 16) | ((uint32_t)q8[7] << 24);
-    };
-    pack(ql[0], &nd.q[0]); pack(ql[1], &nd.q[2]); pack(ql[2], &nd.q[4]);
-    pack(qh[0], &nd.q[6]); pack(qh[1], &nd.q[8]); pack(qh[2], &nd.q[10]);
+    pack_q(ql, qh, nd.q);
     a.nodes[widx] = nd;
+}
+
+// ---- refit: new vertex positions under the same topology ----
+// Triangle slots [first, first + n) take their primitive's current vertex positions.
+__global__ void k_refit_slots(float4* __restrict__ tris, uint32_t first, uint32_t n, const uint4* __restrict__ tri_idx,
+                              const float4* __restrict__ vpos) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4* t = tris + 3u * ((size_t)first + i);
+    const float w = t[0].w;
+    const uint4 id = tri_idx[__float_as_uint(w)];
+    const float4 v0 = vpos[id.x], v1 = vpos[id.y], v2 = vpos[id.z];
+    t[0] = make_float4(v0.x, v0.y, v0.z, w);
+    t[1] = make_float4(v1.x, v1.y, v1.z, 0.0f);
+    t[2] = make_float4(v2.x, v2.y, v2.z, 0.0f);
+}
+
+// Nodes [first, first + n), one level, deepest level first: each child's exact box
+// (a leaf child from its triangle slots, an internal child from the box the launch
+// of the level below wrote), the node's box, then its grid and child boxes
+// requantised as the build does; topology, slots and metadata are kept.
+__global__ void k_refit_level(WideNode* __restrict__ nodes, uint32_t first, uint32_t n, const float4* __restrict__ tris,
+                              float4* __restrict__ box_lo, float4* __restrict__ box_hi, int emin) {
+    const uint32_t w = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= first + n) return;
+    WideNode nd = nodes[w];
+    const uint32_t imask = nd.exyz_imask >> 24;
+    float4 clo[8], chi[8];
+    float4 plo = make_float4(INFINITY, INFINITY, INFINITY, 0), phi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
+    uint32_t present = 0;
+    for (int s = 0; s < 8; s++) {
+        const uint32_t meta = (nd.meta[s >> 2] >> (8 * (s & 3))) & 0xFFu;
+        if (meta == 0u) continue;
+        present |= 1u << s;
+        if (imask & (1u << s)) {
+            const uint32_t c = nd.child_base + __popc(imask & ((1u << s) - 1u));
+            clo[s] = box_lo[c];
+            chi[s] = box_hi[c];
+        } else {
+            float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
+            const uint32_t off = meta & 31u, cnt = __popc(meta >> 5);
+            for (uint32_t j = 0; j < cnt; j++)
+                for (int v = 0; v < 3; v++) {
+                    const float4 q = tris[3u * ((size_t)nd.tri_base + off + j) + v];
+                    lo = make_float4(fminf(lo.x, q.x), fminf(lo.y, q.y), fminf(lo.z, q.z), 0);
+                    hi = make_float4(fmaxf(hi.x, q.x), fmaxf(hi.y, q.y), fmaxf(hi.z, q.z), 0);
+                }
+            clo[s] = lo;
+            chi[s] = hi;
+        }
+        plo = make_float4(fminf(plo.x, clo[s].x), fminf(plo.y, clo[s].y), fminf(plo.z, clo[s].z), 0);
+        phi = make_float4(fmaxf(phi.x, chi[s].x), fmaxf(phi.y, chi[s].y), fmaxf(phi.z, chi[s].z), 0);
+    }
+    box_lo[w] = plo;
+    box_hi[w] = phi;
+    int e[3];
+    float p3[3];
+    node_grid(plo, phi, emin, p3, e);
+    uint8_t ql[3][8], qh[3][8];
+    for (int s = 0; s < 8; s++) {
+        uint8_t cql[3] = {0, 0, 0}, cqh[3] = {0, 0, 0};
+        if (present & (1u << s)) child_q(clo[s], chi[s], p3, e, emin, cql, cqh);
+        for (int k = 0; k < 3; k++) { ql[k][s] = cql[k]; qh[k][s] = cqh[k]; }
+    }
+    nd.px = p3[0]; nd.py = p3[1]; nd.pz = p3[2];
+    nd.exyz_imask = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
+    pack_q(ql, qh, nd.q);
+    nodes[w] = nd;
 }
 
 // ---- PLOC: Meister and Bittner, "Parallel Locally-Ordered Clustering for
@@ -575,13 +673,15 @@ xr_status dalloc(Context* ctx, T** p, size_t count) {
 
 }  // namespace
 
-xr_status build_bvh(Context* ctx) {
+xr_status build_wide(Context* ctx, WideBuild& B) {
     cudaStream_t st = ctx->stream;
-    const uint32_t n = ctx->ntri;
-    if (ctx->d_nodes) { cudaFree(ctx->d_nodes); ctx->d_nodes = nullptr; }
-    if (ctx->d_tris) { cudaFree(ctx->d_tris); ctx->d_tris = nullptr; }
-    ctx->n_nodes = 0; ctx->n_tri_slots = 0; ctx->bvh_depth = 0;
-    if (n == 0) { ctx->bvh_ready = true; return XR_OK; }
+    const uint32_t n = B.n;
+    const bool records = B.records != nullptr;
+    const uint32_t slot_words = records ? 4u : 3u;
+    B.nodes = nullptr; B.slots = nullptr;
+    B.n_nodes = 0; B.n_slots = 0; B.depth = 0; B.emin = 0; B.ms = 0.0f;
+    B.level_off.clear();
+    if (n == 0) return XR_OK;
 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
@@ -605,13 +705,13 @@ xr_status build_bvh(Context* ctx) {
         (s = dalloc(ctx, &flags, nint + 1)) || (s = dalloc(ctx, &range, nint)) || (s = dalloc(ctx, &nlo, nint)) ||
         (s = dalloc(ctx, &nhi, nint)) || (s = dalloc(ctx, &ta, n)) || (s = dalloc(ctx, &tb, n)) ||
         (s = dalloc(ctx, &wa, n)) || (s = dalloc(ctx, &wb, n)) || (s = dalloc(ctx, &counters, 4)) ||
-        (s = dalloc(ctx, &nodes_tmp, nint)) || (s = dalloc(ctx, &ctx->d_tris, 3 * (size_t)n)))
+        (s = dalloc(ctx, &nodes_tmp, nint)) || (s = dalloc(ctx, &B.slots, (size_t)slot_words * n)))
         goto done;
     {
         uint32_t binit[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
         cudaMemcpyAsync(bounds, binit, sizeof(binit), cudaMemcpyHostToDevice, st);
         uint32_t blocks = (n + 255) / 256;
-        k_tri_prep<<<blocks, 256, 0, st>>>(ctx->d_tri_idx, ctx->d_vpos, n, tlo, thi, bounds);
+        k_tri_prep<<<blocks, 256, 0, st>>>(B.tri_idx, B.vpos, n, B.box_lo, B.box_hi, tlo, thi, bounds);
         k_morton<<<blocks, 256, 0, st>>>(tlo, thi, n, bounds, k0, v0);
         for (int pass = 0; pass < 8; pass++) {
             int shift = pass * 8;
@@ -629,6 +729,8 @@ xr_status build_bvh(Context* ctx) {
         int emin;
         frexpf(fmaxf(amax, 1e-20f), &emin);
         emin -= 17;   // cells of at least 2^-17 of the largest coordinate
+        emin = std::max(emin, B.emin_floor);
+        B.emin = emin;
         cudaMemsetAsync(pint, 0xFF, nint * 4, st);
         cudaMemsetAsync(pleaf, 0xFF, (size_t)n * 4, st);
         cudaMemsetAsync(flags, 0, (nint + 1) * 4, st);
@@ -686,17 +788,23 @@ xr_status build_bvh(Context* ctx) {
         cudaMemcpyAsync(ta, &root_ref, 4, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(wa, &zero, 4, cudaMemcpyHostToDevice, st);
         uint32_t ntask = 1, depth = 0;
+        B.level_off.push_back(0u);
+        B.level_off.push_back(1u);   // level 0: the root
         while (ntask > 0) {
             CollapseArgs ca;
             ca.left = left; ca.right = right; ca.count = range; ca.nlo = nlo; ca.nhi = nhi; ca.tlo = tlo; ca.thi = thi;
-            ca.sorted = v0; ca.tri_idx = ctx->d_tri_idx; ca.vpos = ctx->d_vpos;
+            ca.sorted = v0; ca.tri_idx = B.tri_idx; ca.vpos = B.vpos; ca.records = B.records;
             ca.task_in = ta; ca.task_wide_in = wa; ca.n_tasks = ntask; ca.task_out = tb; ca.task_wide_out = wb;
-            ca.counters = counters; ca.nodes = nodes_tmp; ca.tris = ctx->d_tris; ca.emin = emin;
+            ca.counters = counters; ca.nodes = nodes_tmp; ca.tris = B.slots; ca.emin = emin;
             ca.max_nodes = nint; ca.n_prims = n;
             cudaMemsetAsync(counters + 2, 0, 4, st);
             k_collapse<<<(ntask + 127) / 128, 128, 0, st>>>(ca);
-            cudaMemcpyAsync(&ntask, counters + 2, 4, cudaMemcpyDeviceToHost, st);
+            uint32_t cnt3[3];
+            cudaMemcpyAsync(cnt3, counters, sizeof(cnt3), cudaMemcpyDeviceToHost, st);
             if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: collapse"))) goto done;
+            ntask = cnt3[2];
+            // the nodes this level allocated are the next level
+            if (cnt3[0] > B.level_off.back()) B.level_off.push_back(cnt3[0]);
             std::swap(ta, tb);
             std::swap(wa, wb);
             depth++;
@@ -707,15 +815,14 @@ xr_status build_bvh(Context* ctx) {
         cudaMemcpy(&bflag, flags + nint, 4, cudaMemcpyDeviceToHost);
         if (ch[3] || bflag) { s = fail(ctx, XR_ERR_STATE, "bvh: inconsistent radix tree"); goto done; }
         if (ch[1] != n) { s = fail(ctx, XR_ERR_STATE, "bvh: triangle slots do not match the primitive count"); goto done; }
-        if ((s = dalloc(ctx, &ctx->d_nodes, ch[0]))) goto done;
-        cudaMemcpyAsync(ctx->d_nodes, nodes_tmp, (size_t)ch[0] * sizeof(WideNode), cudaMemcpyDeviceToDevice, st);
+        if ((s = dalloc(ctx, &B.nodes, ch[0]))) goto done;
+        cudaMemcpyAsync(B.nodes, nodes_tmp, (size_t)ch[0] * sizeof(WideNode), cudaMemcpyDeviceToDevice, st);
         cudaEventRecord(e1, st);
         if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: finish"))) goto done;
-        ctx->n_nodes = ch[0];
-        ctx->n_tri_slots = ch[1];
-        ctx->bvh_depth = depth;
-        cudaEventElapsedTime(&ctx->ms_bvh, e0, e1);
-        ctx->bvh_ready = true;
+        B.n_nodes = ch[0];
+        B.n_slots = ch[1];
+        B.depth = depth;
+        cudaEventElapsedTime(&B.ms, e0, e1);
     }
 done:
     cudaFree(tlo); cudaFree(thi); cudaFree(k0); cudaFree(k1); cudaFree(v0); cudaFree(v1); cudaFree(bounds);
@@ -723,8 +830,44 @@ done:
     cudaFree(range); cudaFree(nlo); cudaFree(nhi); cudaFree(ta); cudaFree(tb); cudaFree(wa); cudaFree(wb);
     cudaFree(counters); cudaFree(nodes_tmp);
     cudaEventDestroy(e0); cudaEventDestroy(e1);
-    if (s != XR_OK && ctx->d_tris) { cudaFree(ctx->d_tris); ctx->d_tris = nullptr; }
+    if (s != XR_OK) {
+        cudaFree(B.slots); B.slots = nullptr;
+        cudaFree(B.nodes); B.nodes = nullptr;
+        B.level_off.clear();
+    }
     return s;
+}
+
+xr_status build_bvh(Context* ctx) {
+    if (ctx->d_nodes) { cudaFree(ctx->d_nodes); ctx->d_nodes = nullptr; }
+    if (ctx->d_tris) { cudaFree(ctx->d_tris); ctx->d_tris = nullptr; }
+    ctx->n_nodes = 0; ctx->n_tri_slots = 0; ctx->bvh_depth = 0;
+    ctx->bvh_levels.clear();
+    WideBuild wb;
+    wb.n = ctx->ntri;
+    wb.tri_idx = ctx->d_tri_idx;
+    wb.vpos = ctx->d_vpos;
+    xr_status s = build_wide(ctx, wb);
+    if (s) return s;
+    ctx->d_nodes = wb.nodes;
+    ctx->d_tris = wb.slots;
+    ctx->n_nodes = wb.n_nodes;
+    ctx->n_tri_slots = wb.n_slots;
+    ctx->bvh_depth = wb.depth;
+    ctx->bvh_levels = wb.level_off;
+    ctx->bvh_emin = wb.emin;
+    ctx->ms_bvh = wb.ms;
+    ctx->bvh_ready = true;
+    return XR_OK;
+}
+
+void launch_refit_slots(float4* tris, uint32_t first, uint32_t n, const uint4* tri_idx, const float4* vpos,
+                        cudaStream_t st) {
+    if (n) k_refit_slots<<<(n + 255) / 256, 256, 0, st>>>(tris, first, n, tri_idx, vpos);
+}
+void launch_refit_level(WideNode* nodes, uint32_t first, uint32_t n, const float4* tris, float4* box_lo,
+                        float4* box_hi, int emin, cudaStream_t st) {
+    if (n) k_refit_level<<<(n + 127) / 128, 128, 0, st>>>(nodes, first, n, tris, box_lo, box_hi, emin);
 }
 
 }  // namespace xr

@@ -243,6 +243,8 @@ xr_status xr_cache_set_params(XrContext* c, const XrCacheParams* p) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "cache_set_params: null context");
     xr_status s = validate(c, p);
     if (s) return s;
+    if (p->enabled && !c->instances.empty())
+        return fail(c, XR_ERR_UNSUPPORTED, "cache_set_params: the learned cache covers one scene without instances");
     DeviceGuard g(c->device);
     invalidate_graphs(c);
     c->cache.params = *p;

@@ -39,8 +39,14 @@ struct HitPayload {
     float t;
 };
 
-// Ray.rchit.hlsl:26-60 with identity instance transforms; miss = material -1
-// (Ray.rmiss.hlsl:3-8).
+// Ray.rchit.hlsl:26-60; miss = material -1 (Ray.rmiss.hlsl:3-8).  Without
+// instances the object space is the world space (the reference's identity
+// instances).  A hit on an instance maps the interpolated position by its
+// object-to-world rows (Ray.rchit.hlsl:46-47) and the shading and geometric
+// normals by the transpose of its world-to-object rows, the inverse transpose
+// (Ray.rchit.hlsl:53 does this for the geometric normal; its shading normal,
+// mul(float4(n, 0), WorldToObject4x3()), equals the same thing only for the
+// identity transforms it is used with).
 __device__ __forceinline__ HitPayload closest_hit(const DeviceScene& sc, const HitRec& h) {
     HitPayload pl;
     uint4 id = __ldg(sc.tri_idx + h.prim);
@@ -56,7 +62,16 @@ __device__ __forceinline__ HitPayload closest_hit(const DeviceScene& sc, const H
         pl.uv = make_float2(u0.x * bx + u1.x * by + u2.x * bz, u0.y * bx + u1.y * by + u2.y * bz);
     }
     float3 e0 = v2 - v0, e1 = v1 - v0;
-    pl.geo = normalize(cross(e0, e1));
+    float3 geo = cross(e0, e1);
+    if (sc.n_inst && h.inst >= 0) {
+        const float4* X = sc.inst_xform + 6u * (uint32_t)h.inst;
+        const float4 o0 = __ldg(X), o1 = __ldg(X + 1), o2 = __ldg(X + 2);
+        const float4 w0 = __ldg(X + 3), w1 = __ldg(X + 4), w2 = __ldg(X + 5);
+        pl.pos = xform_point(o0, o1, o2, pl.pos);
+        normal = xform_normal(w0, w1, w2, normal);
+        geo = xform_normal(w0, w1, w2, geo);
+    }
+    pl.geo = normalize(geo);
     pl.normal = normalize(normal);
     pl.mat = (int32_t)id.w;
     pl.t = h.t;
@@ -502,12 +517,13 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 // ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
 // With several scenes each ray starts at its view's root; a path whose pixel slot
 // holds a cache training record (pixel_is_record) finds its pixel in the record.
+template <bool INST>
 __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_paths(FrameArgs fa, const float4* __restrict__ q0,
                                                         const float4* __restrict__ q1, uint4* __restrict__ hits,
                                                         const uint32_t* count_ptr, uint32_t* next, uint32_t* err,
                                                         uint32_t* nonfinite, uint32_t pixel_is_record) {
     const uint32_t count = *(volatile const uint32_t*)count_ptr;
-    trace_persistent<false>(
+    trace_persistent<false, INST>(
         fa.sc, count, next,
         [&](uint32_t i) {
             float4 a = q0[i], b = q1[i];
@@ -523,6 +539,7 @@ __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_paths(Fra
         },
         [&](uint32_t i, const HitRec& h) {
             hits[i] = make_uint4((uint32_t)h.prim, __float_as_uint(h.t), __float_as_uint(h.b1), __float_as_uint(h.b2));
+            if (INST) fa.hit_inst[i] = h.inst;
         },
         err, nullptr, nonfinite);
 }
@@ -550,6 +567,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformB
             s.thr = xyz(c); s.pq = c.w;
             HitRec h;
             h.prim = (int32_t)hr.x; h.t = __uint_as_float(hr.y); h.b1 = __uint_as_float(hr.z); h.b2 = __uint_as_float(hr.w);
+            h.inst = fa.sc.n_inst ? fa.hit_inst[i] : -1;
             const XrUniformBufferObject* __restrict__ uv = u;
             if (fa.n_views > 1u) {
                 uint32_t p = s.pixel;
@@ -1017,9 +1035,10 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
 // Spatial reuse, step 2 of 3: any-hit traversal of the queued shadow rays
 // (ReSTIRGISpatialReuse.rgen.hlsl:44-62 with the centre pixel's visible point as
 // origin); an occluded ray sets its slot's bit in the pixel's occlusion word.
+template <bool INST>
 __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_shadow(FrameArgs fa) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[32];
-    trace_persistent<true>(
+    trace_persistent<true, INST>(
         fa.sc, count, &fa.counters[kCntFetchShadow],
         [&](uint32_t i) {
             const uint2 e = fa.shadow_q[i];
@@ -1281,7 +1300,7 @@ uint32_t trace_grid(int sm_count) {
     static int occ = 0;
     if (occ == 0) {
         int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<false>, kBlock, 0);
         occ = v > 0 ? v : 4;
     }
     return (uint32_t)(occ * sm_count);
@@ -1296,9 +1315,14 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
     for (uint32_t b = 0; b < nb; b++) {
         // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
-        k_trace_paths<<<fa.grid_trace, kBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
-                                                        fa.counters + kCntFetchPath + b, fa.counters + kCntError,
-                                                        fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u);
+        if (fa.sc.n_inst)
+            k_trace_paths<true><<<fa.grid_trace, kBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+                                                              fa.counters + kCntFetchPath + b, fa.counters + kCntError,
+                                                              fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u);
+        else
+            k_trace_paths<false><<<fa.grid_trace, kBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+                                                               fa.counters + kCntFetchPath + b, fa.counters + kCntError,
+                                                               fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u);
         const bool nee = cache && b >= 1u && b + 1u < nb;
         if (nee) cudaMemsetAsync(fa.counters + kCntCacheNee, 0, 2 * sizeof(uint32_t), st);   // count + fetch
         if (fa.compat) k_shade<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
@@ -1345,7 +1369,10 @@ void launch_spatial(const FrameArgs& fa, cudaStream_t st) {
         return;
     }
     k_spatial_select<<<blocks, 256, 0, st>>>(fa, fa.ubo);
-    if (fa.visibility) k_trace_shadow<<<fa.grid_trace, kBlock, 0, st>>>(fa);
+    if (fa.visibility) {
+        if (fa.sc.n_inst) k_trace_shadow<true><<<fa.grid_trace, kBlock, 0, st>>>(fa);
+        else k_trace_shadow<false><<<fa.grid_trace, kBlock, 0, st>>>(fa);
+    }
     k_spatial_resolve<<<blocks, 256, 0, st>>>(fa, fa.ubo);
 }
 

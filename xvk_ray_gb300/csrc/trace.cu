@@ -13,12 +13,12 @@ namespace {
 
 constexpr int kTraceBlock = 128;
 
-template <bool ANY>
+template <bool ANY, bool INST>
 __global__ void __launch_bounds__(kTraceBlock) k_trace(DeviceScene sc, const float4* __restrict__ rays, uint32_t n,
-                                                       int32_t* __restrict__ prim, float* __restrict__ t,
-                                                       float2* __restrict__ bary, uint32_t* fetch, uint32_t* flags,
-                                                       unsigned long long* work) {
-    trace_persistent<ANY>(
+                                                       int32_t* __restrict__ prim, int32_t* __restrict__ inst,
+                                                       float* __restrict__ t, float2* __restrict__ bary, uint32_t* fetch,
+                                                       uint32_t* flags, unsigned long long* work) {
+    trace_persistent<ANY, INST>(
         sc, n, fetch,
         [&](uint32_t i) {
             float4 a = rays[2 * i], b = rays[2 * i + 1];
@@ -29,31 +29,49 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DeviceScene sc, const flo
         },
         [&](uint32_t i, const HitRec& h) {
             prim[i] = h.prim;
+            if (inst) inst[i] = h.prim >= 0 ? h.inst : -1;
             t[i] = h.prim >= 0 ? h.t : -1.0f;
             bary[i] = make_float2(h.b1, h.b2);
         },
         flags, work);
 }
 
+template <bool ANY, bool INST>
+int trace_occupancy() {
+    static int occ = 0;
+    if (occ == 0) {
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace<ANY, INST>, kTraceBlock, 0);
+        occ = v > 0 ? v : 4;
+    }
+    return occ;
+}
+
+template <bool ANY, bool INST>
+void launch_k_trace(const DeviceScene& sc, const float4* r, uint32_t n, int32_t* prim, int32_t* inst, float* t,
+                    float2* b, uint32_t* fetch, uint32_t* flags, unsigned long long* work, int sm_count,
+                    cudaStream_t st) {
+    const uint32_t blocks = std::min<uint32_t>((n + kTraceBlock - 1) / kTraceBlock,
+                                               (uint32_t)(sm_count * trace_occupancy<ANY, INST>()));
+    k_trace<ANY, INST><<<blocks, kTraceBlock, 0, st>>>(sc, r, n, prim, inst, t, b, fetch, flags, work);
+}
+
 }  // namespace
 
-void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_hit, int32_t* prim, float* t,
-                  float* bary, uint32_t* fetch, uint32_t* flags, unsigned long long* work, int sm_count,
+void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_hit, int32_t* prim, int32_t* inst,
+                  float* t, float* bary, uint32_t* fetch, uint32_t* flags, unsigned long long* work, int sm_count,
                   cudaStream_t st) {
     if (n == 0) return;
-    static int occ[2] = {0, 0};
-    int& o = occ[any_hit ? 1 : 0];
-    if (o == 0) {
-        int v = 0;
-        if (any_hit) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace<true>, kTraceBlock, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace<false>, kTraceBlock, 0);
-        o = v > 0 ? v : 4;
-    }
-    uint32_t blocks = std::min<uint32_t>((n + kTraceBlock - 1) / kTraceBlock, (uint32_t)(sm_count * o));
     const float4* r = reinterpret_cast<const float4*>(rays);
     float2* b = reinterpret_cast<float2*>(bary);
-    if (any_hit) k_trace<true><<<blocks, kTraceBlock, 0, st>>>(sc, r, n, prim, t, b, fetch, flags, work);
-    else k_trace<false><<<blocks, kTraceBlock, 0, st>>>(sc, r, n, prim, t, b, fetch, flags, work);
+    if (sc.n_inst) {
+        if (any_hit) launch_k_trace<true, true>(sc, r, n, prim, inst, t, b, fetch, flags, work, sm_count, st);
+        else launch_k_trace<false, true>(sc, r, n, prim, inst, t, b, fetch, flags, work, sm_count, st);
+    } else {
+        if (inst) cudaMemsetAsync(inst, 0xFF, (size_t)n * 4, st);   // -1: no instances
+        if (any_hit) launch_k_trace<true, false>(sc, r, n, prim, nullptr, t, b, fetch, flags, work, sm_count, st);
+        else launch_k_trace<false, false>(sc, r, n, prim, nullptr, t, b, fetch, flags, work, sm_count, st);
+    }
 }
 
 }  // namespace xr

@@ -89,7 +89,7 @@ extern "C" xr_status xr_trace_rays_noalloc(XrContext* c, const float* rays, uint
         cudaStream_t sm = c->stream;
         cudaMemsetAsync(&s->flags, 0, 2 * sizeof(uint32_t), sm);   // flags and fetch
         cudaMemcpyAsync(s->rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, sm);
-        launch_trace(c->fa.sc, reinterpret_cast<const float*>(s->rays), n, any_hit, s->prim, s->t,
+        launch_trace(c->fa.sc, reinterpret_cast<const float*>(s->rays), n, any_hit, s->prim, nullptr, s->t,
                      reinterpret_cast<float*>(s->bary), &s->fetch, &s->flags, nullptr, c->sm_count, sm);
         cudaMemcpyAsync(prim, s->prim, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);
         cudaMemcpyAsync(t, s->t, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);

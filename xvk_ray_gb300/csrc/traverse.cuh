@@ -90,7 +90,26 @@ __device__ __forceinline__ bool hit_triangle(const RayTri& r, float3 v0, float3 
 struct HitRec {
     int32_t prim;   // -1: miss
     float t, b1, b2;
+    int32_t inst;   // instance of the hit (scenes with instances; -1 otherwise)
 };
+
+// 3 x 4 row-major transforms (rows r0, r1, r2; column 3 = translation), each
+// component one product at a time in the order written (no contraction), as in
+// the oracle.
+__device__ __forceinline__ float3 xform_point(float4 r0, float4 r1, float4 r2, float3 p) {
+    return make_float3(((r0.x * p.x + r0.y * p.y) + r0.z * p.z) + r0.w, ((r1.x * p.x + r1.y * p.y) + r1.z * p.z) + r1.w,
+                       ((r2.x * p.x + r2.y * p.y) + r2.z * p.z) + r2.w);
+}
+__device__ __forceinline__ float3 xform_dir(float4 r0, float4 r1, float4 r2, float3 d) {
+    return make_float3((r0.x * d.x + r0.y * d.y) + r0.z * d.z, (r1.x * d.x + r1.y * d.y) + r1.z * d.z,
+                       (r2.x * d.x + r2.y * d.y) + r2.z * d.z);
+}
+// Transpose of the linear part applied to v: the inverse transpose of the
+// object-to-world map when the rows are those of world-to-object (normals).
+__device__ __forceinline__ float3 xform_normal(float4 r0, float4 r1, float4 r2, float3 v) {
+    return make_float3((r0.x * v.x + r1.x * v.y) + r2.x * v.z, (r0.y * v.x + r1.y * v.y) + r2.y * v.z,
+                       (r0.z * v.x + r1.z * v.y) + r2.z * v.z);
+}
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w0, uint32_t w1, uint32_t i) {
     uint32_t w = i < 4 ? w0 : w1;

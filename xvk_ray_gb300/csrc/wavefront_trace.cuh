@@ -21,6 +21,7 @@
 namespace xr {
 
 constexpr uint32_t kTriGroupBit = 0x80000000u;   // stack entry holds a triangle group
+constexpr uint32_t kLevelBit = 0x40000000u;      // stack entry marks the return to the top-level BVH
 constexpr int kPostponeBelow = 8;                 // lanes; fewer testing triangles -> postpone
 constexpr float kMinDir = 1e-20f;                 // smallest direction component seen by the box test
 
@@ -58,7 +59,15 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // With `work` non-null (query kernels only) the node visits and triangle tests
 // are summed into work[0] and work[1]; with `nonfinite` non-null, the rays ended
 // early for a non-finite origin or direction are counted there.
-template <bool ANY, typename LoadRay, typename StoreHit>
+//
+// INST: two-level traversal of a scene with instances.  Rays start at the root of
+// the top-level BVH (sc.tlas_nodes), whose leaf slots are instances; "testing" one
+// saves the rest of the lane's top-level work on its stack under a level marker,
+// maps the ray into the instance's object space (origin and direction by its
+// world-to-object rows; t is unchanged) and continues at the root of its
+// bottom-level BVH in sc.nodes.  Popping the marker restores the world-space ray
+// (reloaded from the queue).  Hits compare t, then instance, then primitive.
+template <bool ANY, bool INST = false, typename LoadRay, typename StoreHit>
 __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t count, uint32_t* next,
                                                  LoadRay load, StoreHit store, uint32_t* err,
                                                  unsigned long long* work = nullptr, uint32_t* nonfinite = nullptr) {
@@ -80,6 +89,16 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
     uint32_t tg_base = 0, tg_mask = 0;
     uint32_t visits_left = 0;
     bool bad = false;
+    bool in_blas = !INST;    // INST: the lane's ray is in an instance's object space
+    int32_t cur_inst = -1;   // that instance
+    h.inst = -1;
+    // box-test reciprocals and sign bits of a direction (see the comment at the ray start)
+    auto set_dir = [&](float3 d) {
+        idx = 1.0f / copysignf(fmaxf(fabsf(d.x), kMinDir), d.x);
+        idy = 1.0f / copysignf(fmaxf(fabsf(d.y), kMinDir), d.y);
+        idz = 1.0f / copysignf(fmaxf(fabsf(d.z), kMinDir), d.z);
+        flip = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) | ((__float_as_uint(d.z) >> 31) << 2);
+    };
 
     while (true) {
         // ---- refill idle lanes ----
@@ -107,20 +126,28 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     // departs from the true one by at most kMinDir * t, far inside the
                     // slack of the stored boxes, so no box holding a hit is culled;
                     // the triangle test uses the true direction.
-                    idx = 1.0f / copysignf(fmaxf(fabsf(r.d.x), kMinDir), r.d.x);
-                    idy = 1.0f / copysignf(fmaxf(fabsf(r.d.y), kMinDir), r.d.y);
-                    idz = 1.0f / copysignf(fmaxf(fabsf(r.d.z), kMinDir), r.d.z);
+                    // The sign bits select the near planes (so that -0 picks the same
+                    // planes as its infinite reciprocal).
+                    set_dir(r.d);
                     rt = prep_ray(r.o, r.d);
-                    // sign bits (so that -0 selects the same planes as its infinite reciprocal)
-                    flip = (__float_as_uint(r.d.x) >> 31) | ((__float_as_uint(r.d.y) >> 31) << 1) |
-                           ((__float_as_uint(r.d.z) >> 31) << 2);
-                    h.prim = -1; h.t = r.tmax; h.b1 = 0.0f; h.b2 = 0.0f;
+                    h.prim = -1; h.t = r.tmax; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = -1;
                     sp = 0;
                     tg_mask = 0;
-                    visits_left = sc.n_nodes;
-                    // a virtual group whose only child is the root (node 0)
-                    ng_base = r.root;
-                    ng_bits = (r.root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;   // no root: a miss
+                    if (INST) {
+                        // every instance may be entered once: bound the visits accordingly
+                        const unsigned long long lim = ((unsigned long long)sc.n_nodes + sc.n_tlas_nodes) *
+                                                       (unsigned long long)max(sc.n_inst, 1u);
+                        visits_left = lim > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)lim;
+                        in_blas = false;
+                        cur_inst = -1;
+                        ng_base = 0u;   // the top-level root
+                        ng_bits = sc.n_tlas_nodes ? (1u | ((1u << flip) << 8)) : 0u;
+                    } else {
+                        visits_left = sc.n_nodes;
+                        // a virtual group whose only child is the root (node 0)
+                        ng_base = r.root;
+                        ng_bits = (r.root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;   // no root: a miss
+                    }
                     // A non-finite origin or direction (or a zero direction) can hit
                     // nothing -- every triangle test fails -- but would make every box
                     // test pass through NaN slabs and walk the whole tree: end it as a miss.
@@ -144,13 +171,15 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 if (sp < kStackSize) stack[sp++] = make_uint2(ng_base, ng_bits);
                 else bad = true;
             }
-            if (node >= sc.n_nodes || visits_left == 0u) {
+            const WideNode* level_nodes = (INST && !in_blas) ? sc.tlas_nodes : sc.nodes;
+            const uint32_t level_count = (INST && !in_blas) ? sc.n_tlas_nodes : sc.n_nodes;
+            if (node >= level_count || visits_left == 0u) {
                 bad = true;
                 ng_bits = 0;
             } else {
                 visits_left--;
                 n_visits++;
-                const uint4* np = reinterpret_cast<const uint4*>(sc.nodes + node);
+                const uint4* np = reinterpret_cast<const uint4*>(level_nodes + node);
                 const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
                             w4 = __ldg(np + 4);
                 // per axis: S = 32768 * 2^e / d and A = (p - o) / d - S (see qplane)
@@ -210,7 +239,35 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 break;
             }
             first = false;
-            if (want) {
+            if (want && INST && !in_blas) {
+                // an instance: enter its bottom-level BVH in object space
+                const uint32_t bit = __ffs(tg_mask) - 1u;
+                tg_mask &= tg_mask - 1u;
+                if (tg_base + bit >= sc.n_inst_slots || sp + 3 > kStackSize) {
+                    bad = true;
+                    tg_mask = 0u;
+                    ng_bits = 0u;
+                } else {
+                    const float4* ip = sc.inst_slots + 4u * (tg_base + bit);
+                    const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2), m3 = __ldg(ip + 3);
+                    // the rest of the top-level work, then the level marker
+                    if (ng_bits & 0xFFu) stack[sp++] = make_uint2(ng_base, ng_bits);
+                    if (tg_mask) stack[sp++] = make_uint2(tg_base, tg_mask | kTriGroupBit);
+                    stack[sp++] = make_uint2(0u, kLevelBit);
+                    tg_mask = 0u;
+                    const RayIn wr = load(ray_id);
+                    o = xform_point(m0, m1, m2, wr.o);
+                    const float3 od = xform_dir(m0, m1, m2, wr.d);
+                    set_dir(od);
+                    rt = prep_ray(o, od);
+                    cur_inst = (int32_t)__float_as_uint(m3.x);
+                    in_blas = true;
+                    ng_base = __float_as_uint(m3.y);
+                    const float chk = o.x + o.y + o.z + od.x + od.y + od.z;
+                    const bool ok = ng_base < sc.n_nodes && isfinite(chk) && !(od.x == 0.0f && od.y == 0.0f && od.z == 0.0f);
+                    ng_bits = ok ? (1u | ((1u << flip) << 8)) : 0u;
+                }
+            } else if (want) {
                 const uint32_t bit = __ffs(tg_mask) - 1u;
                 n_tests++;
                 tg_mask &= tg_mask - 1u;
@@ -221,9 +278,11 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                     const int32_t prim = (int32_t)__float_as_uint(a.w);
                     float tt, b1, b2;
+                    const bool tie_wins = INST ? (cur_inst < h.inst || (cur_inst == h.inst && prim < h.prim))
+                                               : prim < h.prim;
                     if (hit_triangle(rt, xyz(a), xyz(b), xyz(c), tmin, h.t, &tt, &b1, &b2) &&
-                        (h.prim < 0 || tt < h.t || (tt == h.t && prim < h.prim))) {
-                        h.prim = prim; h.t = tt; h.b1 = b1; h.b2 = b2;
+                        (h.prim < 0 || tt < h.t || (tt == h.t && tie_wins))) {
+                        h.prim = prim; h.t = tt; h.b1 = b1; h.b2 = b2; h.inst = cur_inst;
                         if (ANY) { tg_mask = 0u; ng_bits = 0u; sp = 0; }
                     }
                 }
@@ -237,7 +296,15 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 active = false;
             } else {
                 const uint2 e = stack[--sp];
-                if (e.y & kTriGroupBit) { tg_base = e.x; tg_mask = e.y & 0x00FFFFFFu; ng_bits = 0u; }
+                if (INST && e.y == kLevelBit) {
+                    // back to the top level: the world-space ray
+                    const RayIn wr = load(ray_id);
+                    o = wr.o;
+                    set_dir(wr.d);
+                    in_blas = false;
+                    cur_inst = -1;
+                    ng_bits = 0u;
+                } else if (e.y & kTriGroupBit) { tg_base = e.x; tg_mask = e.y & 0x00FFFFFFu; ng_bits = 0u; }
                 else { ng_base = e.x; ng_bits = e.y; }
             }
         }

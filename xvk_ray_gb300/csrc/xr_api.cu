@@ -113,6 +113,7 @@ xr_status alloc_pixels(Context* c) {
         add((void**)&fa.nb_slot, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
     }
     add((void**)&fa.hits, N * 16);
+    add((void**)&fa.hit_inst, N * 4);
     add((void**)&fa.out_ldr, N * 4);
     if (P.write_hdr) add((void**)&fa.out_hdr, N * 16);
     for (int i = 0; i < 2; i++)
@@ -332,8 +333,6 @@ bad:
     return s;
 }
 
-static void free_lights(Context* c);
-
 void xr_destroy(XrContext* c) {
     if (!c) return;
     DeviceGuard g(c->device);
@@ -346,6 +345,7 @@ void xr_destroy(XrContext* c) {
     cudaFree(c->d_nodes); cudaFree(c->d_tris); cudaFree(c->d_counters); cudaFree(c->d_ubo); cudaFree(c->d_work);
     cudaFree(c->d_vuv); cudaFree(c->d_tex_info); cudaFree(c->d_texels);
     free_lights(c);
+    free_instances(c);
     if (c->h_ubo) cudaFreeHost(c->h_ubo);
     for (int i = 0; i < 8; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
@@ -353,7 +353,9 @@ void xr_destroy(XrContext* c) {
     delete c;
 }
 
-static void free_lights(Context* c) {
+}  // extern "C"
+
+void xr::free_lights(Context* c) {
     cudaFree(c->d_light_prim); cudaFree(c->d_light_cdf); cudaFree(c->d_light_pmf); cudaFree(c->d_prim_light_pdf);
     c->d_light_prim = nullptr; c->d_light_cdf = nullptr; c->d_light_pmf = nullptr; c->d_prim_light_pdf = nullptr;
     c->n_lights = 0;
@@ -363,8 +365,8 @@ static void free_lights(Context* c) {
 // area * luminance(4 * base colour) (the emission of shade_step), pmf = power /
 // total, inclusive CDF in primitive order with the last entry 1, and per
 // primitive pmf / area (the area-measure density of picking a point on it).
-static xr_status upload_lights(Context* c, const std::vector<uint4>& tri, const std::vector<float4>& pos,
-                        const XrMaterial* m, uint32_t nm) {
+xr_status xr::upload_lights(Context* c, const std::vector<uint4>& tri, const std::vector<float4>& pos,
+                            const XrMaterial* m, uint32_t nm) {
     std::vector<uint32_t> prim;
     std::vector<float> area, power;
     for (uint32_t i = 0; i < (uint32_t)tri.size(); i++) {
@@ -409,6 +411,8 @@ static xr_status upload_lights(Context* c, const std::vector<uint4>& tri, const 
     cudaMemcpy(c->d_prim_light_pdf, prim_pdf.data(), tri.size() * 4, cudaMemcpyHostToDevice);
     return XR_OK;
 }
+
+extern "C" {
 
 xr_status xr_upload_textures(XrContext* c, const XrTexture* t, uint32_t n) {
     if (!c || (n && !t)) return fail(c, XR_ERR_INVALID_ARGUMENT, "upload_textures: null argument");
@@ -481,10 +485,18 @@ xr_status xr_upload_scene(XrContext* c, const XrVertex* v, uint32_t nv, const ui
             return fail(c, XR_ERR_INVALID_ARGUMENT, "upload: non-finite vertex position");
     }
     cudaStreamSynchronize(c->stream);
+    free_instances(c);
+    c->parts.clear();
     cudaFree(c->d_tri_idx); cudaFree(c->d_vpos); cudaFree(c->d_vnrm); cudaFree(c->d_mats); cudaFree(c->d_vuv);
     c->d_tri_idx = nullptr; c->d_vpos = nullptr; c->d_vnrm = nullptr; c->d_mats = nullptr; c->d_vuv = nullptr;
     free_lights(c);
     c->scene_ready = false; c->bvh_ready = false;
+    for (int k = 0; k < 3; k++) { c->scene_lo[k] = nv ? INFINITY : 0.0f; c->scene_hi[k] = nv ? -INFINITY : 0.0f; }
+    for (uint32_t i = 0; i < nv; i++)
+        for (int k = 0; k < 3; k++) {
+            c->scene_lo[k] = std::min(c->scene_lo[k], v[i].pos[k]);
+            c->scene_hi[k] = std::max(c->scene_hi[k], v[i].pos[k]);
+        }
     xr_status s;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_tri_idx, std::max<size_t>(ntri, 1) * 16), "scene alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&c->d_vpos, std::max<size_t>(nv, 1) * 16), "scene alloc")) ||
@@ -519,6 +531,13 @@ xr_status xr_build_bvh(XrContext* c) {
     invalidate_graphs(c);
     xr_status s = build_bvh(c);
     if (s) return s;
+    ScenePart part;
+    part.nv = c->nv; part.ntri = c->ntri; part.nm = c->nm;
+    part.n_nodes = c->n_nodes; part.n_slots = c->n_tri_slots;
+    part.levels = c->bvh_levels;
+    part.emin = c->bvh_emin;
+    for (int k = 0; k < 3; k++) { part.lo[k] = c->scene_lo[k]; part.hi[k] = c->scene_hi[k]; }
+    c->parts.assign(1, part);
     DeviceScene& sc = c->fa.sc;
     sc.tri = c->d_tris; sc.nodes = c->d_nodes; sc.n_nodes = c->n_nodes;
     sc.tri_idx = c->d_tri_idx; sc.vpos = c->d_vpos; sc.vnrm = c->d_vnrm;
@@ -526,6 +545,7 @@ xr_status xr_build_bvh(XrContext* c) {
     sc.light_prim = c->d_light_prim; sc.light_cdf = c->d_light_cdf; sc.light_pmf = c->d_light_pmf;
     sc.prim_light_pdf = c->d_prim_light_pdf; sc.n_lights = c->n_lights;
     sc.vuv = c->d_vuv; sc.tex_info = c->d_tex_info; sc.texels = c->d_texels; sc.n_tex = c->n_tex;
+    if (!c->instances.empty()) return rebuild_tlas(c);   // the instances now refer to the new BVH
     return XR_OK;
 }
 
@@ -857,6 +877,10 @@ xr_status xr_get_stats(XrContext* c, XrStats* st) {
     }
     o.bvh_nodes = c->n_nodes; o.bvh_triangles = c->n_tri_slots; o.bvh_depth = c->bvh_depth;
     o.ms_bvh_build = c->ms_bvh;
+    o.instances = (uint32_t)c->instances.size();
+    o.tlas_nodes = c->n_tlas_nodes;
+    o.ms_tlas_build = c->ms_tlas;
+    o.ms_refit = c->ms_refit;
     if (c->query_rays) {
         unsigned long long w[2] = {0, 0};
         cudaMemcpy(w, c->d_work, sizeof(w), cudaMemcpyDeviceToHost);
@@ -951,8 +975,8 @@ xr_status xr_run_pass(XrContext* c, const XrUniformBufferObject* ubo, uint32_t p
     return xr_sync(c);
 }
 
-xr_status xr_trace_rays_device(XrContext* c, const float* d_rays, uint32_t n, int32_t any_hit, int32_t* d_prim,
-                               float* d_t, float* d_bary) {
+static xr_status trace_device(XrContext* c, const float* d_rays, uint32_t n, int32_t any_hit, int32_t* d_prim,
+                              int32_t* d_inst, float* d_t, float* d_bary) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "trace: null context");
     if (!c->bvh_ready) return fail(c, XR_ERR_STATE, "trace: build the BVH first");
     if (n && (!d_rays || !d_prim || !d_t || !d_bary)) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null array");
@@ -960,33 +984,51 @@ xr_status xr_trace_rays_device(XrContext* c, const float* d_rays, uint32_t n, in
     cudaMemsetAsync(c->d_counters + kCntFetchQuery, 0, 4, c->stream);
     cudaMemsetAsync(c->d_work, 0, 2 * sizeof(unsigned long long), c->stream);
     c->query_rays = n;
-    launch_trace(c->fa.sc, d_rays, n, any_hit, d_prim, d_t, d_bary, c->d_counters + kCntFetchQuery,
+    launch_trace(c->fa.sc, d_rays, n, any_hit, d_prim, d_inst, d_t, d_bary, c->d_counters + kCntFetchQuery,
                  c->d_counters + kCntError, c->d_work, c->sm_count, c->stream);
     return cuda_check(c, cudaGetLastError(), "trace launch");
 }
 
-xr_status xr_trace_rays(XrContext* c, const float* rays, uint32_t n, int32_t any_hit, int32_t* prim, float* t,
-                        float* bary) {
+xr_status xr_trace_rays_device(XrContext* c, const float* d_rays, uint32_t n, int32_t any_hit, int32_t* d_prim,
+                               float* d_t, float* d_bary) {
+    return trace_device(c, d_rays, n, any_hit, d_prim, nullptr, d_t, d_bary);
+}
+
+static xr_status trace_host(XrContext* c, const float* rays, uint32_t n, int32_t any_hit, int32_t* prim,
+                            int32_t* inst, float* t, float* bary) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "trace: null context");
     if (n == 0) return XR_OK;
     if (!rays || !prim || !t || !bary) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null array");
     DeviceGuard g(c->device);
-    float* dr = nullptr; int32_t* dp = nullptr; float* dt = nullptr; float* db = nullptr;
+    float* dr = nullptr; int32_t* dp = nullptr; int32_t* di = nullptr; float* dt = nullptr; float* db = nullptr;
     xr_status s = XR_OK;
     if ((s = cuda_check(c, cudaMalloc((void**)&dr, (size_t)n * 32), "trace alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&dp, (size_t)n * 4), "trace alloc")) ||
+        (inst && (s = cuda_check(c, cudaMalloc((void**)&di, (size_t)n * 4), "trace alloc"))) ||
         (s = cuda_check(c, cudaMalloc((void**)&dt, (size_t)n * 4), "trace alloc")) ||
         (s = cuda_check(c, cudaMalloc((void**)&db, (size_t)n * 8), "trace alloc")))
         goto out;
     cudaMemcpyAsync(dr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream);
-    if ((s = xr_trace_rays_device(c, dr, n, any_hit, dp, dt, db))) goto out;
+    if ((s = trace_device(c, dr, n, any_hit, dp, di, dt, db))) goto out;
     cudaMemcpyAsync(prim, dp, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (inst) cudaMemcpyAsync(inst, di, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(t, dt, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(bary, db, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream);
     s = xr_sync(c);
 out:
-    cudaFree(dr); cudaFree(dp); cudaFree(dt); cudaFree(db);
+    cudaFree(dr); cudaFree(dp); cudaFree(di); cudaFree(dt); cudaFree(db);
     return s;
+}
+
+xr_status xr_trace_rays(XrContext* c, const float* rays, uint32_t n, int32_t any_hit, int32_t* prim, float* t,
+                        float* bary) {
+    return trace_host(c, rays, n, any_hit, prim, nullptr, t, bary);
+}
+
+xr_status xr_trace_rays_instanced(XrContext* c, const float* rays, uint32_t n, int32_t any_hit, int32_t* prim,
+                                  int32_t* instance, float* t, float* bary) {
+    if (c && n && !instance) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null instance array");
+    return trace_host(c, rays, n, any_hit, prim, instance, t, bary);
 }
 
 xr_status xr_event_record(XrContext* c, uint32_t slot) {

@@ -93,6 +93,14 @@ struct DeviceScene {
     const uint4* tex_info;           // per texture {first texel, width, height, 0}
     const uint32_t* texels;          // RGBA8 texels of all textures, row 0 = v 0
     uint32_t n_tex;
+    // instances (xr_set_instances): a top-level BVH over the instances' world boxes
+    // whose leaves are instance records; `nodes` then holds the bottom-level BVHs
+    const WideNode* tlas_nodes;
+    uint32_t n_tlas_nodes;
+    const float4* inst_slots;        // 4 float4 per top-level leaf slot: world-to-object rows, {instance, root}
+    uint32_t n_inst_slots;
+    const float4* inst_xform;        // 6 float4 per instance: object-to-world rows, world-to-object rows
+    uint32_t n_inst;                 // 0: no instances
 };
 
 // One view of a multi-view context: its pixels are [pix_off, pix_off + W H) of the
@@ -135,6 +143,7 @@ struct FrameArgs {
     // wavefront
     float4* q_in[3]; float4* q_out[3];
     uint4* hits;              // closest-hit record per queue slot {prim, t, b1, b2}
+    int32_t* hit_inst;        // its instance (scenes with instances)
     uint2* shadow_q;          // corrected spatial pass: {pixel << 5 | slot, neighbour pixel}
     uint32_t* occ;            // per pixel: occluded neighbour slots
     uint2* nb_slot;           // corrected spatial pass, plane per slot: {neighbour pixel, target * Jacobian}
@@ -179,6 +188,36 @@ struct CacheState {
     bool frame_trained = false;
 };
 
+// One scene of a context: its ranges in the concatenated vertex, primitive,
+// material, node and triangle-slot arrays, the node ranges of its BVH levels
+// (relative to node_off), the finest grid exponent of its quantisation and the
+// bounds of its vertices.
+struct ScenePart {
+    uint32_t vert_off = 0, nv = 0, prim_off = 0, ntri = 0, mat_off = 0, nm = 0;
+    uint32_t node_off = 0, n_nodes = 0, slot_off = 0, n_slots = 0;
+    std::vector<uint32_t> levels;
+    int emin = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+// Input and output of a wide-BVH build (bvh_build.cu): triangles (tri_idx, vpos),
+// or boxes whose leaves copy a 4-float4 record per primitive (instances).
+struct WideBuild {
+    uint32_t n = 0;
+    const uint4* tri_idx = nullptr;
+    const float4* vpos = nullptr;
+    const float4* box_lo = nullptr;
+    const float4* box_hi = nullptr;
+    const float4* records = nullptr;
+    int emin_floor = -1000;             // lower bound of the finest grid exponent
+    WideNode* nodes = nullptr;          // device arrays owned by the caller afterwards
+    float4* slots = nullptr;
+    uint32_t n_nodes = 0, n_slots = 0, depth = 0;
+    int emin = 0;
+    std::vector<uint32_t> level_off;    // first node of each level, then the node count
+    float ms = 0.0f;
+};
+
 struct Context {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -213,6 +252,20 @@ struct Context {
     uint32_t n_nodes = 0, n_tri_slots = 0, bvh_depth = 0;
     bool bvh_ready = false;
     float ms_bvh = 0.0f;
+    std::vector<uint32_t> bvh_levels;   // build of a single scene: first node of each level, then the node count
+    int bvh_emin = 0;                   // its finest grid exponent
+    float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};   // bounds of the uploaded scene's vertices
+    // the scenes of the context (one after xr_upload_scene, n after xr_upload_scenes):
+    // ranges in the concatenated arrays, BVH levels for refit, vertex bounds
+    std::vector<ScenePart> parts;
+    // instances (xr_set_instances)
+    std::vector<XrInstance> instances;
+    std::vector<float> inst_xform_host;   // 24 floats per instance: object-to-world, world-to-object
+    float4* d_inst_xform = nullptr;
+    WideNode* d_tlas_nodes = nullptr;
+    float4* d_inst_slots = nullptr;
+    uint32_t n_tlas_nodes = 0, n_inst_slots = 0;
+    float ms_tlas = 0.0f, ms_refit = 0.0f;
 
     // per-pixel buffers
     uint32_t W = 0, H = 0, N = 0;
@@ -278,11 +331,22 @@ struct DeviceGuard {
 
 // ---- launch wrappers (bvh_build.cu) ----
 xr_status build_bvh(Context* ctx);
+xr_status build_wide(Context* ctx, WideBuild& wb);
+void launch_refit_slots(float4* tris, uint32_t first, uint32_t n, const uint4* tri_idx, const float4* vpos,
+                        cudaStream_t st);
+void launch_refit_level(WideNode* nodes, uint32_t first, uint32_t n, const float4* tris, float4* box_lo,
+                        float4* box_hi, int emin, cudaStream_t st);
+xr_status refit_part(Context* c, uint32_t part, int emin);   // instances.cu
+void free_lights(Context* c);
+xr_status upload_lights(Context* c, const std::vector<uint4>& tri, const std::vector<float4>& pos,
+                        const XrMaterial* m, uint32_t nm);
+xr_status rebuild_tlas(Context* c);                           // instances.cu
+void free_instances(Context* c);                              // instances.cu
 
 // ---- launch wrappers (trace.cu) ----
 // `fetch` must be zero when the launch starts (the kernel's ray-fetch counter).
-void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_hit, int32_t* prim, float* t,
-                  float* bary, uint32_t* fetch, uint32_t* flags, unsigned long long* work, int sm_count,
+void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_hit, int32_t* prim, int32_t* inst,
+                  float* t, float* bary, uint32_t* fetch, uint32_t* flags, unsigned long long* work, int sm_count,
                   cudaStream_t st);
 
 // ---- launch wrappers (restir.cu) ----
