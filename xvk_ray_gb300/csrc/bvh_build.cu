@@ -736,7 +736,7 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
         cudaMemsetAsync(flags, 0, (nint + 1) * 4, st);
         uint32_t root_ref = 0u;
         const char* builder = getenv("XR_BVH_BUILDER");
-        const bool use_lbvh = builder && strcmp(builder, "lbvh") == 0;
+        const bool use_lbvh = B.builder == 2 || (B.builder == 0 && builder && strcmp(builder, "lbvh") == 0);
         if (n == 1) {
             root_ref = 0u | kLeafBit;
         } else if (use_lbvh) {

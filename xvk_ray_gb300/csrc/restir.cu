@@ -31,6 +31,11 @@ constexpr int kBlock = 128;
 #ifndef XR_TRACE_MIN_BLOCKS
 #define XR_TRACE_MIN_BLOCKS 8
 #endif
+// The two-level variants (scenes with instances) keep more state per lane: 7 CTAs
+// per SM (72 registers) traverse without spills where 8 (64) spill.
+#ifndef XR_TRACE_MIN_BLOCKS_INST
+#define XR_TRACE_MIN_BLOCKS_INST 7
+#endif
 
 struct HitPayload {
     float3 pos, normal, geo;
@@ -518,7 +523,7 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 // With several scenes each ray starts at its view's root; a path whose pixel slot
 // holds a cache training record (pixel_is_record) finds its pixel in the record.
 template <bool INST>
-__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_paths(FrameArgs fa, const float4* __restrict__ q0,
+__global__ void __launch_bounds__(kBlock, INST ? XR_TRACE_MIN_BLOCKS_INST : XR_TRACE_MIN_BLOCKS) k_trace_paths(FrameArgs fa, const float4* __restrict__ q0,
                                                         const float4* __restrict__ q1, uint4* __restrict__ hits,
                                                         const uint32_t* count_ptr, uint32_t* next, uint32_t* err,
                                                         uint32_t* nonfinite, uint32_t pixel_is_record) {
@@ -1036,7 +1041,7 @@ __global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUn
 // (ReSTIRGISpatialReuse.rgen.hlsl:44-62 with the centre pixel's visible point as
 // origin); an occluded ray sets its slot's bit in the pixel's occlusion word.
 template <bool INST>
-__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_shadow(FrameArgs fa) {
+__global__ void __launch_bounds__(kBlock, INST ? XR_TRACE_MIN_BLOCKS_INST : XR_TRACE_MIN_BLOCKS) k_trace_shadow(FrameArgs fa) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[32];
     trace_persistent<true, INST>(
         fa.sc, count, &fa.counters[kCntFetchShadow],
@@ -1296,14 +1301,16 @@ uint32_t persistent_grid(int sm_count, bool compat) {
     return (uint32_t)(o * sm_count);
 }
 
-uint32_t trace_grid(int sm_count) {
-    static int occ = 0;
-    if (occ == 0) {
+uint32_t trace_grid(int sm_count, bool instances) {
+    static int occ[2] = {0, 0};
+    int& o = occ[instances ? 1 : 0];
+    if (o == 0) {
         int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<false>, kBlock, 0);
-        occ = v > 0 ? v : 4;
+        if (instances) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<true>, kBlock, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<false>, kBlock, 0);
+        o = v > 0 ? v : 4;
     }
-    return (uint32_t)(occ * sm_count);
+    return (uint32_t)(o * sm_count);
 }
 
 void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {

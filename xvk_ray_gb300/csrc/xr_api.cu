@@ -48,7 +48,7 @@ void invalidate_graphs(Context* c) {
 }
 
 uint32_t persistent_grid(int sm_count, bool compat);
-uint32_t trace_grid(int sm_count);
+uint32_t trace_grid(int sm_count, bool instances);
 
 namespace {
 
@@ -175,7 +175,7 @@ void set_frame_pointers(Context* c, uint32_t parity) {
     }
     fa.grid_persistent = c->tune_shade_ctas ? c->tune_shade_ctas * (uint32_t)c->sm_count
                                             : persistent_grid(c->sm_count, P.compat_reference != 0);
-    fa.grid_trace = c->tune_trace_ctas ? c->tune_trace_ctas * (uint32_t)c->sm_count : trace_grid(c->sm_count);
+    fa.grid_trace = c->tune_trace_ctas ? c->tune_trace_ctas * (uint32_t)c->sm_count : trace_grid(c->sm_count, !c->instances.empty());
 }
 
 // Host side of a frame's UBO upload: wait until the previous frame's transfer has
@@ -724,7 +724,7 @@ xr_status xr_autotune(XrContext* c, const XrUniformBufferObject* ubos, uint32_t 
     int occ_t = 0, occ_s = 0;
     {
         // the occupancy maxima are what grid 0 (the default) resolves to
-        const uint32_t t0 = trace_grid(c->sm_count), s0 = persistent_grid(c->sm_count, c->params.compat_reference != 0);
+        const uint32_t t0 = trace_grid(c->sm_count, !c->instances.empty()), s0 = persistent_grid(c->sm_count, c->params.compat_reference != 0);
         occ_t = (int)(t0 / (uint32_t)c->sm_count);
         occ_s = (int)(s0 / (uint32_t)c->sm_count);
     }

@@ -210,6 +210,7 @@ struct WideBuild {
     const float4* box_hi = nullptr;
     const float4* records = nullptr;
     int emin_floor = -1000;             // lower bound of the finest grid exponent
+    int builder = 0;                    // 0: XR_BVH_BUILDER (PLOC unless "lbvh"), 1: PLOC, 2: LBVH
     WideNode* nodes = nullptr;          // device arrays owned by the caller afterwards
     float4* slots = nullptr;
     uint32_t n_nodes = 0, n_slots = 0, depth = 0;
