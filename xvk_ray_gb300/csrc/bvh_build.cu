@@ -270,6 +270,7 @@ struct CollapseArgs {
     const uint32_t* sorted;           // sorted primitive ids
     const uint4* tri_idx; const float4* vpos;
     const float4* records;            // non-null: leaves copy 4 float4 per primitive from here (instances)
+    const uint8_t* dec;               // non-null: wide nodes follow the SAH decisions of k_sah_dp
     const uint32_t* task_in; const uint32_t* task_wide_in; uint32_t n_tasks;
     uint32_t* task_out; uint32_t* task_wide_out;
     uint32_t* counters;               // [0] wide nodes, [1] tri slots, [2] next task count
@@ -289,6 +290,92 @@ __device__ __forceinline__ int ceil_log2f(float v) {   // smallest e with 2^e >=
     int e;
     float m = frexpf(v, &e);                           // v = m 2^e, m in [0.5, 1)
     return (m == 0.5f) ? e - 1 : e;
+}
+
+// ---- SAH-optimal collapse (Ylitie, Karras and Laine, HPG 2017, section 3.2) ----
+// For every binary node n and every i in 1..8, cost(n, i) is the smallest SAH cost
+// of representing n's subtree by at most i children of a wide node:
+//   cost(n, 1) = min(leaf: A(n) ct count(n) if count(n) <= 3,
+//                    wide node: A(n) cn + min_{j=2..8} D(n, j)),
+//   cost(n, i) = min(cost(n, i - 1), D(n, i)),  D(n, i) = min_k cost(l, k) + cost(r, i - k);
+// a primitive costs A ct for every i.  Computed bottom-up (the second thread to
+// reach a node evaluates it); the decisions -- leaf or wide node, the best j, and
+// per i the split k (0: i - 1 children suffice) -- drive the top-down collapse.
+#ifndef XR_SAH_TRI
+#define XR_SAH_TRI 1.2f
+#endif
+constexpr float kSahNode = 1.0f, kSahTri = XR_SAH_TRI;
+constexpr uint32_t kDecStride = 16;   // bytes per binary node: [0] leaf?, [1] j*, [i] split of i (2..8)
+
+__global__ void k_parents(uint32_t nint, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                          uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nint) return;
+    const uint32_t lc = left[i], rc = right[i];
+    if (lc & kLeafBit) parent_leaf[lc & ~kLeafBit] = i; else parent_int[lc] = i;
+    if (rc & kLeafBit) parent_leaf[rc & ~kLeafBit] = i; else parent_int[rc] = i;
+}
+
+__device__ __forceinline__ void child_costs(uint32_t ref, const float* cost, const uint32_t* sorted, const float4* tlo,
+                                            const float4* thi, float c[9]) {
+    if (ref & kLeafBit) {
+        const uint32_t p = sorted[ref & ~kLeafBit];
+        const float4 lo = tlo[p], hi = thi[p];
+        const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+        const float v = (dx * dy + dy * dz + dz * dx) * kSahTri;
+        for (int i = 1; i <= 8; i++) c[i] = v;
+    } else {
+        for (int i = 1; i <= 8; i++) c[i] = __ldcg(cost + 8u * ref + (i - 1));
+    }
+}
+
+__global__ void k_sah_dp(int n, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                         const uint32_t* __restrict__ count, const uint32_t* __restrict__ parent_int,
+                         const uint32_t* __restrict__ parent_leaf, const uint32_t* __restrict__ sorted,
+                         const float4* __restrict__ tlo, const float4* __restrict__ thi, const float4* __restrict__ nlo,
+                         const float4* __restrict__ nhi, float* cost, uint8_t* __restrict__ dec, uint32_t* flags) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t node = parent_leaf[j];
+    for (int guard = 0; node != kInvalid; guard++) {
+        if (guard >= n || node >= (uint32_t)(n - 1)) { atomicOr(&flags[n - 1], 1u); return; }
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0u) return;   // the sibling's thread evaluates it
+        __threadfence();
+        float cl[9], cr[9];
+        child_costs(left[node], cost, sorted, tlo, thi, cl);
+        child_costs(right[node], cost, sorted, tlo, thi, cr);
+        float D[9];
+        uint8_t ks[9];
+        for (int i = 2; i <= 8; i++) {
+            D[i] = INFINITY;
+            ks[i] = 1;
+            for (int k = 1; k < i; k++) {
+                const float v = cl[k] + cr[i - k];
+                if (v < D[i]) { D[i] = v; ks[i] = (uint8_t)k; }
+            }
+        }
+        int jstar = 2;
+        for (int i = 3; i <= 8; i++)
+            if (D[i] < D[jstar]) jstar = i;
+        const float4 lo = __ldcg(nlo + node), hi = __ldcg(nhi + node);
+        const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+        const float A = dx * dy + dy * dz + dz * dx;
+        const uint32_t cnt = count[node];
+        const float c_leaf = cnt <= 3u ? A * kSahTri * (float)cnt : INFINITY;
+        const float c_int = A * kSahNode + D[jstar];
+        uint8_t* d = dec + (size_t)kDecStride * node;
+        float c = fminf(c_leaf, c_int);
+        d[0] = c_leaf <= c_int ? 1u : 0u;
+        d[1] = (uint8_t)jstar;
+        __stcg(cost + 8u * node, c);
+        for (int i = 2; i <= 8; i++) {
+            if (D[i] < c) { c = D[i]; d[i] = ks[i]; }
+            else d[i] = 0u;
+            __stcg(cost + 8u * node + (i - 1), c);
+        }
+        node = parent_int[node];
+    }
 }
 
 // Quantisation grid of a node over its box: p = lo - one cell, cells of 2^e per
@@ -334,6 +421,28 @@ __global__ void k_collapse(CollapseArgs a) {
     int nc = 0;
     if (bref & kLeafBit) {
         refs[nc++] = bref;
+    } else if (a.dec) {
+        // the children the SAH decisions give: expand (node, slots) pairs depth first
+        uint32_t sx[8], si[8];
+        int ssp = 0;
+        sx[ssp] = bref; si[ssp] = a.dec[(size_t)kDecStride * bref + 1]; ssp++;
+        while (ssp > 0) {
+            ssp--;
+            const uint32_t x = sx[ssp], i = si[ssp];
+            if ((x & kLeafBit) || i <= 1u) {
+                if (nc < 8) refs[nc++] = x;
+                else atomicOr(&a.counters[3], 4u);
+                continue;
+            }
+            const uint32_t k = a.dec[(size_t)kDecStride * x + i];
+            if (k == 0u) { sx[ssp] = x; si[ssp] = i - 1u; ssp++; }
+            else if (ssp + 2 <= 8) {
+                sx[ssp] = a.right[x]; si[ssp] = i - k; ssp++;
+                sx[ssp] = a.left[x]; si[ssp] = k; ssp++;
+            } else {
+                atomicOr(&a.counters[3], 4u);
+            }
+        }
     } else {
         refs[nc++] = a.left[bref];
         refs[nc++] = a.right[bref];
@@ -543,7 +652,10 @@ __global__ void k_refit_level(WideNode* __restrict__ nodes, uint32_t first, uint
 // globally best pair is always mutual and every round merges), mutual pairs
 // merge into a new internal node at the lower position, the array is
 // compacted, and rounds repeat until one cluster is left.
-constexpr int kPlocRadius = 16;
+#ifndef XR_PLOC_RADIUS
+#define XR_PLOC_RADIUS 64
+#endif
+constexpr int kPlocRadius = XR_PLOC_RADIUS;
 constexpr int kPlocBlock = 256;
 
 __global__ void k_ploc_init(uint32_t n, const uint32_t* __restrict__ sorted, const float4* __restrict__ tlo,
@@ -694,6 +806,9 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
     uint32_t* range = nullptr;   // primitives below each binary internal node
     uint32_t *ta = nullptr, *tb = nullptr, *wa = nullptr, *wb = nullptr, *counters = nullptr;
     WideNode* nodes_tmp = nullptr;
+    float* sah_cost = nullptr;     // SAH collapse: 8 costs and kDecStride decision bytes per binary node
+    uint8_t* sah_dec = nullptr;
+    uint32_t* sah_flags = nullptr;
     xr_status s = XR_OK;
     const uint32_t nint = n > 1 ? n - 1 : 1;
     const uint32_t chunk = 4096;
@@ -782,6 +897,18 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
             cudaFree(clo0); cudaFree(chi0); cudaFree(clo1); cudaFree(chi1);
             if (s) goto done;
         }
+        // SAH decisions for the collapse (XR_BVH_COLLAPSE=greedy: the area-greedy widening)
+        const char* coll = getenv("XR_BVH_COLLAPSE");
+        const bool sah = n > 1 && !(coll && strcmp(coll, "greedy") == 0);
+        if (sah) {
+            if ((s = dalloc(ctx, &sah_cost, 8 * (size_t)nint)) || (s = dalloc(ctx, &sah_dec, kDecStride * (size_t)nint)) ||
+                (s = dalloc(ctx, &sah_flags, nint + 1)))
+                goto done;
+            if (!use_lbvh) k_parents<<<(nint + 255) / 256, 256, 0, st>>>(nint, left, right, pint, pleaf);
+            cudaMemsetAsync(sah_flags, 0, (nint + 1) * 4, st);
+            k_sah_dp<<<(n + 255) / 256, 256, 0, st>>>((int)n, left, right, range, pint, pleaf, v0, tlo, thi, nlo, nhi,
+                                                      sah_cost, sah_dec, sah_flags);
+        }
         uint32_t cinit[4] = {1u, 0u, 0u, 0u};
         cudaMemcpyAsync(counters, cinit, sizeof(cinit), cudaMemcpyHostToDevice, st);
         uint32_t zero = 0u;
@@ -794,6 +921,7 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
             CollapseArgs ca;
             ca.left = left; ca.right = right; ca.count = range; ca.nlo = nlo; ca.nhi = nhi; ca.tlo = tlo; ca.thi = thi;
             ca.sorted = v0; ca.tri_idx = B.tri_idx; ca.vpos = B.vpos; ca.records = B.records;
+            ca.dec = sah ? sah_dec : nullptr;
             ca.task_in = ta; ca.task_wide_in = wa; ca.n_tasks = ntask; ca.task_out = tb; ca.task_wide_out = wb;
             ca.counters = counters; ca.nodes = nodes_tmp; ca.tris = B.slots; ca.emin = emin;
             ca.max_nodes = nint; ca.n_prims = n;
@@ -810,9 +938,11 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
             depth++;
             if (depth > 200) { s = fail(ctx, XR_ERR_OVERFLOW, "bvh: collapse did not terminate"); goto done; }
         }
-        uint32_t ch[4], bflag = 0;
+        uint32_t ch[4], bflag = 0, dflag = 0;
         cudaMemcpy(ch, counters, sizeof(ch), cudaMemcpyDeviceToHost);
         cudaMemcpy(&bflag, flags + nint, 4, cudaMemcpyDeviceToHost);
+        if (sah) cudaMemcpy(&dflag, sah_flags + nint, 4, cudaMemcpyDeviceToHost);
+        bflag |= dflag;
         if (ch[3] || bflag) { s = fail(ctx, XR_ERR_STATE, "bvh: inconsistent radix tree"); goto done; }
         if (ch[1] != n) { s = fail(ctx, XR_ERR_STATE, "bvh: triangle slots do not match the primitive count"); goto done; }
         if ((s = dalloc(ctx, &B.nodes, ch[0]))) goto done;
@@ -829,6 +959,7 @@ done:
     cudaFree(hist); cudaFree(left); cudaFree(right); cudaFree(pint); cudaFree(pleaf); cudaFree(flags);
     cudaFree(range); cudaFree(nlo); cudaFree(nhi); cudaFree(ta); cudaFree(tb); cudaFree(wa); cudaFree(wb);
     cudaFree(counters); cudaFree(nodes_tmp);
+    cudaFree(sah_cost); cudaFree(sah_dec); cudaFree(sah_flags);
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     if (s != XR_OK) {
         cudaFree(B.slots); B.slots = nullptr;
