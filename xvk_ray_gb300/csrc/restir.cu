@@ -601,19 +601,23 @@ __device__ __forceinline__ void res_init(Res& r) {
     r.code = 0u; r.w_sum = 0.0f; r.W = 0.0f; r.m = 0u;
 }
 // UpdateReservoir (ReSTIRGICommon.hlsl:52-61): candidate fields passed by value
-__device__ __forceinline__ void res_update(Res& r, const Res& cand, float w_new, uint32_t& seed) {
+// Returns whether the candidate replaced the reservoir's sample.
+__device__ __forceinline__ bool res_update(Res& r, const Res& cand, float w_new, uint32_t& seed) {
     r.w_sum += w_new;
     r.m++;
     if (random_float(seed) < w_new / fmaxf(1e-10f, r.w_sum)) {
         r.xs = cand.xs; r.L = cand.L; r.ns = cand.ns; r.f = cand.f; r.code = cand.code;
+        return true;
     }
+    return false;
 }
 // MergeReservoir (ReSTIRGICommon.hlsl:63-73)
-__device__ __forceinline__ void res_merge(Res& t, const Res& src, float p_hat, uint32_t& seed) {
+__device__ __forceinline__ bool res_merge(Res& t, const Res& src, float p_hat, uint32_t& seed) {
     uint32_t M0 = t.m;
     float w_new = p_hat * src.W * (float)src.m;
-    res_update(t, src, w_new, seed);
+    const bool took = res_update(t, src, w_new, seed);
     t.m = M0 + src.m;
+    return took;
 }
 // ReSTIRGITemporalReuse.rgen.hlsl:33-40
 __device__ __forceinline__ float eval_target(float3 xs, float3 L, float3 x_curr, float3 n_curr) {
@@ -866,6 +870,35 @@ __device__ __forceinline__ float target_corrected(const PixelShading& P, float3 
 // differs slightly from the sampled one (the path left from a point offset
 // along the normal), and in a lobe that sharp f alone changes by orders of
 // magnitude over that angle while the ratio stays bounded.
+// The final target of a reservoir's sample and its shading from one BSDF
+// evaluation: target_corrected and shade_corrected evaluate the same lobe at the
+// same direction, so the results are theirs bit for bit.  `tp_known` >= 0 is the
+// target when the caller already has it (the selected candidate's), else < 0.
+__device__ __forceinline__ float3 finish_corrected(const PixelShading& P, Res& r, float tp_known, uint32_t m_cap,
+                                                   bool shade) {
+    const float3 wi = normalize(r.xs - P.x);
+    const float c = dot(P.n, wi);
+    Lobe lb;
+    lb.f = f3(0, 0, 0);
+    lb.pdf = 0.0f;
+    const bool front = c > 0.0f;
+    if (front && (tp_known < 0.0f || shade))
+        lb = eval_material(P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n));
+    const float tpf = tp_known >= 0.0f ? tp_known : (front ? length(r.L * lb.f * c) : 0.0f);
+    if (r.m > m_cap) {
+        r.w_sum *= (float)m_cap / (float)r.m;
+        r.m = m_cap;
+    }
+    r.W = (tpf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * tpf) : 0.0f;
+    float3 col = f3(0, 0, 0);
+    if (shade && r.W > 0.0f) {
+        const float ct = fmaxf(0.0f, c);
+        if (P.reuse) col = r.L * r.W * lb.f * ct;
+        else if (lb.pdf > 0.0f) col = r.L * lb.f * (ct / lb.pdf);
+    }
+    return col;
+}
+
 __device__ __forceinline__ float3 shade_corrected(const PixelShading& P, const Res& r) {
     float3 c = f3(0, 0, 0);
     if (r.W > 0.0f) {
@@ -942,23 +975,19 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
         }
     }
     Res r; res_init(r);
-    float tp_new = target_corrected(P, s_new.xs, s_new.L);
+    const float tp_new = target_corrected(P, s_new.xs, s_new.L);
     float w_new = (a.w > 1e-6f) ? (tp_new / a.w) : 0.0f;
-    res_update(r, s_new, w_new, rng);
+    // the target of the sample the reservoir ends with, when it is one already evaluated
+    float tp_sel = res_update(r, s_new, w_new, rng) ? tp_new : -1.0f;
     if (found) {
-        float tp_prev = target_corrected(P, r_prev.xs, r_prev.L);
-        res_merge(r, r_prev, tp_prev, rng);
+        const float tp_prev = target_corrected(P, r_prev.xs, r_prev.L);
+        if (res_merge(r, r_prev, tp_prev, rng)) tp_sel = tp_prev;
     } else {
         r.m = 1u;
     }
-    if (r.m > fa.m_cap_t) {
-        r.w_sum *= (float)fa.m_cap_t / (float)r.m;
-        r.m = fa.m_cap_t;
-    }
-    float tpf = target_corrected(P, r.xs, r.L);
-    r.W = (tpf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * tpf) : 0.0f;
+    const float3 col = finish_corrected(P, r, tp_sel, fa.m_cap_t, out_here);
     store_packed(fa.rt_cur0, fa.rt_cur1, p, r);
-    if (out_here) write_out(fa, p, shade_corrected(P, r), true);
+    if (out_here) write_out(fa, p, col, true);
 }
 
 // Spatial reuse, step 1 of 3 (corrected mode): picks each pixel's neighbours,
@@ -1125,7 +1154,8 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
     const uint32_t nn = P.reuse ? fa.n_nb : 0u;   // the neighbours k_spatial_select picked and tested
     rng_skip(rng, 2u * nn);                         // the merges draw after the picks
     Res r; res_init(r);
-    res_merge(r, center, target_corrected(P, center.xs, center.L), rng);
+    const float tp_center = target_corrected(P, center.xs, center.L);
+    float tp_sel = res_merge(r, center, tp_center, rng) ? tp_center : -1.0f;
     for (uint32_t i = 0; i < nn; i++) {
         const uint2 slot = fa.nb_slot[(size_t)i * fa.N + p];
         if (slot.x == kInvalid) continue;   // not similar: no merge, no draw
@@ -1134,20 +1164,15 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
         float ph = __uint_as_float(slot.y);
         const bool occluded = ph > 0.0f && ((occ >> i) & 1u);
         if (occluded) ph = 0.0f;
-        res_merge(r, rn, ph, rng);
+        if (res_merge(r, rn, ph, rng)) tp_sel = -1.0f;   // a neighbour's sample: its target is re-evaluated
         // every similar neighbour counts towards M (1/M normalisation) except one
         // whose sample is occluded; the reference also drops zero-weight neighbours
         // (ReSTIRGISpatialReuse.rgen.hlsl:140-143), which biases the estimate upwards
         if (occluded) r.m -= rn.m;
     }
-    if (r.m > fa.m_cap_s) {
-        r.w_sum *= (float)fa.m_cap_s / (float)r.m;
-        r.m = fa.m_cap_s;
-    }
-    float phf = target_corrected(P, r.xs, r.L);
-    r.W = (phf > 1e-6f && r.m > 0u) ? r.w_sum / ((float)r.m * phf) : 0.0f;
+    const float3 col = finish_corrected(P, r, tp_sel, fa.m_cap_s, true);
     store_packed(fa.rs0, fa.rs1, p, r);
-    write_out(fa, p, shade_corrected(P, r), true);
+    write_out(fa, p, col, true);
 }
 
 // ---------------------------------------------------------------------------
