@@ -402,6 +402,32 @@ __device__ __forceinline__ void push_path(const FrameArgs& fa, bool alive, const
     }
 }
 
+// push_path for every thread of a block at once (all threads of the block call
+// it): one atomic per block instead of one per warp -- appends from all warps of
+// the grid go to the same counter, whose atomics serialise.
+template <int BLOCK>
+__device__ __forceinline__ void push_path_block(const FrameArgs& fa, bool alive, const PathState& s, uint32_t qslot) {
+    constexpr int kWarps = BLOCK / 32;
+    __shared__ uint32_t warp_base[kWarps + 1];
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, alive);
+    if (lane == 0u) warp_base[warp] = (uint32_t)__popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0u) {
+        uint32_t run = 0u;
+        for (int w = 0; w < kWarps; w++) { const uint32_t c = warp_base[w]; warp_base[w] = run; run += c; }
+        warp_base[kWarps] = run ? atomicAdd(&fa.counters[qslot], run) : 0u;
+    }
+    __syncthreads();
+    if (alive) {
+        const uint32_t i = warp_base[kWarps] + warp_base[warp] + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+        fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
+        fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
+        fa.q_out[2][i] = f4(s.thr, s.pq);
+    }
+    __syncthreads();   // warp_base is reused by the next call
+}
+
 // Radiance-cache records of bounce 1 (all lanes of the warp call this): one
 // query per surface x_s, appended with one atomic per warp; training pixels also
 // take a training record (target zero, filled by the rest of the path) and keep
@@ -493,8 +519,9 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
     }
     const XrUniformBufferObject* __restrict__ u = ubos + v;
     const uint32_t tiles_x = (VW + 15u) / 16u;
-    const uint32_t x = (lt % tiles_x) * 16u + (threadIdx.x & 15u);
-    const uint32_t y = (lt / tiles_x) * 8u + (threadIdx.x >> 4);
+    const uint32_t tx = lt % tiles_x, ty = lt / tiles_x;
+    const uint32_t x = tx * 16u + (threadIdx.x & 15u);
+    const uint32_t y = ty * 8u + (threadIdx.x >> 4);
     const bool inside = x < VW && y < VH;
     PathState s;
     bool alive = false;
@@ -515,7 +542,17 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
         if (nb == 0u) write_invalid<COMPAT>(fa, s.pixel, f3(0, 0, 0), f3(0, 0, 0), f3(0, 0, 0));
         else alive = true;
     }
-    push_path(fa, alive, s, 0u);
+    // Every pixel starts a path, so its queue slot is its index in tile order: the
+    // view's first pixel, the full tile rows above (only the last can be short),
+    // the tiles to the left in this row, the position inside the (possibly cut) tile.
+    if (alive) {
+        const uint32_t rows = min(8u, VH - ty * 8u), cols = min(16u, VW - tx * 16u);
+        const uint32_t i = base + ty * 8u * VW + tx * 16u * rows + (threadIdx.x >> 4) * cols + (threadIdx.x & 15u);
+        fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
+        fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
+        fa.q_out[2][i] = f4(s.thr, s.pq);
+    }
+    if (blockIdx.x == 0u && threadIdx.x == 0u) fa.counters[0] = nb ? fa.N : 0u;   // the paths of bounce 0
 }
 
 // Closest hits of the paths of one bounce (TMin 1e-4, TMax 1e4,
@@ -583,7 +620,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformB
         }
         if (!COMPAT && fa.cache_on && bounce == 1u) alive = cache_emit(fa, ce, alive, s);
         if (!COMPAT && fa.cache_on && bounce >= 2u) push_nee(fa, ce.nee.valid, ce.nee, s.pixel);
-        push_path(fa, alive, s, bounce + 1u);
+        push_path_block<kBlock>(fa, alive, s, bounce + 1u);
     }
 }
 
