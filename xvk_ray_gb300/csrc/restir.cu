@@ -677,18 +677,21 @@ __device__ __forceinline__ void store_wide(float4* const* planes, uint32_t i, co
     planes[2][i] = f4(r.ns, __uint_as_float(r.m));
     planes[3][i] = f4(r.f, 0.0f);
 }
-__device__ __forceinline__ void decode_packed(float4 a, float4 b, Res& r) {
+// with_normal = false leaves ns zero: the passes that never read the sample normal
+// (temporal; resolve, whose Jacobians were evaluated by select) skip its decode.
+__device__ __forceinline__ void decode_packed(float4 a, float4 b, Res& r, bool with_normal = true) {
     uint32_t w = __float_as_uint(b.w);
     r.xs = xyz(a); r.W = a.w;
     r.L = xyz(b);
     r.code = w & 0x00FFFFFFu;
     r.m = w >> 24;
-    r.ns = oct_decode(r.code, 12);
+    r.ns = with_normal ? oct_decode(r.code, 12) : f3(0, 0, 0);
     r.f = f3(0, 0, 0);
     r.w_sum = 0.0f;
 }
-__device__ __forceinline__ void load_packed(const float4* p0, const float4* p1, uint32_t i, Res& r) {
-    decode_packed(p0[i], p1[i], r);
+__device__ __forceinline__ void load_packed(const float4* p0, const float4* p1, uint32_t i, Res& r,
+                                            bool with_normal = true) {
+    decode_packed(p0[i], p1[i], r, with_normal);
 }
 __device__ __forceinline__ void store_packed(float4* p0, float4* p1, uint32_t i, const Res& r) {
     p0[i] = f4(r.xs, r.W);
@@ -980,7 +983,7 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     const float3 x_view = xyz(g);
     const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
     Res s_new;
-    s_new.xs = xyz(a); s_new.L = xyz(b); s_new.code = bw & 0x00FFFFFFu; s_new.ns = oct_decode(s_new.code, 12);
+    s_new.xs = xyz(a); s_new.L = xyz(b); s_new.code = bw & 0x00FFFFFFu; s_new.ns = f3(0, 0, 0);   // travels as its code
     s_new.f = f3(0, 0, 0);
     // Reprojection first, and every previous-frame word of the reprojected pixel
     // gathered at once (material, position, reservoir): one memory round trip
@@ -1007,7 +1010,7 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
         float3 pn = oct_decode(__float_as_uint(pg.w), 16);
         float3 dd = x_view - xyz(pg);
         if (!(dot(n_view, pn) < 0.8f) && !(dot(dd, dd) > 0.1f)) {
-            decode_packed(rp0, rp1, r_prev);
+            decode_packed(rp0, rp1, r_prev, false);
             found = true;
         }
     }
@@ -1187,7 +1190,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
     const float3 n_view = oct_decode(__float_as_uint(g.w), 16);
     const uint32_t occ = fa.visibility ? fa.occ[p] : 0u;
     const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat, p);
-    Res center; load_packed(fa.rt_cur0, fa.rt_cur1, p, center);
+    Res center; load_packed(fa.rt_cur0, fa.rt_cur1, p, center, false);
     const uint32_t nn = P.reuse ? fa.n_nb : 0u;   // the neighbours k_spatial_select picked and tested
     rng_skip(rng, 2u * nn);                         // the merges draw after the picks
     Res r; res_init(r);
@@ -1197,7 +1200,7 @@ __global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrU
         const uint2 slot = fa.nb_slot[(size_t)i * fa.N + p];
         if (slot.x == kInvalid) continue;   // not similar: no merge, no draw
         Res rn;
-        load_packed(fa.rt_cur0, fa.rt_cur1, slot.x, rn);
+        load_packed(fa.rt_cur0, fa.rt_cur1, slot.x, rn, false);
         float ph = __uint_as_float(slot.y);
         const bool occluded = ph > 0.0f && ((occ >> i) & 1u);
         if (occluded) ph = 0.0f;
