@@ -143,3 +143,94 @@ def test_instance_errors():
         assert r.stats().instances == 0
         p, inst, t, _ = r.trace_instanced(random_rays(np.random.default_rng(0), 100, -3, 3))
         assert np.all(inst == -1)
+
+
+def test_instanced_views_match_single_views():
+    """With instances set every view renders the instanced world; each view of a
+    two-view frame is bit-identical to rendering it alone."""
+    scenes = _scenes(13)
+    inst = _instances(0.0)
+    cam = xr._lib.XrCamera()
+    cam.position[:] = [0.0, 1.0, 12.0]
+    cam.yaw_deg, cam.pitch_deg, cam.fov_deg = 0.0, -5.0, 60.0
+    base = xr.Scene(scenes[0].vertices, scenes[0].indices, scenes[0].materials, scenes[0].ranges, cam)
+    views = [(0, 64, 48), (1, 40, 56)]
+
+    def mover(dyaw):
+        def f(frame, c):
+            c.yaw_deg += dyaw
+        return f
+
+    seqs = [camera_sequence(base, w, h, 3, 4, move=mover(0.3 * (k + 1))) for k, (_, w, h) in enumerate(views)]
+    alone = []
+    for k, (_, w, h) in enumerate(views):
+        with xr.Renderer(w, h) as r:
+            r.set_params(xr.params_default(w, h, write_hdr=1))
+            r.upload_scenes(list(scenes))
+            r.set_instances(inst)
+            for u in seqs[k]:
+                r.render(u)
+            alone.append(r.read_output(XR.XR_OUT_HDR).copy())
+    r = xr.Renderer(8, 8)
+    r.upload_scenes(list(scenes))
+    r.set_views(views, xr.params_default(8, 8, write_hdr=1))
+    r.set_instances(inst)
+    for f in range(3):
+        r.render_views([seqs[v][f] for v in range(len(views))])
+    for k in range(len(views)):
+        got = r.read_view_output(k, XR.XR_OUT_HDR)
+        assert np.array_equal(got.view(np.uint32), alone[k].view(np.uint32)), f"view {k}"
+    r.close()
+
+
+def test_frames_across_a_refit_match_oracle():
+    """Frames before and after new vertex positions (the temporal pass reprojecting
+    across the change) against the oracle rebuilt on the moved geometry."""
+    rng = np.random.default_rng(21)
+    scene = box_scene(rng, 24, 3.0)
+    W, H = 80, 60
+    cam = xr._lib.XrCamera()
+    cam.position[:] = [0.0, 0.5, 10.0]
+    cam.yaw_deg, cam.pitch_deg, cam.fov_deg = 0.0, -3.0, 60.0
+    view = xr.Scene(scene.vertices, scene.indices, scene.materials, scene.ranges, cam)
+    ubos = camera_sequence(view, W, H, 5, 4)
+    p = xr.params_default(W, H, write_hdr=1, write_pt=1)
+    world = ob.OracleWorld([ob.OracleScene.from_scene(scene)])   # no instances: traced as one scene
+    o = ob.OracleRenderer(world, p)
+    moved = scene.vertices.copy()
+    moved[:, 1] += 0.2 * np.sin(0.9 * moved[:, 0])
+    with xr.Renderer(W, H) as r:
+        r.set_params(p)
+        r.upload_scene(scene)
+        r.build_bvh()
+        for f, u in enumerate(ubos):
+            if f == 2:
+                r.update_vertices(0, moved)
+                world.update_vertices(0, moved)
+            r.render(u)
+            o.render(u)
+            _compare_frame(r, o, False, f"frame {f}")
+
+
+def test_instances_of_empty_and_one_triangle_scenes():
+    rng = np.random.default_rng(17)
+    boxes = box_scene(rng, 8, 2.0)
+    tri = xr.Scene(np.array([[-1, -1, 0, 0, 0, 1, 0, 0, 0], [1, -1, 0, 0, 0, 1, 0, 0, 0],
+                             [0, 1, 0, 0, 0, 1, 0, 0, 0]], np.float32),
+                   np.array([0, 1, 2], np.uint32), boxes.materials[:1].copy(), np.zeros((1, 2), np.uint32),
+                   boxes.camera)
+    empty = xr.Scene(np.zeros((0, 9), np.float32), np.zeros(0, np.uint32), boxes.materials[:1].copy(),
+                     np.zeros((1, 2), np.uint32), boxes.camera)
+    scenes = [boxes, tri, empty]
+    inst = [(0, affine(np.eye(3), [0, 0, 0])), (1, affine(rotation([0, 1, 0], 40) * 2.0, [3.0, 0.0, 1.0])),
+            (2, affine(np.eye(3), [0.0, 5.0, 0.0])), (1, affine(np.eye(3), [-3.0, 1.0, -1.0]))]
+    world = _world(scenes, inst)
+    rays = random_rays(np.random.default_rng(3), 20000, -6.0, 6.0)
+    with xr.Renderer(32, 32) as r:
+        r.upload_scenes(scenes)
+        r.set_instances(inst)
+        g = r.trace_instanced(rays)
+        c = world.trace_instanced(rays)
+        assert np.any(c[1] == 1) and np.any(c[1] == 3)   # the one-triangle instances are hit
+        for name, x, y in zip(("prim", "instance", "t", "bary"), g, c):
+            assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32)), name
