@@ -123,7 +123,8 @@ typedef struct XrStats {
     float ms_initial, ms_temporal, ms_spatial, ms_frame;   /* last frame, CUDA events */
     uint64_t rays_traced;        /* closest-hit rays of the last frame */
     uint64_t shadow_rays;        /* any-hit rays of the last frame */
-    uint32_t bvh_nodes, bvh_triangles, bvh_depth;
+    uint32_t bvh_nodes, bvh_triangles, bvh_depth;   /* bvh_triangles: leaf slots (>= triangles: split
+                                                       large triangles are referenced by several pieces) */
     float ms_bvh_build;
     uint64_t query_rays;         /* rays of the last xr_trace_rays call */
     uint64_t query_node_visits;  /* BVH nodes visited by those rays */

@@ -82,7 +82,7 @@ def test_procedural_hits_bit_exact(n_objects, builder, monkeypatch):
     osc = ob.OracleScene.from_scene(scene)
     op, ot, obary = osc.trace(rays)
     assert st.error_flags == 0
-    assert st.bvh_triangles == scene.n_triangles
+    assert st.bvh_triangles >= scene.n_triangles   # slots: large triangles are split into pieces
     assert np.array_equal(gp, op)
     hit = op >= 0
     assert np.array_equal(gt[hit].view(np.uint32), ot[hit].view(np.uint32))

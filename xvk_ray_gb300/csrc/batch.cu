@@ -173,7 +173,7 @@ extern "C" xr_status xr_upload_scenes(XrContext* c, const XrSceneData* scenes, u
     DeviceScene& sc = c->fa.sc;
     sc.tri = c->d_tris; sc.nodes = c->d_nodes; sc.n_nodes = c->n_nodes;
     sc.tri_idx = c->d_tri_idx; sc.vpos = c->d_vpos; sc.vnrm = c->d_vnrm;
-    sc.mats = c->d_mats; sc.n_mats = c->nm; sc.ntri = c->ntri;
+    sc.mats = c->d_mats; sc.n_mats = c->nm; sc.ntri = c->ntri; sc.n_tri_slots = c->n_tri_slots;
     sc.light_prim = c->d_light_prim; sc.light_cdf = c->d_light_cdf; sc.light_pmf = c->d_light_pmf;
     sc.prim_light_pdf = c->d_prim_light_pdf; sc.n_lights = c->n_lights;
     sc.vuv = c->d_vuv; sc.tex_info = c->d_tex_info; sc.texels = c->d_texels; sc.n_tex = c->n_tex;

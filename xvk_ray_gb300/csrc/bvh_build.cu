@@ -271,6 +271,7 @@ struct CollapseArgs {
     const uint4* tri_idx; const float4* vpos;
     const float4* records;            // non-null: leaves copy 4 float4 per primitive from here (instances)
     const uint8_t* dec;               // non-null: wide nodes follow the SAH decisions of k_sah_dp
+    const uint32_t* ref_prim;         // non-null: primitives are triangle pieces; the triangle of each
     const uint32_t* task_in; const uint32_t* task_wide_in; uint32_t n_tasks;
     uint32_t* task_out; uint32_t* task_wide_out;
     uint32_t* counters;               // [0] wide nodes, [1] tri slots, [2] next task count
@@ -561,6 +562,7 @@ __global__ void k_collapse(CollapseArgs a) {
                     for (int w = 0; w < 4; w++) dst[w] = a.records[4u * prim + w];
                     continue;
                 }
+                if (a.ref_prim) prim = a.ref_prim[prim];
                 uint4 id = a.tri_idx[prim];
                 float4 v0 = a.vpos[id.x], v1 = a.vpos[id.y], v2 = a.vpos[id.z];
                 float4* dst = a.tris + 3u * (tri_base + off + j);
@@ -643,6 +645,113 @@ __global__ void k_refit_level(WideNode* __restrict__ nodes, uint32_t first, uint
     nd.exyz_imask = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
     pack_q(ql, qh, nd.q);
     nodes[w] = nd;
+}
+
+// ---- early split clipping (Ernst and Greiner, "Early Split Clipping for Bounding
+// Volume Hierarchies", RT 2007) ----
+// A triangle whose box diagonal exceeds kEscMult times the mean is referenced by
+// several pieces: its box is halved at the midpoint of the longest axis, the
+// triangle clipped to each half (Sutherland-Hodgman against the one new plane; the
+// crossing point of an edge is computed once per edge, so both halves share it),
+// and halves larger than the threshold are split again, at most kEscMaxDepth
+// times.  Each piece keeps the bounds of its clipped polygon; the BVH is built over
+// the pieces and every leaf slot holds the whole triangle, so a ray meeting any
+// piece tests the same triangle and finds the same hit.
+#ifndef XR_ESC_MULT
+#define XR_ESC_MULT 4.0f
+#endif
+constexpr float kEscMult = XR_ESC_MULT;
+constexpr int kEscMaxDepth = 6;   // up to 64 pieces per triangle
+
+struct EscPoly {
+    float3 v[9];   // a triangle clipped by up to six axis-aligned planes
+    int n;
+};
+
+__device__ __forceinline__ void esc_clip(const EscPoly& in, int axis, float c, bool below, EscPoly& out) {
+    out.n = 0;
+    for (int k = 0; k < in.n; k++) {
+        const float3 a = in.v[k], b = in.v[k + 1 == in.n ? 0 : k + 1];
+        const float da = sel3(a, axis) - c, db = sel3(b, axis) - c;
+        const bool ina = below ? da <= 0.0f : da >= 0.0f;
+        const bool inb = below ? db <= 0.0f : db >= 0.0f;
+        if (ina && out.n < 9) out.v[out.n++] = a;
+        if (ina != inb && (da != 0.0f && db != 0.0f) && out.n < 9) {
+            const float t = da / (da - db);
+            float3 q = a + (b - a) * t;
+            if (axis == 0) q.x = c; else if (axis == 1) q.y = c; else q.z = c;
+            out.v[out.n++] = q;
+        }
+    }
+}
+
+// Pieces of one triangle in a fixed depth-first order; EMIT writes them at `base`.
+template <bool EMIT>
+__device__ uint32_t esc_pieces(float3 v0, float3 v1, float3 v2, float thr, uint32_t prim, uint32_t base,
+                               float4* __restrict__ rlo, float4* __restrict__ rhi, uint32_t* __restrict__ rprim) {
+    EscPoly st[kEscMaxDepth + 2];
+    int dep[kEscMaxDepth + 2];
+    int sp = 0;
+    st[0].v[0] = v0; st[0].v[1] = v1; st[0].v[2] = v2; st[0].n = 3;
+    dep[0] = 0;
+    sp = 1;
+    uint32_t cnt = 0;
+    while (sp > 0) {
+        sp--;
+        const EscPoly p = st[sp];
+        const int d = dep[sp];
+        float3 lo = p.v[0], hi = p.v[0];
+        for (int k = 1; k < p.n; k++) {
+            lo = f3(fminf(lo.x, p.v[k].x), fminf(lo.y, p.v[k].y), fminf(lo.z, p.v[k].z));
+            hi = f3(fmaxf(hi.x, p.v[k].x), fmaxf(hi.y, p.v[k].y), fmaxf(hi.z, p.v[k].z));
+        }
+        const float3 e = hi - lo;
+        if (d < kEscMaxDepth && length(e) > thr && sp + 2 <= kEscMaxDepth + 2) {
+            const int axis = (e.x >= e.y && e.x >= e.z) ? 0 : (e.y >= e.z ? 1 : 2);
+            const float c = 0.5f * (sel3(lo, axis) + sel3(hi, axis));
+            EscPoly a, b;
+            esc_clip(p, axis, c, true, a);
+            esc_clip(p, axis, c, false, b);
+            if (b.n >= 3) { st[sp] = b; dep[sp] = d + 1; sp++; }
+            if (a.n >= 3) { st[sp] = a; dep[sp] = d + 1; sp++; }
+        } else {
+            if (EMIT) {
+                rlo[base + cnt] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+                rhi[base + cnt] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+                rprim[base + cnt] = prim;
+            }
+            cnt++;
+        }
+    }
+    return cnt;
+}
+
+__global__ void k_esc_diag(const uint4* __restrict__ tri_idx, const float4* __restrict__ vpos, uint32_t n,
+                           double* __restrict__ sum) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    float d = 0.0f;
+    if (t < n) {
+        const uint4 id = tri_idx[t];
+        const float4 a = vpos[id.x], b = vpos[id.y], c = vpos[id.z];
+        const float ex = fmaxf(a.x, fmaxf(b.x, c.x)) - fminf(a.x, fminf(b.x, c.x));
+        const float ey = fmaxf(a.y, fmaxf(b.y, c.y)) - fminf(a.y, fminf(b.y, c.y));
+        const float ez = fmaxf(a.z, fmaxf(b.z, c.z)) - fminf(a.z, fminf(b.z, c.z));
+        d = sqrtf(ex * ex + ey * ey + ez * ez);
+    }
+    for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, off);
+    if ((threadIdx.x & 31) == 0 && d != 0.0f) atomicAdd(sum, (double)d);
+}
+
+template <bool EMIT>
+__global__ void k_esc(const uint4* __restrict__ tri_idx, const float4* __restrict__ vpos, uint32_t n, float thr,
+                      uint32_t* __restrict__ count, const uint32_t* __restrict__ offset, const uint32_t* __restrict__ sums,
+                      float4* __restrict__ rlo, float4* __restrict__ rhi, uint32_t* __restrict__ rprim) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint4 id = tri_idx[t];
+    const float3 a = xyz(vpos[id.x]), b = xyz(vpos[id.y]), c = xyz(vpos[id.z]);
+    if (EMIT) esc_pieces<true>(a, b, c, thr, t, offset[t] + sums[t >> 10], rlo, rhi, rprim);
+    else count[t] = esc_pieces<false>(a, b, c, thr, t, 0u, nullptr, nullptr, nullptr);
 }
 
 // ---- PLOC: Meister and Bittner, "Parallel Locally-Ordered Clustering for
@@ -922,6 +1031,7 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
             ca.left = left; ca.right = right; ca.count = range; ca.nlo = nlo; ca.nhi = nhi; ca.tlo = tlo; ca.thi = thi;
             ca.sorted = v0; ca.tri_idx = B.tri_idx; ca.vpos = B.vpos; ca.records = B.records;
             ca.dec = sah ? sah_dec : nullptr;
+            ca.ref_prim = B.ref_prim;
             ca.task_in = ta; ca.task_wide_in = wa; ca.n_tasks = ntask; ca.task_out = tb; ca.task_wide_out = wb;
             ca.counters = counters; ca.nodes = nodes_tmp; ca.tris = B.slots; ca.emin = emin;
             ca.max_nodes = nint; ca.n_prims = n;
@@ -978,7 +1088,48 @@ xr_status build_bvh(Context* ctx) {
     wb.n = ctx->ntri;
     wb.tri_idx = ctx->d_tri_idx;
     wb.vpos = ctx->d_vpos;
-    xr_status s = build_wide(ctx, wb);
+    float4 *rlo = nullptr, *rhi = nullptr;
+    uint32_t *rprim = nullptr, *cnt = nullptr, *off = nullptr, *sums = nullptr;
+    double* dsum = nullptr;
+    xr_status s = XR_OK;
+    // Off by default: on the benchmark scene the unsplit ground triangles sit near the
+    // root, where almost every ray meets them first and gets an early closest t that
+    // culls the rest; split into pieces deep in the tree they lose that role, and the
+    // frame is slower (threshold 4 / 8 / 16 x the mean diagonal: 3.01 / 2.91 / 2.80 ms
+    // against 2.68 ms), although triangle tests per camera ray drop from 4.7 to 3.4.
+    const char* split_env = getenv("XR_BVH_SPLIT");
+    const bool split = ctx->ntri > 1 && split_env && strcmp(split_env, "1") == 0;
+    if (split) {
+        // references: pieces of the large triangles, one box per piece
+        const uint32_t n = ctx->ntri, nb = (n + 1023) / 1024;
+        cudaStream_t st = ctx->stream;
+        if ((s = dalloc(ctx, &dsum, 1)) || (s = dalloc(ctx, &cnt, n)) || (s = dalloc(ctx, &off, n)) ||
+            (s = dalloc(ctx, &sums, nb + 1)))
+            goto out;
+        cudaMemsetAsync(dsum, 0, sizeof(double), st);
+        k_esc_diag<<<(n + 255) / 256, 256, 0, st>>>(ctx->d_tri_idx, ctx->d_vpos, n, dsum);
+        double total = 0.0;
+        cudaMemcpyAsync(&total, dsum, sizeof(double), cudaMemcpyDeviceToHost, st);
+        if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: split threshold"))) goto out;
+        const float thr = (float)(kEscMult * total / n);
+        k_esc<false><<<(n + 127) / 128, 128, 0, st>>>(ctx->d_tri_idx, ctx->d_vpos, n, thr, cnt, nullptr, nullptr,
+                                                       nullptr, nullptr, nullptr);
+        k_scan_local<<<nb, 1024, 0, st>>>(cnt, n, off, sums);
+        k_scan_top<<<1, 32, 0, st>>>(sums, nb);
+        uint32_t nref = 0;
+        cudaMemcpyAsync(&nref, sums + nb, 4, cudaMemcpyDeviceToHost, st);
+        if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: split count"))) goto out;
+        if ((s = dalloc(ctx, &rlo, nref)) || (s = dalloc(ctx, &rhi, nref)) || (s = dalloc(ctx, &rprim, nref))) goto out;
+        k_esc<true><<<(n + 127) / 128, 128, 0, st>>>(ctx->d_tri_idx, ctx->d_vpos, n, thr, nullptr, off, sums, rlo, rhi,
+                                                      rprim);
+        wb.n = nref;
+        wb.box_lo = rlo;
+        wb.box_hi = rhi;
+        wb.ref_prim = rprim;
+    }
+    s = build_wide(ctx, wb);
+out:
+    cudaFree(rlo); cudaFree(rhi); cudaFree(rprim); cudaFree(cnt); cudaFree(off); cudaFree(sums); cudaFree(dsum);
     if (s) return s;
     ctx->d_nodes = wb.nodes;
     ctx->d_tris = wb.slots;

@@ -274,7 +274,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 const uint32_t bit = __ffs(tg_mask) - 1u;
                 n_tests++;
                 tg_mask &= tg_mask - 1u;
-                if (tg_base + bit >= sc.ntri) {
+                if (tg_base + bit >= sc.n_tri_slots) {
                     bad = true;
                 } else {
                     const float4* tp = sc.tri + 3u * (tg_base + bit);

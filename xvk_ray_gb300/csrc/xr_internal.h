@@ -82,6 +82,7 @@ struct DeviceScene {
     const XrMaterial* mats;
     uint32_t n_mats;
     uint32_t ntri;
+    uint32_t n_tri_slots;     // BVH triangle slots (>= ntri: split triangles have several)
     // emissive triangles (next-event estimation of the cache's training paths)
     const uint32_t* light_prim;      // primitive of light k
     const float* light_cdf;          // inclusive CDF of the power pmf (last entry 1)
@@ -209,6 +210,7 @@ struct WideBuild {
     const float4* box_lo = nullptr;
     const float4* box_hi = nullptr;
     const float4* records = nullptr;
+    const uint32_t* ref_prim = nullptr;   // box input of triangle pieces: the triangle of each box
     int emin_floor = -1000;             // lower bound of the finest grid exponent
     int builder = 0;                    // 0: XR_BVH_BUILDER (PLOC unless "lbvh"), 1: PLOC, 2: LBVH
     WideNode* nodes = nullptr;          // device arrays owned by the caller afterwards
