@@ -589,7 +589,13 @@ __global__ void __launch_bounds__(kBlock, INST ? XR_TRACE_MIN_BLOCKS_INST : XR_T
 // Shading of one bounce over the queue (persistent grid): coherent per-path
 // work after the divergent traversal.
 template <bool COMPAT>
-__global__ void __launch_bounds__(kBlock) k_shade(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t bounce,
+// Shading is bound by its dependent gathers (hit -> indices -> vertices ->
+// material): 8 CTAs per SM (64 registers, 100 bytes spilled) hide them better than
+// the 5 that 96 registers allow (1080p frame 2.68 -> 2.64 ms).
+#ifndef XR_SHADE_MIN_BLOCKS
+#define XR_SHADE_MIN_BLOCKS 8
+#endif
+__global__ void __launch_bounds__(kBlock, XR_SHADE_MIN_BLOCKS) k_shade(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t bounce,
                                                   uint32_t nb) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[bounce];
     const uint32_t stride = gridDim.x * blockDim.x;
