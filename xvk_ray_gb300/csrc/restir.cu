@@ -1042,7 +1042,14 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
 // {neighbour, p-hat} per slot for the resolve step; with shadow rays on, queues
 // one ray {pixel << 5 | slot, neighbour} per neighbour with p-hat > 0.  Every
 // pixel clears its occlusion bits.
-__global__ void __launch_bounds__(256) k_spatial_select(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+// Like shading, spatial select and resolve wait on neighbour gathers: 4 CTAs of 256
+// per SM for select (64 registers, 16 bytes spilled) and 5 for resolve (48
+// registers, 44 bytes spilled) beat the occupancy their register counts allow
+// (spatial pass 0.76 -> 0.66 ms at 1080p, measured twice in one session).
+#ifndef XR_SELECT_MIN_BLOCKS
+#define XR_SELECT_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(256, XR_SELECT_MIN_BLOCKS) k_spatial_select(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = lane_id();
     uint32_t emit_mask = 0u;
@@ -1175,7 +1182,10 @@ __global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_nee(Frame
 // Spatial reuse, step 3 of 3: the merge of ReSTIRGISpatialReuse.rgen.hlsl:91-176
 // over the similar neighbours and p-hat values of step 1, with the visibility of
 // step 2, M cap, W, shading and tone mapping.
-__global__ void __launch_bounds__(256) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+#ifndef XR_RESOLVE_MIN_BLOCKS
+#define XR_RESOLVE_MIN_BLOCKS 5
+#endif
+__global__ void __launch_bounds__(256, XR_RESOLVE_MIN_BLOCKS) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
     const PixView pv = pix_view(fa, p);
