@@ -38,8 +38,9 @@ BOUNCES = 4
 SCENE_KW = dict(seed=1, n_objects=4096, n_lights=16, extent=40.0, sphere_subdiv=2)
 METRIC = "ms/frame 1080p & relMSE vs FP64 ref: plain ReSTIR GI vs ReSTIR GI+MLP cache"
 # algorithmic bytes per pixel of the temporal reuse pass in the packed layout:
-# reads G-buffer 16+4, candidate 16+16, previous G-buffer 4+16, previous reservoir 32; writes reservoir 32
-TEMPORAL_BYTES_PER_PX = 136
+# reads G-buffer 16+4, candidate 16+16, reprojected pixel index 4, previous G-buffer 4+16,
+# previous reservoir 32; writes reservoir 32
+TEMPORAL_BYTES_PER_PX = 140
 SPATIAL_BYTES_PER_PX = 104   # reads G-buffer 16+4, candidate 16, reservoir 32; writes reservoir 32 + RGBA8 4
 # DRAM bytes (read + write) of one k_temporal launch at 1920x1080 measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum): 179.6 MB + 47.1 MB

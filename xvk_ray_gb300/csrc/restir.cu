@@ -85,6 +85,16 @@ __device__ __forceinline__ HitPayload closest_hit(const DeviceScene& sc, const H
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// The previous frame's pixel of a visible point (ReSTIRGITemporalReuse.rgen.hlsl:
+// motion vector -> previous uv), kInvalid when it falls outside the view.
+__device__ __forceinline__ uint32_t reproject(float3 x_view, const XrUniformBufferObject* __restrict__ u, uint32_t W,
+                                              uint32_t H, uint32_t base) {
+    const float2 puv = world_to_screen_uv(x_view, u->view_prev, u->projection_prev);
+    const float fx = floorf(puv.x * (float)W), fy = floorf(puv.y * (float)H);
+    if (fx >= 0.0f && fx < (float)W && fy >= 0.0f && fy < (float)H) return base + (uint32_t)fy * W + (uint32_t)fx;
+    return kInvalid;
+}
+
 // ---- views: a pixel's view, its view-local coordinates and extent ----
 __device__ __forceinline__ uint32_t view_index(const FrameArgs& fa, uint32_t p) {
     if (fa.n_views <= 1u) return 0u;
@@ -343,6 +353,12 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
         } else {
             fa.gb_pos_cur[p] = f4(pl.pos, __uint_as_float(oct_encode(pl.normal, 16)));
             fa.gb_mat_cur[p] = (uint32_t)pl.mat;
+            // the temporal pass's reprojection, done here where the visible point is
+            // known so that the temporal pass can gather the previous frame at once
+            if (fa.temporal_on) {
+                const PixView pv = pix_view(fa, p);
+                fa.reproj[p] = reproject(pl.pos, u, pv.W, pv.H, pv.base);
+            }
         }
         if (fa.write_pt) fa.thr0[p] = f4(factor, 0.0f);
         s.pq = pdf;
@@ -973,6 +989,7 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     float4 g = fa.gb_pos_cur[p];
     uint32_t mat = fa.gb_mat_cur[p];
     float4 a = fa.cand_a[p], b = fa.cand_b[p];
+    const uint32_t q = (fa.temporal_on && mat != kInvalid) ? fa.reproj[p] : kInvalid;   // set by bounce 0's shading
     const uint32_t bw = __float_as_uint(b.w);
     const bool valid = mat != kInvalid, has = (bw >> 31) != 0u;
     if (fa.write_pt) {
@@ -991,23 +1008,18 @@ __global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformB
     Res s_new;
     s_new.xs = xyz(a); s_new.L = xyz(b); s_new.code = bw & 0x00FFFFFFu; s_new.ns = f3(0, 0, 0);   // travels as its code
     s_new.f = f3(0, 0, 0);
-    // Reprojection first, and every previous-frame word of the reprojected pixel
-    // gathered at once (material, position, reservoir): one memory round trip
-    // instead of three dependent ones; the tests below decide what is used.
+    // Every previous-frame word of the reprojected pixel gathered at once (material,
+    // position, reservoir): one memory round trip after the coalesced loads; the
+    // tests below decide what is used.
     bool in_prev = false;
     uint32_t pmat = kInvalid;
     float4 pg = make_float4(0, 0, 0, 0), rp0 = pg, rp1 = pg;
-    if (fa.temporal_on) {
-        float2 puv = world_to_screen_uv(x_view, u->view_prev, u->projection_prev);
-        float fx = floorf(puv.x * (float)pv.W), fy = floorf(puv.y * (float)pv.H);
-        if (fx >= 0.0f && fx < (float)pv.W && fy >= 0.0f && fy < (float)pv.H) {
-            const uint32_t q = pv.base + (uint32_t)fy * pv.W + (uint32_t)fx;
-            pmat = fa.gb_mat_prev[q];
-            pg = fa.gb_pos_prev[q];
-            rp0 = fa.rt_prev0[q];
-            rp1 = fa.rt_prev1[q];
-            in_prev = true;
-        }
+    if (q != kInvalid) {
+        pmat = fa.gb_mat_prev[q];
+        pg = fa.gb_pos_prev[q];
+        rp0 = fa.rt_prev0[q];
+        rp1 = fa.rt_prev1[q];
+        in_prev = true;
     }
     const PixelShading P = pixel_shading(fa, u, x_view, n_view, mat, p);
     bool found = false;
@@ -1326,6 +1338,16 @@ __global__ void k_export_res_packed(const float4* __restrict__ p0, const float4*
     for (int k = 0; k < 7; k++) o[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
 }
 
+// The reprojection of every valid pixel from the stored G-buffer (a temporal pass
+// run on its own, after imported samples; frames get it from bounce 0's shading).
+__global__ void k_reproject(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fa.N) return;
+    if (fa.gb_mat_cur[p] == kInvalid) return;
+    const PixView pv = pix_view(fa, p);
+    fa.reproj[p] = reproject(xyz(fa.gb_pos_cur[p]), u + pv.v, pv.W, pv.H, pv.base);
+}
+
 __global__ void k_import_samples(FrameArgs fa, const uint32_t* __restrict__ in) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
@@ -1427,6 +1449,9 @@ void launch_temporal(const FrameArgs& fa, bool write_image, cudaStream_t st) {
 
 void launch_export_samples(const FrameArgs& fa, uint32_t* out, cudaStream_t st) {
     k_export_samples<<<(fa.N + 255u) / 256u, 256, 0, st>>>(fa, out);
+}
+void launch_reproject(const FrameArgs& fa, cudaStream_t st) {
+    k_reproject<<<(fa.N + 255u) / 256u, 256, 0, st>>>(fa, fa.ubo);
 }
 void launch_import_samples(const FrameArgs& fa, const uint32_t* in, cudaStream_t st) {
     k_import_samples<<<(fa.N + 255u) / 256u, 256, 0, st>>>(fa, in);

@@ -111,6 +111,7 @@ xr_status alloc_pixels(Context* c) {
         add((void**)&fa.occ, N * 4);
         add((void**)&fa.shadow_q, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
         add((void**)&fa.nb_slot, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
+        add((void**)&fa.reproj, N * 4);
     }
     add((void**)&fa.hits, N * 16);
     add((void**)&fa.hit_inst, N * 4);
@@ -968,6 +969,7 @@ xr_status xr_run_pass(XrContext* c, const XrUniformBufferObject* ubo, uint32_t p
     if (s) return s;
     set_frame_pointers(c, ubo->current_frame % 2u);
     const bool compat = c->params.compat_reference != 0;
+    if (pass == 1 && !compat && c->params.temporal_on) launch_reproject(c->fa, c->stream);
     if (pass == 1) launch_temporal(c->fa, compat ? (ubo->reuse == 0u) : (c->params.spatial_on == 0u), c->stream);
     else launch_spatial(c->fa, c->stream);
     s = cuda_check(c, cudaGetLastError(), "run_pass launch");

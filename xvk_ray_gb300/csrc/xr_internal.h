@@ -147,6 +147,7 @@ struct FrameArgs {
     int32_t* hit_inst;        // its instance (scenes with instances)
     uint2* shadow_q;          // corrected spatial pass: {pixel << 5 | slot, neighbour pixel}
     uint32_t* occ;            // per pixel: occluded neighbour slots
+    uint32_t* reproj;         // corrected mode, per pixel: its visible point's pixel in the previous frame (kInvalid: none)
     uint2* nb_slot;           // corrected spatial pass, plane per slot: {neighbour pixel, target * Jacobian}
                               // of a similar neighbour, {kInvalid, 0} otherwise
     uint32_t* counters;       // [b] paths entering bounce b, then the kCnt* words above
@@ -359,6 +360,7 @@ void launch_spatial(const FrameArgs& fa, cudaStream_t st);
 void launch_accumulate_sample(const FrameArgs& fa, double* acc, cudaStream_t st);
 void launch_export_samples(const FrameArgs& fa, uint32_t* out, cudaStream_t st);
 void launch_import_samples(const FrameArgs& fa, const uint32_t* in, cudaStream_t st);
+void launch_reproject(const FrameArgs& fa, cudaStream_t st);   // reprojection of the stored G-buffer (temporal pass on its own)
 void launch_export_res_wide(float4* const planes[4], uint32_t n, uint32_t* out, cudaStream_t st);
 void launch_export_res_packed(const float4* p0, const float4* p1, uint32_t n, uint32_t* out, cudaStream_t st);
 void launch_import_res_wide(float4* const planes[4], uint32_t n, const uint32_t* in, cudaStream_t st);
