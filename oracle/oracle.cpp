@@ -992,7 +992,7 @@ inline PixelShading pixel_shading(const Renderer& R, const Sample& s, const OrUB
     P.m = resolve_material(*R.sc, s.materialID, R.sc->tex_info.empty() ? f2{0.0f, 0.0f} : R.gb_uv[p]);
     P.x = s.x_view;
     P.n = s.n_view;
-    f3 cam = xyz(mul(u.view_inverse, f4{0, 0, 0, 1}));
+    f3 cam{u.view_inverse[12], u.view_inverse[13], u.view_inverse[14]};   // translation column (column-major)
     P.wo = normalize(cam - P.x);
     branchless_onb(P.n, &P.T, &P.B);
     const bool glossy = (P.m.model == MAT_METALLIC || P.m.model == MAT_PLASTIC) && P.m.fuzz < kReuseMinRoughness;

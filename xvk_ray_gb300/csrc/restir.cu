@@ -909,7 +909,8 @@ __device__ __forceinline__ PixelShading pixel_shading(const FrameArgs& fa, const
     P.m = resolve_material(fa.sc, mat, fa.sc.n_tex ? fa.gb_uv[p] : make_float2(0.0f, 0.0f));
     P.x = x;
     P.n = n;
-    const float3 cam = xyz(mat_mul(u->view_inverse, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));
+    // the camera position: the translation column of view_inverse (column-major)
+    const float3 cam = f3(u->view_inverse[12], u->view_inverse[13], u->view_inverse[14]);
     P.wo = normalize(cam - x);
     branchless_onb(n, &P.T, &P.B);
     const bool glossy = (P.m.material_model == XR_MAT_METALLIC || P.m.material_model == XR_MAT_PLASTIC) &&
