@@ -402,25 +402,9 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
     return alive;
 }
 
-__device__ __forceinline__ void push_path(const FrameArgs& fa, bool alive, const PathState& s, uint32_t qslot) {
-    uint32_t mask = __ballot_sync(0xFFFFFFFFu, alive);
-    if (mask == 0u) return;
-    uint32_t lane = lane_id();
-    int leader = __ffs(mask) - 1;
-    uint32_t base = 0;
-    if ((int)lane == leader) base = atomicAdd(&fa.counters[qslot], (uint32_t)__popc(mask));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    if (alive) {
-        uint32_t i = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
-        fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
-        fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
-        fa.q_out[2][i] = f4(s.thr, s.pq);
-    }
-}
-
-// push_path for every thread of a block at once (all threads of the block call
-// it): one atomic per block instead of one per warp -- appends from all warps of
-// the grid go to the same counter, whose atomics serialise.
+// Appends the alive paths of a whole block to the next bounce's queue (all threads
+// of the block call it): one atomic per block -- appends from all warps of the grid
+// go to the same counter, whose atomics serialise.
 template <int BLOCK>
 __device__ __forceinline__ void push_path_block(const FrameArgs& fa, bool alive, const PathState& s, uint32_t qslot) {
     constexpr int kWarps = BLOCK / 32;
@@ -926,17 +910,15 @@ __device__ __forceinline__ float target_corrected(const PixelShading& P, float3 
     return length(L * f * c);
 }
 
-// Final shading of a reservoir at its pixel: L W f cos along the reconnection
-// direction.  A near-specular pixel (no reuse: its reservoir is its own
-// candidate) is shaded with the path tracer's ratio f cos / pdf evaluated at that
-// one direction instead: the reconnection direction from the visible point
-// differs slightly from the sampled one (the path left from a point offset
-// along the normal), and in a lobe that sharp f alone changes by orders of
-// magnitude over that angle while the ratio stays bounded.
-// The final target of a reservoir's sample and its shading from one BSDF
-// evaluation: target_corrected and shade_corrected evaluate the same lobe at the
-// same direction, so the results are theirs bit for bit.  `tp_known` >= 0 is the
-// target when the caller already has it (the selected candidate's), else < 0.
+// The final target of a reservoir's sample and its shading, from one BSDF
+// evaluation (target_corrected's lobe at the same direction).  `tp_known` >= 0 is
+// the target when the caller already has it (the selected candidate's), else < 0.
+// Shading: L W f cos along the reconnection direction.  A near-specular pixel (no
+// reuse: its reservoir is its own candidate) is shaded with the path tracer's
+// ratio f cos / pdf at that one direction instead: the reconnection direction from
+// the visible point differs slightly from the sampled one (the path left from a
+// point offset along the normal), and in a lobe that sharp f alone changes by
+// orders of magnitude over that angle while the ratio stays bounded.
 __device__ __forceinline__ float3 finish_corrected(const PixelShading& P, Res& r, float tp_known, uint32_t m_cap,
                                                    bool shade) {
     const float3 wi = normalize(r.xs - P.x);
@@ -960,18 +942,6 @@ __device__ __forceinline__ float3 finish_corrected(const PixelShading& P, Res& r
         else if (lb.pdf > 0.0f) col = r.L * lb.f * (ct / lb.pdf);
     }
     return col;
-}
-
-__device__ __forceinline__ float3 shade_corrected(const PixelShading& P, const Res& r) {
-    float3 c = f3(0, 0, 0);
-    if (r.W > 0.0f) {
-        const float3 wi = normalize(r.xs - P.x);
-        const float ct = fmaxf(0.0f, dot(P.n, wi));
-        const Lobe lb = eval_material(P.m, to_local(P.wo, P.T, P.B, P.n), to_local(wi, P.T, P.B, P.n));
-        if (P.reuse) c = r.L * r.W * lb.f * ct;
-        else if (lb.pdf > 0.0f) c = r.L * lb.f * (ct / lb.pdf);
-    }
-    return c;
 }
 
 // Neighbours of the corrected spatial pass: the first 2 n draws of the pixel's
