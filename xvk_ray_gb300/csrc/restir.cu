@@ -951,10 +951,10 @@ __device__ __forceinline__ void rng_skip(uint32_t& st, uint32_t n) {
     for (uint32_t k = 0; k < n; k++) st = st * 747796405u + 2891336453u;   // the state step of next_random
 }
 
-// 128-thread blocks: finer scheduling of a latency-bound pass (swept 128 / 256 /
-// 512: 71.2 / 73.7 / 77.3 us at 1080p, CUDA events).
+// 64-thread blocks: finer scheduling of a latency-bound pass (swept 64 / 128 / 256 /
+// 512: 69.7 / 71.2 / 73.7 / 77.3 us at 1080p, CUDA events).
 #ifndef XR_TEMPORAL_BLOCK
-#define XR_TEMPORAL_BLOCK 128
+#define XR_TEMPORAL_BLOCK 64
 #endif
 __global__ void __launch_bounds__(XR_TEMPORAL_BLOCK) k_temporal(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
