@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
     "-Xptxas", "-warn-spills",
     f"-I{ROOT / 'include'}", f"-I{CSRC}",
-] + os.environ.get("XR_EXTRA_NVCC_FLAGS", "").split()   # e.g. -DXR_TRACE_MIN_BLOCKS=10 (tuning builds)
+] + os.environ.get("XR_EXTRA_NVCC_FLAGS", "").split()   # e.g. -DXR_TRACE_BLOCK=512 (tuning builds)
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 
 CU_SOURCES = ["bvh_build.cu", "trace.cu", "trace_noalloc.cu", "restir.cu", "nrc.cu", "cache_api.cu", "batch.cu",

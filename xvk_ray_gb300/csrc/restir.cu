@@ -25,17 +25,24 @@
 namespace xr {
 namespace {
 
-constexpr int kBlock = 128;
-// Minimum resident CTAs per SM requested from the compiler for the traversal
-// kernels (a register budget: 8 -> 64 registers, 10 -> 48).
-#ifndef XR_TRACE_MIN_BLOCKS
-#define XR_TRACE_MIN_BLOCKS 8
+constexpr int kBlock = 128;   // raygen (one 16 x 8 tile per block)
+// Persistent traversal in one 1024-thread CTA per SM (64 registers: the whole
+// register file): swept 128 / 256 / 512 / 1024 threads at the same occupancy,
+// 2.597 / 2.577 / 2.552 / 2.525 ms per 1080p frame.  The two-level variants keep
+// more state per lane and run one 896-thread CTA per SM (72 registers, no spills).
+#ifndef XR_TRACE_BLOCK
+#define XR_TRACE_BLOCK 1024
 #endif
-// The two-level variants (scenes with instances) keep more state per lane: 7 CTAs
-// per SM (72 registers) traverse without spills where 8 (64) spill.
-#ifndef XR_TRACE_MIN_BLOCKS_INST
-#define XR_TRACE_MIN_BLOCKS_INST 7
+#ifndef XR_TRACE_BLOCK_INST
+#define XR_TRACE_BLOCK_INST 896
 #endif
+#ifndef XR_SHADE_BLOCK
+#define XR_SHADE_BLOCK 128
+#endif
+constexpr int kTraceBlock = XR_TRACE_BLOCK;   // persistent traversal kernels
+constexpr int kTraceBlockInst = XR_TRACE_BLOCK_INST;
+template <bool INST> constexpr int trace_block() { return INST ? kTraceBlockInst : kTraceBlock; }
+constexpr int kShadeBlock = XR_SHADE_BLOCK;   // persistent shading kernel
 
 struct HitPayload {
     float3 pos, normal, geo;
@@ -560,7 +567,7 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 // With several scenes each ray starts at its view's root; a path whose pixel slot
 // holds a cache training record (pixel_is_record) finds its pixel in the record.
 template <bool INST>
-__global__ void __launch_bounds__(kBlock, INST ? XR_TRACE_MIN_BLOCKS_INST : XR_TRACE_MIN_BLOCKS) k_trace_paths(FrameArgs fa, const float4* __restrict__ q0,
+__global__ void __launch_bounds__(trace_block<INST>(), 1) k_trace_paths(FrameArgs fa, const float4* __restrict__ q0,
                                                         const float4* __restrict__ q1, uint4* __restrict__ hits,
                                                         const uint32_t* count_ptr, uint32_t* next, uint32_t* err,
                                                         uint32_t* nonfinite, uint32_t pixel_is_record) {
@@ -595,7 +602,7 @@ template <bool COMPAT>
 #ifndef XR_SHADE_MIN_BLOCKS
 #define XR_SHADE_MIN_BLOCKS 8
 #endif
-__global__ void __launch_bounds__(kBlock, XR_SHADE_MIN_BLOCKS) k_shade(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t bounce,
+__global__ void __launch_bounds__(kShadeBlock, XR_SHADE_MIN_BLOCKS * 128 / kShadeBlock) k_shade(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, uint32_t bounce,
                                                   uint32_t nb) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[bounce];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -626,7 +633,7 @@ __global__ void __launch_bounds__(kBlock, XR_SHADE_MIN_BLOCKS) k_shade(FrameArgs
         }
         if (!COMPAT && fa.cache_on && bounce == 1u) alive = cache_emit(fa, ce, alive, s);
         if (!COMPAT && fa.cache_on && bounce >= 2u) push_nee(fa, ce.nee.valid, ce.nee, s.pixel);
-        push_path_block<kBlock>(fa, alive, s, bounce + 1u);
+        push_path_block<kShadeBlock>(fa, alive, s, bounce + 1u);
     }
 }
 
@@ -1116,7 +1123,7 @@ __global__ void __launch_bounds__(XR_SPATIAL_BLOCK, XR_SELECT_MIN_BLOCKS * 256 /
 // (ReSTIRGISpatialReuse.rgen.hlsl:44-62 with the centre pixel's visible point as
 // origin); an occluded ray sets its slot's bit in the pixel's occlusion word.
 template <bool INST>
-__global__ void __launch_bounds__(kBlock, INST ? XR_TRACE_MIN_BLOCKS_INST : XR_TRACE_MIN_BLOCKS) k_trace_shadow(FrameArgs fa) {
+__global__ void __launch_bounds__(trace_block<INST>(), 1) k_trace_shadow(FrameArgs fa) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[32];
     trace_persistent<true, INST>(
         fa.sc, count, &fa.counters[kCntFetchShadow],
@@ -1146,7 +1153,7 @@ __global__ void __launch_bounds__(kBlock, INST ? XR_TRACE_MIN_BLOCKS_INST : XR_T
 
 // Next-event rays of the cache's training paths (one bounce): any-hit
 // traversal; an unoccluded ray adds its contribution to its record's target.
-__global__ void __launch_bounds__(kBlock, XR_TRACE_MIN_BLOCKS) k_trace_nee(FrameArgs fa) {
+__global__ void __launch_bounds__(kTraceBlock, 1) k_trace_nee(FrameArgs fa) {
     const uint32_t count = *(volatile const uint32_t*)&fa.counters[kCntCacheNee];
     trace_persistent<true>(
         fa.sc, count < fa.cache_t_cap ? count : fa.cache_t_cap, &fa.counters[kCntFetchNee],
@@ -1378,8 +1385,8 @@ uint32_t persistent_grid(int sm_count, bool compat) {
     int& o = occ[compat ? 1 : 0];
     if (o == 0) {
         int v = 0;
-        if (compat) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_shade<true>, kBlock, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_shade<false>, kBlock, 0);
+        if (compat) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_shade<true>, kShadeBlock, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_shade<false>, kShadeBlock, 0);
         o = v > 0 ? v : 4;
     }
     return (uint32_t)(o * sm_count);
@@ -1390,8 +1397,8 @@ uint32_t trace_grid(int sm_count, bool instances) {
     int& o = occ[instances ? 1 : 0];
     if (o == 0) {
         int v = 0;
-        if (instances) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<true>, kBlock, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<false>, kBlock, 0);
+        if (instances) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<true>, kTraceBlockInst, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<false>, kTraceBlock, 0);
         o = v > 0 ? v : 4;
     }
     return (uint32_t)(o * sm_count);
@@ -1407,18 +1414,18 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
         // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
         if (fa.sc.n_inst)
-            k_trace_paths<true><<<fa.grid_trace, kBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+            k_trace_paths<true><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                               fa.counters + kCntFetchPath + b, fa.counters + kCntError,
                                                               fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u);
         else
-            k_trace_paths<false><<<fa.grid_trace, kBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+            k_trace_paths<false><<<fa.grid_trace, kTraceBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                                fa.counters + kCntFetchPath + b, fa.counters + kCntError,
                                                                fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u);
         const bool nee = cache && b >= 1u && b + 1u < nb;
         if (nee) cudaMemsetAsync(fa.counters + kCntCacheNee, 0, 2 * sizeof(uint32_t), st);   // count + fetch
-        if (fa.compat) k_shade<true><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
-        else k_shade<false><<<fa.grid_persistent, kBlock, 0, st>>>(a, fa.ubo, b, nb);
-        if (nee) k_trace_nee<<<fa.grid_trace, kBlock, 0, st>>>(a);
+        if (fa.compat) k_shade<true><<<fa.grid_persistent, kShadeBlock, 0, st>>>(a, fa.ubo, b, nb);
+        else k_shade<false><<<fa.grid_persistent, kShadeBlock, 0, st>>>(a, fa.ubo, b, nb);
+        if (nee) k_trace_nee<<<fa.grid_trace, kTraceBlock, 0, st>>>(a);
     }
 }
 
@@ -1465,8 +1472,8 @@ void launch_spatial(const FrameArgs& fa, cudaStream_t st) {
     const uint32_t sblocks = (fa.N + XR_SPATIAL_BLOCK - 1u) / XR_SPATIAL_BLOCK;
     k_spatial_select<<<sblocks, XR_SPATIAL_BLOCK, 0, st>>>(fa, fa.ubo);
     if (fa.visibility) {
-        if (fa.sc.n_inst) k_trace_shadow<true><<<fa.grid_trace, kBlock, 0, st>>>(fa);
-        else k_trace_shadow<false><<<fa.grid_trace, kBlock, 0, st>>>(fa);
+        if (fa.sc.n_inst) k_trace_shadow<true><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(fa);
+        else k_trace_shadow<false><<<fa.grid_trace, kTraceBlock, 0, st>>>(fa);
     }
     k_spatial_resolve<<<sblocks, XR_SPATIAL_BLOCK, 0, st>>>(fa, fa.ubo);
 }

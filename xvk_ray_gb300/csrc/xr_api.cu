@@ -731,8 +731,13 @@ xr_status xr_autotune(XrContext* c, const XrUniformBufferObject* ubos, uint32_t 
     }
     std::vector<std::pair<uint32_t, uint32_t>> cands;
     for (int t : {0, occ_t * 3 / 4, occ_t / 2})
-        for (int sh : {0, occ_s / 2})
-            if ((t == 0 || t >= 1) && (sh == 0 || sh >= 1)) cands.push_back({(uint32_t)t, (uint32_t)sh});
+        for (int sh : {0, occ_s / 2}) {
+            // 0 is the occupancy maximum; fractions that round to it or to nothing are skipped
+            const std::pair<uint32_t, uint32_t> cand{(uint32_t)(t == occ_t ? 0 : t), (uint32_t)(sh == occ_s ? 0 : sh)};
+            if ((t == 0 || t >= 1) && (sh == 0 || sh >= 1) &&
+                std::find(cands.begin(), cands.end(), cand) == cands.end())
+                cands.push_back(cand);
+        }
     float best = 1e30f, dflt = 0.0f;
     std::pair<uint32_t, uint32_t> pick{0u, 0u};
     xr_status s = XR_OK;
