@@ -27,6 +27,7 @@ def test_struct_layouts_match_the_reference():
     assert C.sizeof(L.XrVertex) == 36
     assert C.sizeof(L.XrMaterial) == 32
     assert C.sizeof(L.XrUniformBufferObject) == 412
+    assert C.sizeof(L.XrInstance) == 56   # {scene, reserved, 3 x 4 object-to-world}
     assert L.load().xr_api_version() == 1
 
 

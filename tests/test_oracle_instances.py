@@ -110,3 +110,20 @@ def test_world_vertex_update_retraces():
     r1, r2 = world.trace_instanced(rays), w2.trace_instanced(rays)
     for x, y in zip(r1, r2):
         assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32))
+
+
+def test_world_without_instances_traces_the_concatenated_scenes():
+    """Scenes concatenated as xr_upload_scenes does (indices and material indices
+    relocated) and traced as one scene when no instances are set."""
+    rng = np.random.default_rng(6)
+    a, b = box_scene(rng, 10, 2.0), box_scene(rng, 6, 1.5, light=False)
+    world = ob.OracleWorld([ob.OracleScene.from_scene(a), ob.OracleScene.from_scene(b)])
+    flat, inst_of, prim_of = bake_instances([a, b], [(0, affine(np.eye(3), [0, 0, 0])),
+                                                     (1, affine(np.eye(3), [0, 0, 0]))])
+    rays = random_rays(rng, 10000, -4.0, 4.0)
+    p0, t0, b0 = ob.OracleScene.from_scene(flat).trace(rays)
+    p1, t1, b1 = world.trace(rays)
+    assert (p0 >= 0).mean() > 0.05
+    assert np.array_equal(p0, p1)   # identity bakes keep the concatenation's primitive order
+    assert np.array_equal(t0.view(np.uint32), t1.view(np.uint32))
+    assert np.array_equal(b0.view(np.uint32), b1.view(np.uint32))
