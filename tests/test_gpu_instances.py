@@ -234,3 +234,52 @@ def test_instances_of_empty_and_one_triangle_scenes():
         assert np.any(c[1] == 1) and np.any(c[1] == 3)   # the one-triangle instances are hit
         for name, x, y in zip(("prim", "instance", "t", "bary"), g, c):
             assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32)), name
+
+
+def test_many_instances_match_oracle():
+    """600 instances: a top-level BVH several levels deep (the tests above fit in one
+    node), rotated and scaled copies scattered over a 40-unit cube."""
+    rng = np.random.default_rng(31)
+    box = box_scene(rng, 1, 1.0, light=False)
+    inst = []
+    for k in range(600):
+        R = rotation(rng.normal(size=3), float(rng.uniform(0, 360))) * float(rng.uniform(0.3, 1.5))
+        inst.append((0, affine(R, rng.uniform(-20.0, 20.0, 3))))
+    world = _world([box], inst)
+    # rays from random origins aimed at random instances (most of them hit something)
+    rr = np.random.default_rng(2)
+    rays = random_rays(rr, 8000, -22.0, 22.0)
+    pick = rr.integers(0, len(inst), 8000)
+    vtx = box.vertices[rr.integers(0, box.vertices.shape[0], 8000), 0:3].astype(np.float64)
+    mats = np.array([m for _, m in inst], np.float64)[pick]
+    targets = np.einsum("nij,nj->ni", mats[:, :, :3], vtx) + mats[:, :, 3] + rr.normal(0, 0.05, (8000, 3))
+    d = targets - rays[:, 0:3]
+    rays[:, 4:7] = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    with xr.Renderer(32, 32) as r:
+        r.upload_scenes([box])
+        r.set_instances(inst)
+        assert r.stats().tlas_nodes > 8
+        g = r.trace_instanced(rays)
+        c = world.trace_instanced(rays)
+        assert (c[0] >= 0).mean() > 0.3
+        for name, x, y in zip(("prim", "instance", "t", "bary"), g, c):
+            assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32)), name
+        ga = r.trace_instanced(rays, any_hit=True)
+        ca = world.trace_instanced(rays, any_hit=True)
+        assert np.array_equal(ga[0] >= 0, ca[0] >= 0)
+
+
+def test_vertex_update_errors():
+    scene = xr.Scene.cornell()
+    with xr.Renderer(32, 32) as r:
+        r.upload_scene(scene)
+        r.build_bvh()
+        with pytest.raises(xr.XrError):
+            r.update_vertices(0, scene.vertices[:-1])          # the count must stay
+        with pytest.raises(xr.XrError):
+            r.update_vertices(1, scene.vertices)               # no such scene
+        bad = scene.vertices.copy()
+        bad[0, 0] = np.nan
+        with pytest.raises(xr.XrError):
+            r.update_vertices(0, bad)
+        r.update_vertices(0, scene.vertices)                   # unchanged geometry refits fine
