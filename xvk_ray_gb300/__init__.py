@@ -6,10 +6,10 @@ not need a GPU; creating a Renderer does.
 """
 from . import _lib
 from ._lib import XrError, load
-from .api import (CACHE_SAMPLE_DTYPE, Cache, PinnedBuffer, Renderer, Scene, cache_params_default, camera_ubo,
-                  params_default, params_reference, ubo_bytes)
+from .api import (CACHE_SAMPLE_DTYPE, INSTANCE_DTYPE, Cache, PinnedBuffer, Renderer, Scene, cache_params_default,
+                  camera_ubo, pack_instances, params_default, params_reference, ubo_bytes)
 from .path_tracer import PathTracer, UserSettings
 
 __all__ = ["XrError", "load", "Renderer", "Scene", "PinnedBuffer", "Cache", "CACHE_SAMPLE_DTYPE", "cache_params_default",
-           "camera_ubo", "params_default",
+           "INSTANCE_DTYPE", "pack_instances", "camera_ubo", "params_default",
            "params_reference", "ubo_bytes", "PathTracer", "UserSettings", "_lib"]

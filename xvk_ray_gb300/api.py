@@ -289,12 +289,10 @@ class Renderer:
         return prim, inst, t, bary
 
     def set_instances(self, instances) -> None:
-        """instances: (scene index, 3x4 object-to-world matrix) pairs; [] clears them."""
-        arr = (L.XrInstance * max(len(instances), 1))()
-        for k, (scene, m) in enumerate(instances):
-            arr[k].scene = int(scene)
-            arr[k].object_to_world[:] = [float(x) for x in np.asarray(m, np.float64).reshape(12)]
-        self._c(self._lib.xr_set_instances(self.ctx, C.cast(arr, C.c_void_p), len(instances)))
+        """instances: (scene index, 3x4 object-to-world matrix) pairs, or an array of
+        INSTANCE_DTYPE records (no per-instance Python work); [] clears them."""
+        arr = pack_instances(instances)
+        self._c(self._lib.xr_set_instances(self.ctx, arr.ctypes.data_as(C.c_void_p), arr.shape[0]))
 
     def instance_transforms(self, n: int) -> np.ndarray:
         """(n, 2, 3, 4): object-to-world and world-to-object of the first n instances."""
@@ -306,6 +304,24 @@ class Renderer:
         """New vertices (same count and layout as uploaded) of a scene, then a refit of its BVH."""
         v = np.ascontiguousarray(vertices, np.float32)
         self._c(self._lib.xr_update_vertices(self.ctx, int(scene), _ptr(v), v.shape[0]))
+
+
+# host layout of XrInstance (56 B)
+INSTANCE_DTYPE = np.dtype([("scene", "<u4"), ("reserved", "<u4"), ("object_to_world", "<f4", 12)])
+assert INSTANCE_DTYPE.itemsize == C.sizeof(L.XrInstance)
+
+
+def pack_instances(instances) -> np.ndarray:
+    """XrInstance records of (scene index, 3x4 matrix) pairs; records pass through."""
+    if isinstance(instances, np.ndarray) and instances.dtype == INSTANCE_DTYPE:
+        return np.ascontiguousarray(instances)
+    n = len(instances)
+    arr = np.zeros(n, INSTANCE_DTYPE)
+    if n:
+        arr["scene"] = [int(s) for s, _ in instances]
+        arr["object_to_world"] = np.asarray([np.asarray(m, np.float64).reshape(12) for _, m in instances],
+                                            np.float64).astype(np.float32)
+    return arr
 
 
 # host layout of XrCacheSample (72 B)

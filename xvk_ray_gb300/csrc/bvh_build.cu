@@ -891,6 +891,14 @@ template <typename T>
 xr_status dalloc(Context* ctx, T** p, size_t count) {
     return cuda_check(ctx, cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)), "cudaMalloc (bvh)");
 }
+// Scratch of a build: stream-ordered allocations from the context's pool
+// (rebuilding a top-level BVH every frame would otherwise spend a millisecond in
+// cudaMalloc / cudaFree, each of which also waits for the device).
+template <typename T>
+xr_status salloc(Context* ctx, T** p, size_t count) {
+    return pool_alloc(ctx, p, count, "bvh scratch");
+}
+inline void sfree(Context* ctx, void* p) { pool_free(ctx, p); }
 
 }  // namespace
 
@@ -922,15 +930,17 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
     const uint32_t nint = n > 1 ? n - 1 : 1;
     const uint32_t chunk = 4096;
     const uint32_t nblk = (n + chunk - 1) / chunk;
-    if ((s = dalloc(ctx, &tlo, n)) || (s = dalloc(ctx, &thi, n)) || (s = dalloc(ctx, &k0, n)) ||
-        (s = dalloc(ctx, &k1, n)) || (s = dalloc(ctx, &v0, n)) || (s = dalloc(ctx, &v1, n)) ||
-        (s = dalloc(ctx, &bounds, 8)) || (s = dalloc(ctx, &hist, 256 * nblk)) || (s = dalloc(ctx, &left, nint)) ||
-        (s = dalloc(ctx, &right, nint)) || (s = dalloc(ctx, &pint, nint)) || (s = dalloc(ctx, &pleaf, n)) ||
-        (s = dalloc(ctx, &flags, nint + 1)) || (s = dalloc(ctx, &range, nint)) || (s = dalloc(ctx, &nlo, nint)) ||
-        (s = dalloc(ctx, &nhi, nint)) || (s = dalloc(ctx, &ta, n)) || (s = dalloc(ctx, &tb, n)) ||
-        (s = dalloc(ctx, &wa, n)) || (s = dalloc(ctx, &wb, n)) || (s = dalloc(ctx, &counters, 4)) ||
-        (s = dalloc(ctx, &nodes_tmp, nint)) || (s = dalloc(ctx, &B.slots, (size_t)slot_words * n)))
+    if ((s = salloc(ctx, &tlo, n)) || (s = salloc(ctx, &thi, n)) || (s = salloc(ctx, &k0, n)) ||
+        (s = salloc(ctx, &k1, n)) || (s = salloc(ctx, &v0, n)) || (s = salloc(ctx, &v1, n)) ||
+        (s = salloc(ctx, &bounds, 8)) || (s = salloc(ctx, &hist, 256 * nblk)) || (s = salloc(ctx, &left, nint)) ||
+        (s = salloc(ctx, &right, nint)) || (s = salloc(ctx, &pint, nint)) || (s = salloc(ctx, &pleaf, n)) ||
+        (s = salloc(ctx, &flags, nint + 1)) || (s = salloc(ctx, &range, nint)) || (s = salloc(ctx, &nlo, nint)) ||
+        (s = salloc(ctx, &nhi, nint)) || (s = salloc(ctx, &ta, n)) || (s = salloc(ctx, &tb, n)) ||
+        (s = salloc(ctx, &wa, n)) || (s = salloc(ctx, &wb, n)) || (s = salloc(ctx, &counters, 4)) ||
+        (s = salloc(ctx, &nodes_tmp, nint)) ||
+        (!B.slots_into && (s = dalloc(ctx, &B.slots, (size_t)slot_words * n))))
         goto done;
+    if (B.slots_into) B.slots = B.slots_into;
     {
         uint32_t binit[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
         cudaMemcpyAsync(bounds, binit, sizeof(binit), cudaMemcpyHostToDevice, st);
@@ -971,12 +981,12 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
             uint32_t *cref0 = nullptr, *cref1 = nullptr, *nnb = nullptr, *keep = nullptr, *pos = nullptr, *sums = nullptr;
             float4 *clo0 = nullptr, *chi0 = nullptr, *clo1 = nullptr, *chi1 = nullptr;
             const uint32_t nbmax = (n + 1023) / 1024;
-            if ((s = dalloc(ctx, &cref0, n)) || (s = dalloc(ctx, &cref1, n)) || (s = dalloc(ctx, &nnb, n)) ||
-                (s = dalloc(ctx, &keep, n)) || (s = dalloc(ctx, &pos, n)) || (s = dalloc(ctx, &sums, nbmax + 1)) ||
-                (s = dalloc(ctx, &clo0, n)) || (s = dalloc(ctx, &chi0, n)) || (s = dalloc(ctx, &clo1, n)) ||
-                (s = dalloc(ctx, &chi1, n))) {
-                cudaFree(cref0); cudaFree(cref1); cudaFree(nnb); cudaFree(keep); cudaFree(pos); cudaFree(sums);
-                cudaFree(clo0); cudaFree(chi0); cudaFree(clo1); cudaFree(chi1);
+            if ((s = salloc(ctx, &cref0, n)) || (s = salloc(ctx, &cref1, n)) || (s = salloc(ctx, &nnb, n)) ||
+                (s = salloc(ctx, &keep, n)) || (s = salloc(ctx, &pos, n)) || (s = salloc(ctx, &sums, nbmax + 1)) ||
+                (s = salloc(ctx, &clo0, n)) || (s = salloc(ctx, &chi0, n)) || (s = salloc(ctx, &clo1, n)) ||
+                (s = salloc(ctx, &chi1, n))) {
+                sfree(ctx, cref0); sfree(ctx, cref1); sfree(ctx, nnb); sfree(ctx, keep); sfree(ctx, pos); sfree(ctx, sums);
+                sfree(ctx, clo0); sfree(ctx, chi0); sfree(ctx, clo1); sfree(ctx, chi1);
                 goto done;
             }
             cudaMemsetAsync(counters + 3, 0, 4, st);
@@ -1002,16 +1012,16 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
                 cudaMemcpy(&made, counters + 3, 4, cudaMemcpyDeviceToHost);
                 if (made != n - 1) s = fail(ctx, XR_ERR_STATE, "bvh: clustering built the wrong number of nodes");
             }
-            cudaFree(cref0); cudaFree(cref1); cudaFree(nnb); cudaFree(keep); cudaFree(pos); cudaFree(sums);
-            cudaFree(clo0); cudaFree(chi0); cudaFree(clo1); cudaFree(chi1);
+            sfree(ctx, cref0); sfree(ctx, cref1); sfree(ctx, nnb); sfree(ctx, keep); sfree(ctx, pos); sfree(ctx, sums);
+            sfree(ctx, clo0); sfree(ctx, chi0); sfree(ctx, clo1); sfree(ctx, chi1);
             if (s) goto done;
         }
         // SAH decisions for the collapse (XR_BVH_COLLAPSE=greedy: the area-greedy widening)
         const char* coll = getenv("XR_BVH_COLLAPSE");
         const bool sah = n > 1 && !(coll && strcmp(coll, "greedy") == 0);
         if (sah) {
-            if ((s = dalloc(ctx, &sah_cost, 8 * (size_t)nint)) || (s = dalloc(ctx, &sah_dec, kDecStride * (size_t)nint)) ||
-                (s = dalloc(ctx, &sah_flags, nint + 1)))
+            if ((s = salloc(ctx, &sah_cost, 8 * (size_t)nint)) || (s = salloc(ctx, &sah_dec, kDecStride * (size_t)nint)) ||
+                (s = salloc(ctx, &sah_flags, nint + 1)))
                 goto done;
             if (!use_lbvh) k_parents<<<(nint + 255) / 256, 256, 0, st>>>(nint, left, right, pint, pleaf);
             cudaMemsetAsync(sah_flags, 0, (nint + 1) * 4, st);
@@ -1055,7 +1065,8 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
         bflag |= dflag;
         if (ch[3] || bflag) { s = fail(ctx, XR_ERR_STATE, "bvh: inconsistent radix tree"); goto done; }
         if (ch[1] != n) { s = fail(ctx, XR_ERR_STATE, "bvh: triangle slots do not match the primitive count"); goto done; }
-        if ((s = dalloc(ctx, &B.nodes, ch[0]))) goto done;
+        if (B.nodes_into) B.nodes = B.nodes_into;
+        else if ((s = dalloc(ctx, &B.nodes, ch[0]))) goto done;
         cudaMemcpyAsync(B.nodes, nodes_tmp, (size_t)ch[0] * sizeof(WideNode), cudaMemcpyDeviceToDevice, st);
         cudaEventRecord(e1, st);
         if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: finish"))) goto done;
@@ -1065,15 +1076,16 @@ xr_status build_wide(Context* ctx, WideBuild& B) {
         cudaEventElapsedTime(&B.ms, e0, e1);
     }
 done:
-    cudaFree(tlo); cudaFree(thi); cudaFree(k0); cudaFree(k1); cudaFree(v0); cudaFree(v1); cudaFree(bounds);
-    cudaFree(hist); cudaFree(left); cudaFree(right); cudaFree(pint); cudaFree(pleaf); cudaFree(flags);
-    cudaFree(range); cudaFree(nlo); cudaFree(nhi); cudaFree(ta); cudaFree(tb); cudaFree(wa); cudaFree(wb);
-    cudaFree(counters); cudaFree(nodes_tmp);
-    cudaFree(sah_cost); cudaFree(sah_dec); cudaFree(sah_flags);
+    sfree(ctx, tlo); sfree(ctx, thi); sfree(ctx, k0); sfree(ctx, k1); sfree(ctx, v0); sfree(ctx, v1); sfree(ctx, bounds);
+    sfree(ctx, hist); sfree(ctx, left); sfree(ctx, right); sfree(ctx, pint); sfree(ctx, pleaf); sfree(ctx, flags);
+    sfree(ctx, range); sfree(ctx, nlo); sfree(ctx, nhi); sfree(ctx, ta); sfree(ctx, tb); sfree(ctx, wa); sfree(ctx, wb);
+    sfree(ctx, counters); sfree(ctx, nodes_tmp);
+    sfree(ctx, sah_cost); sfree(ctx, sah_dec); sfree(ctx, sah_flags);
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     if (s != XR_OK) {
-        cudaFree(B.slots); B.slots = nullptr;
-        cudaFree(B.nodes); B.nodes = nullptr;
+        if (!B.slots_into) cudaFree(B.slots);
+        if (!B.nodes_into) cudaFree(B.nodes);
+        B.slots = nullptr; B.nodes = nullptr;
         B.level_off.clear();
     }
     return s;
@@ -1103,8 +1115,8 @@ xr_status build_bvh(Context* ctx) {
         // references: pieces of the large triangles, one box per piece
         const uint32_t n = ctx->ntri, nb = (n + 1023) / 1024;
         cudaStream_t st = ctx->stream;
-        if ((s = dalloc(ctx, &dsum, 1)) || (s = dalloc(ctx, &cnt, n)) || (s = dalloc(ctx, &off, n)) ||
-            (s = dalloc(ctx, &sums, nb + 1)))
+        if ((s = salloc(ctx, &dsum, 1)) || (s = salloc(ctx, &cnt, n)) || (s = salloc(ctx, &off, n)) ||
+            (s = salloc(ctx, &sums, nb + 1)))
             goto out;
         cudaMemsetAsync(dsum, 0, sizeof(double), st);
         k_esc_diag<<<(n + 255) / 256, 256, 0, st>>>(ctx->d_tri_idx, ctx->d_vpos, n, dsum);
@@ -1119,7 +1131,7 @@ xr_status build_bvh(Context* ctx) {
         uint32_t nref = 0;
         cudaMemcpyAsync(&nref, sums + nb, 4, cudaMemcpyDeviceToHost, st);
         if ((s = cuda_check(ctx, cudaStreamSynchronize(st), "bvh: split count"))) goto out;
-        if ((s = dalloc(ctx, &rlo, nref)) || (s = dalloc(ctx, &rhi, nref)) || (s = dalloc(ctx, &rprim, nref))) goto out;
+        if ((s = salloc(ctx, &rlo, nref)) || (s = salloc(ctx, &rhi, nref)) || (s = salloc(ctx, &rprim, nref))) goto out;
         k_esc<true><<<(n + 127) / 128, 128, 0, st>>>(ctx->d_tri_idx, ctx->d_vpos, n, thr, nullptr, off, sums, rlo, rhi,
                                                       rprim);
         wb.n = nref;
@@ -1129,7 +1141,11 @@ xr_status build_bvh(Context* ctx) {
     }
     s = build_wide(ctx, wb);
 out:
-    cudaFree(rlo); cudaFree(rhi); cudaFree(rprim); cudaFree(cnt); cudaFree(off); cudaFree(sums); cudaFree(dsum);
+    sfree(ctx, rlo); sfree(ctx, rhi); sfree(ctx, rprim); sfree(ctx, cnt);
+    sfree(ctx, off); sfree(ctx, sums); sfree(ctx, dsum);
+    // a scene build is a one-off: hand its scratch back to the device
+    cudaStreamSynchronize(ctx->stream);
+    cudaMemPoolTrimTo(ctx->pool, 0);
     if (s) return s;
     ctx->d_nodes = wb.nodes;
     ctx->d_tris = wb.slots;

@@ -120,23 +120,31 @@ int part_emin(const Context* c, uint32_t k, const float* world_lo, const float* 
     return exponent_of(amax) - 17;
 }
 
-void bind_instances(Context* c) {
+// Points the frame's scene at the instance arrays. The bounds the traversal
+// checks against are the arrays' capacities, so a rebuild with the same
+// instance count leaves the scene -- and the captured frame graphs -- as they
+// were. Returns whether anything changed.
+bool bind_instances(Context* c) {
     DeviceScene& sc = c->fa.sc;
+    const DeviceScene old = sc;
+    const uint32_t cap = c->d_tlas_nodes ? c->inst_cap : 0u;
     sc.tlas_nodes = c->d_tlas_nodes;
-    sc.n_tlas_nodes = c->n_tlas_nodes;
+    sc.n_tlas_nodes = cap ? std::max(cap, 2u) - 1u : 0u;
     sc.inst_slots = c->d_inst_slots;
-    sc.n_inst_slots = c->n_inst_slots;
+    sc.n_inst_slots = cap;
     sc.inst_xform = c->d_inst_xform;
     sc.n_inst = (uint32_t)c->instances.size();
+    return std::memcmp(&old, &sc, sizeof(sc)) != 0;
 }
 
 }  // namespace
 
 void free_instances(Context* c) {
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    cudaFree(c->d_tlas_nodes); cudaFree(c->d_inst_slots); cudaFree(c->d_inst_xform);
+    // pool memory, released in stream order after the launches that read it
+    pool_free(c, c->d_tlas_nodes); pool_free(c, c->d_inst_slots); pool_free(c, c->d_inst_xform);
     c->d_tlas_nodes = nullptr; c->d_inst_slots = nullptr; c->d_inst_xform = nullptr;
-    c->n_tlas_nodes = 0; c->n_inst_slots = 0;
+    c->n_tlas_nodes = 0; c->n_inst_slots = 0; c->inst_cap = 0;
+    c->tlas_stale = false;
     c->instances.clear();
     c->inst_xform_host.clear();
     bind_instances(c);
@@ -148,35 +156,35 @@ xr_status refit_part(Context* c, uint32_t k, int emin) {
     cudaStream_t st = c->stream;
     float4 *blo = nullptr, *bhi = nullptr;
     xr_status s;
-    if ((s = cuda_check(c, cudaMalloc((void**)&blo, (size_t)c->n_nodes * 16), "refit scratch")) ||
-        (s = cuda_check(c, cudaMalloc((void**)&bhi, (size_t)c->n_nodes * 16), "refit scratch"))) {
-        cudaFree(blo);
+    if ((s = pool_alloc(c, &blo, c->n_nodes, "refit scratch")) || (s = pool_alloc(c, &bhi, c->n_nodes, "refit scratch"))) {
+        pool_free(c, blo);
         return s;
     }
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0); cudaEventCreate(&e1);
-    cudaEventRecord(e0, st);
+    // stream-ordered behind the frames in flight and ahead of the next; no host wait
+    cudaEventRecord(c->refit_ev[0], st);
     launch_refit_slots(c->d_tris, p.slot_off, p.n_slots, c->d_tri_idx, c->d_vpos, st);
     for (size_t L = p.levels.size() - 1; L-- > 0;)
         launch_refit_level(c->d_nodes, p.node_off + p.levels[L], p.levels[L + 1] - p.levels[L], c->d_tris, blo, bhi,
                            emin, st);
-    cudaEventRecord(e1, st);
-    s = cuda_check(c, cudaStreamSynchronize(st), "refit");
-    if (!s) cudaEventElapsedTime(&c->ms_refit, e0, e1);
-    cudaEventDestroy(e0); cudaEventDestroy(e1);
-    cudaFree(blo); cudaFree(bhi);
+    cudaEventRecord(c->refit_ev[1], st);
+    c->refit_timed = true;
+    s = cuda_check(c, cudaGetLastError(), "refit");
+    pool_free(c, blo); pool_free(c, bhi);
     if (!s) p.emin = emin;
+    return s;
+}
+
+xr_status sync_tlas(Context* c) {
+    if (!c->tlas_stale) return XR_OK;
+    const xr_status s = rebuild_tlas(c);
+    if (s) { free_instances(c); invalidate_graphs(c); }
     return s;
 }
 
 xr_status rebuild_tlas(Context* c) {
     const uint32_t n = (uint32_t)c->instances.size();
-    cudaStreamSynchronize(c->stream);
-    invalidate_graphs(c);
-    cudaFree(c->d_tlas_nodes); cudaFree(c->d_inst_slots);
-    c->d_tlas_nodes = nullptr; c->d_inst_slots = nullptr;
+    c->tlas_stale = false;
     c->n_tlas_nodes = 0; c->n_inst_slots = 0;
-    bind_instances(c);
     if (n == 0) return XR_OK;
     // world boxes, records, and the world's bounds
     std::vector<float4> blo(n), bhi(n), rec(4 * (size_t)n);
@@ -212,16 +220,18 @@ xr_status rebuild_tlas(Context* c) {
     }
     if (s) return s;
     float4 *d_lo = nullptr, *d_hi = nullptr, *d_rec = nullptr;
-    if ((s = cuda_check(c, cudaMalloc((void**)&d_lo, (size_t)n * 16), "tlas alloc")) ||
-        (s = cuda_check(c, cudaMalloc((void**)&d_hi, (size_t)n * 16), "tlas alloc")) ||
-        (s = cuda_check(c, cudaMalloc((void**)&d_rec, (size_t)n * 64), "tlas alloc"))) {
-        cudaFree(d_lo); cudaFree(d_hi);
+    if ((s = pool_alloc(c, &d_lo, n, "tlas alloc")) || (s = pool_alloc(c, &d_hi, n, "tlas alloc")) ||
+        (s = pool_alloc(c, &d_rec, 4 * (size_t)n, "tlas alloc"))) {
+        pool_free(c, d_lo); pool_free(c, d_hi);
         return s;
     }
-    cudaMemcpy(d_lo, blo.data(), (size_t)n * 16, cudaMemcpyHostToDevice);
-    cudaMemcpy(d_hi, bhi.data(), (size_t)n * 16, cudaMemcpyHostToDevice);
-    cudaMemcpy(d_rec, rec.data(), (size_t)n * 64, cudaMemcpyHostToDevice);
+    // pageable sources: each copy returns once its bytes are staged, so the vectors may go out of scope
+    cudaMemcpyAsync(d_lo, blo.data(), (size_t)n * 16, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_hi, bhi.data(), (size_t)n * 16, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_rec, rec.data(), (size_t)n * 64, cudaMemcpyHostToDevice, c->stream);
     WideBuild wb;
+    wb.nodes_into = c->d_tlas_nodes;   // in place: stream order puts the build after the last frame's reads
+    wb.slots_into = c->d_inst_slots;
     wb.n = n;
     wb.box_lo = d_lo;
     wb.box_hi = d_hi;
@@ -231,14 +241,12 @@ xr_status rebuild_tlas(Context* c) {
     wb.builder = 2;
     if (const char* e = getenv("XR_TLAS_BUILDER")) wb.builder = strcmp(e, "ploc") == 0 ? 1 : 2;
     s = build_wide(c, wb);
-    cudaFree(d_lo); cudaFree(d_hi); cudaFree(d_rec);
+    pool_free(c, d_lo); pool_free(c, d_hi); pool_free(c, d_rec);
     if (s) return s;
-    c->d_tlas_nodes = wb.nodes;
-    c->d_inst_slots = wb.slots;
     c->n_tlas_nodes = wb.n_nodes;
     c->n_inst_slots = wb.n_slots;
     c->ms_tlas = wb.ms;
-    bind_instances(c);
+    if (bind_instances(c)) invalidate_graphs(c);
     return XR_OK;
 }
 
@@ -266,22 +274,30 @@ xr_status xr_set_instances(XrContext* c, const XrInstance* inst, uint32_t n) {
             return fail(c, XR_ERR_INVALID_ARGUMENT, "set_instances: singular transform of instance " + std::to_string(i));
     }
     DeviceGuard g(c->device);
-    cudaStreamSynchronize(c->stream);
-    free_instances(c);
-    if (n == 0) { invalidate_graphs(c); return XR_OK; }
-    xr_status s = cuda_check(c, cudaMalloc((void**)&c->d_inst_xform, (size_t)n * 96), "instance alloc");
-    if (s) return s;
+    if (n == 0) { free_instances(c); invalidate_graphs(c); return XR_OK; }
+    xr_status s = XR_OK;
+    if (n > c->inst_cap) {   // new arrays; the old ones go back to the pool behind the frames that read them
+        free_instances(c);
+        if ((s = pool_alloc(c, &c->d_inst_xform, 6 * (size_t)n, "instance alloc")) ||
+            (s = pool_alloc(c, &c->d_tlas_nodes, std::max(n, 2u) - 1u, "instance alloc")) ||
+            (s = pool_alloc(c, &c->d_inst_slots, 4 * (size_t)n, "instance alloc"))) {
+            free_instances(c);
+            invalidate_graphs(c);
+            return s;
+        }
+        c->inst_cap = n;
+    }
     std::vector<float4> x6(6 * (size_t)n);
     for (uint32_t i = 0; i < n; i++)
         for (int r = 0; r < 6; r++) {
             const float* q = &xf[24 * (size_t)i + 4 * r];
             x6[6 * i + r] = make_float4(q[0], q[1], q[2], q[3]);
         }
-    cudaMemcpy(c->d_inst_xform, x6.data(), (size_t)n * 96, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(c->d_inst_xform, x6.data(), (size_t)n * 96, cudaMemcpyHostToDevice, c->stream);
     c->instances.assign(inst, inst + n);
     c->inst_xform_host = xf;
     s = rebuild_tlas(c);
-    if (s) free_instances(c);
+    if (s) { free_instances(c); invalidate_graphs(c); }
     return s;
 }
 
@@ -311,19 +327,19 @@ xr_status xr_update_vertices(XrContext* c, uint32_t scene, const XrVertex* v, ui
         uv[i] = make_float2(v[i].tex_coord[0], v[i].tex_coord[1]);
     }
     DeviceGuard g(c->device);
-    cudaStreamSynchronize(c->stream);
     xr_status s = XR_OK;
-    if (count) {
-        cudaMemcpy(c->d_vpos + p.vert_off, pos.data(), (size_t)count * 16, cudaMemcpyHostToDevice);
-        cudaMemcpy(c->d_vnrm + p.vert_off, nrm.data(), (size_t)count * 16, cudaMemcpyHostToDevice);
-        cudaMemcpy(c->d_vuv + p.vert_off, uv.data(), (size_t)count * 8, cudaMemcpyHostToDevice);
+    if (count) {   // in stream order after the frames that still read the old vertices
+        cudaMemcpyAsync(c->d_vpos + p.vert_off, pos.data(), (size_t)count * 16, cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(c->d_vnrm + p.vert_off, nrm.data(), (size_t)count * 16, cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(c->d_vuv + p.vert_off, uv.data(), (size_t)count * 8, cudaMemcpyHostToDevice, c->stream);
         if ((s = cuda_check(c, cudaGetLastError(), "update_vertices"))) return s;
         for (int k = 0; k < 3; k++) { p.lo[k] = lo[k]; p.hi[k] = hi[k]; }
     }
     if (c->parts.size() == 1) {
         for (int k = 0; k < 3; k++) { c->scene_lo[k] = p.lo[k]; c->scene_hi[k] = p.hi[k]; }
         cache_scene_bounds(c, reinterpret_cast<const float*>(v), count);
-        if (c->n_lights) {   // light areas follow the vertices
+        if (c->n_lights) {   // light areas follow the vertices; the frames in flight still read the old tables
+            cudaStreamSynchronize(c->stream);
             std::vector<uint4> tri(c->ntri);
             std::vector<XrMaterial> mats(c->nm);
             cudaMemcpy(tri.data(), c->d_tri_idx, (size_t)c->ntri * 16, cudaMemcpyDeviceToHost);
@@ -339,7 +355,8 @@ xr_status xr_update_vertices(XrContext* c, uint32_t scene, const XrVertex* v, ui
     // the finest grid: the new coordinates, and the instanced world when there is one
     int emin = part_emin(c, scene, nullptr, nullptr);
     if ((s = refit_part(c, scene, emin))) return s;
-    if (!c->instances.empty()) return rebuild_tlas(c);
+    // the top level follows at the next render or trace, once for any number of updates
+    if (!c->instances.empty()) c->tlas_stale = true;
     return XR_OK;
 }
 

@@ -84,7 +84,8 @@ extern "C" xr_status xr_trace_rays_noalloc(XrContext* c, const float* rays, uint
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     if (prev != c->device) cudaSetDevice(c->device);
     TraceScratch* s = nullptr;
-    xr_status st = scratch_for(c, &s);
+    xr_status st = sync_tlas(c);   // a stale top level is rebuilt first (the only allocation on this path)
+    if (!st) st = scratch_for(c, &s);
     if (!st) {
         cudaStream_t sm = c->stream;
         cudaMemsetAsync(&s->flags, 0, 2 * sizeof(uint32_t), sm);   // flags and fetch

@@ -39,6 +39,15 @@ xr_status cuda_check(Context* ctx, cudaError_t e, const char* what) {
     return fail(ctx, code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+xr_status pool_alloc_bytes(Context* ctx, void** p, size_t bytes, const char* what) {
+    *p = nullptr;
+    return cuda_check(ctx, cudaMallocFromPoolAsync(p, bytes, ctx->pool, ctx->stream), what);
+}
+
+void pool_free(Context* ctx, void* p) {
+    if (p) cudaFreeAsync(p, ctx->stream);
+}
+
 void invalidate_graphs(Context* c) {
     for (int i = 0; i < 2; i++) {
         if (c->graph[i]) cudaGraphExecDestroy(c->graph[i]);
@@ -309,6 +318,17 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     if (prop.major < 10) { s = fail(c, XR_ERR_UNSUPPORTED, "create: this library is built for sm_103a (GB300)"); goto bad; }
     c->sm_count = prop.multiProcessorCount;
     if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) goto bad;
+    {   // the context's own pool: freed scratch stays cached for the next build instead of going back to the driver
+        cudaMemPoolProps pp{};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.handleTypes = cudaMemHandleTypeNone;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = c->device;
+        if ((s = cuda_check(c, cudaMemPoolCreate(&c->pool, &pp), "memory pool"))) goto bad;
+        uint64_t keep = UINT64_MAX;
+        if ((s = cuda_check(c, cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep), "memory pool")))
+            goto bad;
+    }
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_counters, kCounterWords * 4), "counters"))) goto bad;
     if ((s = cuda_check(c, cudaMemset(c->d_counters, 0, kCounterWords * 4), "counters"))) goto bad;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_work, 2 * sizeof(unsigned long long)), "work counters"))) goto bad;
@@ -319,6 +339,8 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
         if ((s = cuda_check(c, cudaEventCreate(&c->ev[i]), "event"))) goto bad;
     for (int i = 0; i < 8; i++)
         if ((s = cuda_check(c, cudaEventCreate(&c->user_ev[i]), "event"))) goto bad;
+    for (int i = 0; i < 2; i++)
+        if ((s = cuda_check(c, cudaEventCreate(&c->refit_ev[i]), "event"))) goto bad;
     cudaEventRecord(c->ev[5], c->stream);
     {
         XrParams p;
@@ -350,6 +372,9 @@ void xr_destroy(XrContext* c) {
     if (c->h_ubo) cudaFreeHost(c->h_ubo);
     for (int i = 0; i < 8; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
+    for (int i = 0; i < 2; i++) if (c->refit_ev[i]) cudaEventDestroy(c->refit_ev[i]);
+    if (c->stream) cudaStreamSynchronize(c->stream);   // pool frees queued by free_instances
+    if (c->pool) cudaMemPoolDestroy(c->pool);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -616,8 +641,9 @@ static xr_status render_impl(Context* c, const XrUniformBufferObject* ubos, uint
     if (c->params.compat_reference && c->scene_has_non_lambert)
         return fail(c, XR_ERR_UNSUPPORTED, std::string(who) + ": reference mode renders only Lambertian and DiffuseLight materials");
     DeviceGuard g(c->device);
-    xr_status s = stage_ubos(c, ubos, n);
+    xr_status s = sync_tlas(c);
     if (s) return s;
+    if ((s = stage_ubos(c, ubos, n))) return s;
     const uint32_t parity = ubos[0].current_frame % 2u;
     set_frame_pointers(c, parity);
     if ((s = cache_prepare_frame(c, ubos[0].current_frame))) return s;
@@ -783,10 +809,11 @@ static xr_status render_reference_impl(XrContext* c, const XrUniformBufferObject
     if (c->params.compat_reference && c->scene_has_non_lambert)
         return fail(c, XR_ERR_UNSUPPORTED, std::string(who) + ": reference mode renders only Lambertian and DiffuseLight materials");
     DeviceGuard g(c->device);
+    xr_status s = sync_tlas(c);
+    if (s) return s;
     const size_t n3 = (size_t)c->N * 3;
     double* acc = nullptr;
-    xr_status s = cuda_check(c, cudaMalloc((void**)&acc, n3 * sizeof(double)), "render_reference alloc");
-    if (s) return s;
+    if ((s = cuda_check(c, cudaMalloc((void**)&acc, n3 * sizeof(double)), "render_reference alloc"))) return s;
     cudaMemsetAsync(acc, 0, n3 * sizeof(double), c->stream);
     std::vector<XrUniformBufferObject> u(ubos, ubos + n);
     for (uint32_t k = 0; k < spp && !s; k++) {
@@ -864,7 +891,12 @@ xr_status xr_output_device_ptr(XrContext* c, uint32_t which, void** dptr) {
 xr_status xr_get_stats(XrContext* c, XrStats* st) {
     if (!c || !st) return fail(c, XR_ERR_INVALID_ARGUMENT, "get_stats: null argument");
     DeviceGuard g(c->device);
-    xr_status s = xr_sync(c);
+    xr_status s = sync_tlas(c);
+    if (!s) s = xr_sync(c);
+    if (!s && c->refit_timed) {
+        cudaEventElapsedTime(&c->ms_refit, c->refit_ev[0], c->refit_ev[1]);
+        c->refit_timed = false;
+    }
     XrStats o;
     memset(&o, 0, sizeof(o));
     o.frames = c->frames;
@@ -970,8 +1002,9 @@ xr_status xr_run_pass(XrContext* c, const XrUniformBufferObject* ubo, uint32_t p
     if (pass != 1 && pass != 2) return fail(c, XR_ERR_INVALID_ARGUMENT, "run_pass: pass must be 1 (temporal) or 2 (spatial)");
     if (!c->params_set || !c->bvh_ready) return fail(c, XR_ERR_STATE, "run_pass: parameters and BVH required");
     DeviceGuard g(c->device);
-    xr_status s = upload_ubo(c, ubo);
+    xr_status s = sync_tlas(c);
     if (s) return s;
+    if ((s = upload_ubo(c, ubo))) return s;
     set_frame_pointers(c, ubo->current_frame % 2u);
     const bool compat = c->params.compat_reference != 0;
     if (pass == 1 && !compat && c->params.temporal_on) launch_reproject(c->fa, c->stream);
@@ -988,6 +1021,7 @@ static xr_status trace_device(XrContext* c, const float* d_rays, uint32_t n, int
     if (!c->bvh_ready) return fail(c, XR_ERR_STATE, "trace: build the BVH first");
     if (n && (!d_rays || !d_prim || !d_t || !d_bary)) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null array");
     DeviceGuard g(c->device);
+    if (xr_status s0 = sync_tlas(c)) return s0;
     cudaMemsetAsync(c->d_counters + kCntFetchQuery, 0, 4, c->stream);
     cudaMemsetAsync(c->d_work, 0, 2 * sizeof(unsigned long long), c->stream);
     c->query_rays = n;

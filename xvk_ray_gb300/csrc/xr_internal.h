@@ -214,6 +214,10 @@ struct WideBuild {
     const uint32_t* ref_prim = nullptr;   // box input of triangle pieces: the triangle of each box
     int emin_floor = -1000;             // lower bound of the finest grid exponent
     int builder = 0;                    // 0: XR_BVH_BUILDER (PLOC unless "lbvh"), 1: PLOC, 2: LBVH
+    // Caller's arrays to build into (capacity max(n - 1, 1) nodes and 4 n slot words); the build allocates its
+    // own when they are null.
+    WideNode* nodes_into = nullptr;
+    float4* slots_into = nullptr;
     WideNode* nodes = nullptr;          // device arrays owned by the caller afterwards
     float4* slots = nullptr;
     uint32_t n_nodes = 0, n_slots = 0, depth = 0;
@@ -225,6 +229,7 @@ struct WideBuild {
 struct Context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;   // stream-ordered scratch of builds and refits, kept cached between frames
     int sm_count = 0;
     XrParams params{};
     bool params_set = false;
@@ -268,8 +273,12 @@ struct Context {
     float4* d_inst_xform = nullptr;
     WideNode* d_tlas_nodes = nullptr;
     float4* d_inst_slots = nullptr;
-    uint32_t n_tlas_nodes = 0, n_inst_slots = 0;
+    uint32_t n_tlas_nodes = 0, n_inst_slots = 0;   // of the last top-level build
+    uint32_t inst_cap = 0;   // instances the transform, top-level node and slot arrays have room for
+    bool tlas_stale = false;   // a bottom-level refit moved instanced geometry: rebuild before the next use
     float ms_tlas = 0.0f, ms_refit = 0.0f;
+    cudaEvent_t refit_ev[2] = {};   // around the last refit; read by xr_get_stats once the stream is idle
+    bool refit_timed = false;
 
     // per-pixel buffers
     uint32_t W = 0, H = 0, N = 0;
@@ -318,6 +327,13 @@ xr_status realloc_pixels(Context* c);   // per-pixel buffers and view table for 
 
 xr_status fail(const Context* ctx, xr_status code, const std::string& msg);
 xr_status cuda_check(Context* ctx, cudaError_t e, const char* what);
+// Stream-ordered allocations from the context's pool, ordered on its stream.
+xr_status pool_alloc_bytes(Context* ctx, void** p, size_t bytes, const char* what);
+template <typename T>
+inline xr_status pool_alloc(Context* ctx, T** p, size_t count, const char* what) {
+    return pool_alloc_bytes(ctx, (void**)p, (count ? count : 1) * sizeof(T), what);
+}
+void pool_free(Context* ctx, void* p);
 xr_status check_flags(Context* c);   // reads the sticky device error word; new bits -> error status
 
 // Makes `dev` current for the scope of a C ABI call and restores the caller's device.
@@ -345,6 +361,7 @@ void free_lights(Context* c);
 xr_status upload_lights(Context* c, const std::vector<uint4>& tri, const std::vector<float4>& pos,
                         const XrMaterial* m, uint32_t nm);
 xr_status rebuild_tlas(Context* c);                           // instances.cu
+xr_status sync_tlas(Context* c);   // instances.cu: rebuild a stale top level (no-op otherwise)
 void free_instances(Context* c);                              // instances.cu
 
 // ---- launch wrappers (trace.cu) ----
