@@ -69,7 +69,7 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // maps the ray into the instance's object space (origin and direction by its
 // world-to-object rows; t is unchanged) and continues at the root of its
 // bottom-level BVH in sc.nodes.  Popping the marker restores the world-space ray
-// (reloaded from the queue).  Hits compare t, then instance, then primitive.
+// (kept in the lane's registers or local memory since the ray's start).  Hits compare t, then instance, then primitive.
 template <bool ANY, bool INST = false, typename LoadRay, typename StoreHit>
 __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t count, uint32_t* next,
                                                  LoadRay load, StoreHit store, uint32_t* err,
@@ -95,6 +95,11 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
     bool in_blas = !INST;    // INST: the lane's ray is in an instance's object space
     int32_t cur_inst = -1;   // that instance
     h.inst = -1;
+    // INST: the world-space ray and its box-test state, kept for instance entries
+    // and for the return to the top level (no reload, no reciprocals recomputed)
+    float3 wo = f3(0, 0, 0), wd = f3(0, 0, 0);
+    float widx = 0, widy = 0, widz = 0;
+    uint32_t wflip = 0;
     // box-test reciprocals and sign bits of a direction (see the comment at the ray start)
     auto set_dir = [&](float3 d) {
         idx = 1.0f / copysignf(fmaxf(fabsf(d.x), kMinDir), d.x);
@@ -133,6 +138,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     // planes as its infinite reciprocal).
                     set_dir(r.d);
                     rt = prep_ray(r.o, r.d);
+                    if (INST) { wo = r.o; wd = r.d; widx = idx; widy = idy; widz = idz; wflip = flip; }
                     h.prim = -1; h.t = r.tmax; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = -1;
                     sp = 0;
                     tg_mask = 0;
@@ -258,9 +264,8 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                     if (tg_mask) stack[sp++] = make_uint2(tg_base, tg_mask | kTriGroupBit);
                     stack[sp++] = make_uint2(0u, kLevelBit);
                     tg_mask = 0u;
-                    const RayIn wr = load(ray_id);
-                    o = xform_point(m0, m1, m2, wr.o);
-                    const float3 od = xform_dir(m0, m1, m2, wr.d);
+                    o = xform_point(m0, m1, m2, wo);
+                    const float3 od = xform_dir(m0, m1, m2, wd);
                     set_dir(od);
                     rt = prep_ray(o, od);
                     cur_inst = (int32_t)__float_as_uint(m3.x);
@@ -294,20 +299,22 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
 
         // ---- pop or finish ----
         if (active && tg_mask == 0u && !(ng_bits & 0xFFu)) {
+            if (INST && sp > 0 && stack[sp - 1].y == kLevelBit) {
+                // back to the top level: the world-space ray, then (same step) the
+                // top-level work saved under the marker -- markers are never adjacent
+                --sp;
+                o = wo;
+                idx = widx; idy = widy; idz = widz;
+                flip = wflip;
+                in_blas = false;
+                cur_inst = -1;
+            }
             if (sp == 0) {
                 store(ray_id, h);
                 active = false;
             } else {
                 const uint2 e = stack[--sp];
-                if (INST && e.y == kLevelBit) {
-                    // back to the top level: the world-space ray
-                    const RayIn wr = load(ray_id);
-                    o = wr.o;
-                    set_dir(wr.d);
-                    in_blas = false;
-                    cur_inst = -1;
-                    ng_bits = 0u;
-                } else if (e.y & kTriGroupBit) { tg_base = e.x; tg_mask = e.y & 0x00FFFFFFu; ng_bits = 0u; }
+                if (e.y & kTriGroupBit) { tg_base = e.x; tg_mask = e.y & 0x00FFFFFFu; ng_bits = 0u; }
                 else { ng_base = e.x; ng_bits = e.y; }
             }
         }
