@@ -31,6 +31,21 @@ def test_struct_layouts_match_the_reference():
     assert L.load().xr_api_version() == 1
 
 
+def test_instance_records_pack_like_the_struct():
+    """pack_instances gives the bytes a ctypes XrInstance array holds (matrices
+    rounded to float the same way), and passes record arrays through unchanged."""
+    rng = np.random.default_rng(4)
+    pairs = [(int(k), rng.normal(size=(3, 4))) for k in rng.integers(0, 5, 9)]
+    arr = xr.pack_instances(pairs)
+    ref = (L.XrInstance * len(pairs))()
+    for i, (k, m) in enumerate(pairs):
+        ref[i].scene = k
+        ref[i].object_to_world[:] = [float(x) for x in m.reshape(12)]
+    assert arr.tobytes() == bytes(ref)
+    assert xr.pack_instances(arr) is arr or np.array_equal(xr.pack_instances(arr), arr)
+    assert xr.pack_instances([]).shape == (0,)
+
+
 def test_no_silent_cpu_fallback():
     """Creating a context needs a CUDA device; without one the call fails loudly."""
     lib = L.load()
