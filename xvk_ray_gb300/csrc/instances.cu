@@ -70,24 +70,55 @@ void inverse_double(const float w[12], double o[12]) {
     }
 }
 
+// World box of an instance: the corners of the root node's child boxes (or, before
+// they are known, of the part's vertex bounds) mapped by the object-to-world
+// transform in double precision, rounded outwards.  The child boxes contain the
+// geometry with the quantisation slack, and for a rotated instance their union
+// maps to a much smaller box than the part's axis-aligned bounds.
 void world_box(const ScenePart& p, const float w2o[12], float lo[3], float hi[3]) {
     double m[12];
     inverse_double(w2o, m);
     double l[3] = {INFINITY, INFINITY, INFINITY}, u[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int corner = 0; corner < 8; corner++) {
-        const double x = (corner & 1) ? p.hi[0] : p.lo[0];
-        const double y = (corner & 2) ? p.hi[1] : p.lo[1];
-        const double z = (corner & 4) ? p.hi[2] : p.lo[2];
-        for (int k = 0; k < 3; k++) {
-            const double v = m[4 * k] * x + m[4 * k + 1] * y + m[4 * k + 2] * z + m[4 * k + 3];
-            l[k] = std::min(l[k], v);
-            u[k] = std::max(u[k], v);
+    const double whole[6] = {p.lo[0], p.lo[1], p.lo[2], p.hi[0], p.hi[1], p.hi[2]};
+    const size_t nb = p.root_boxes.empty() ? 1 : p.root_boxes.size() / 6;
+    for (size_t b = 0; b < nb; b++) {
+        const double* bx = p.root_boxes.empty() ? whole : &p.root_boxes[6 * b];
+        for (int corner = 0; corner < 8; corner++) {
+            const double x = bx[(corner & 1) ? 3 : 0];
+            const double y = bx[(corner & 2) ? 4 : 1];
+            const double z = bx[(corner & 4) ? 5 : 2];
+            for (int k = 0; k < 3; k++) {
+                const double v = m[4 * k] * x + m[4 * k + 1] * y + m[4 * k + 2] * z + m[4 * k + 3];
+                l[k] = std::min(l[k], v);
+                u[k] = std::max(u[k], v);
+            }
         }
     }
     for (int k = 0; k < 3; k++) {
         lo[k] = std::nextafter((float)l[k], -INFINITY);
         hi[k] = std::nextafter((float)u[k], INFINITY);
     }
+}
+
+// Reads part p's root node back and decodes its child boxes: plane = origin + q 2^e
+// per axis (the quantised grid of the node), children with a zero meta byte absent.
+xr_status read_root_boxes(Context* c, ScenePart& p) {
+    if (!p.root_boxes.empty() || p.n_nodes == 0) return XR_OK;
+    WideNode nd;
+    cudaMemcpyAsync(&nd, c->d_nodes + p.node_off, sizeof(nd), cudaMemcpyDeviceToHost, c->stream);
+    if (xr_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "root boxes")) return s;
+    const double org[3] = {nd.px, nd.py, nd.pz};
+    double cell[3];
+    for (int k = 0; k < 3; k++) cell[k] = std::ldexp(1.0, (int)((nd.exyz_imask >> (8 * k)) & 0xFFu) - 127);
+    for (uint32_t slot = 0; slot < 8; slot++) {
+        const uint32_t word = slot < 4 ? 0u : 1u, shift = 8u * (slot & 3u);
+        if (((nd.meta[word] >> shift) & 0xFFu) == 0u) continue;
+        for (int k = 0; k < 3; k++)
+            p.root_boxes.push_back(org[k] + (double)((nd.q[2 * k + word] >> shift) & 0xFFu) * cell[k]);
+        for (int k = 0; k < 3; k++)
+            p.root_boxes.push_back(org[k] + (double)((nd.q[6 + 2 * k + word] >> shift) & 0xFFu) * cell[k]);
+    }
+    return XR_OK;
 }
 
 int exponent_of(double v) {   // e with 2^(e-1) <= v < 2^e (v > 0)
@@ -152,6 +183,7 @@ void free_instances(Context* c) {
 
 xr_status refit_part(Context* c, uint32_t k, int emin) {
     ScenePart& p = c->parts[k];
+    p.root_boxes.clear();   // new boxes below: read again on next use
     if (p.n_nodes == 0 || p.levels.size() < 2) { p.emin = emin; return XR_OK; }
     cudaStream_t st = c->stream;
     float4 *blo = nullptr, *bhi = nullptr;
@@ -186,6 +218,8 @@ xr_status rebuild_tlas(Context* c) {
     c->tlas_stale = false;
     c->n_tlas_nodes = 0; c->n_inst_slots = 0;
     if (n == 0) return XR_OK;
+    for (const XrInstance& in : c->instances)
+        if (xr_status s0 = read_root_boxes(c, c->parts[in.scene])) return s0;
     // world boxes, records, and the world's bounds
     std::vector<float4> blo(n), bhi(n), rec(4 * (size_t)n);
     float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};

@@ -200,6 +200,9 @@ struct ScenePart {
     std::vector<uint32_t> levels;
     int emin = 0;
     float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    // the root node's child boxes as stored (lo xyz, hi xyz per child), read back on first
+    // use after each build or refit: the instance world boxes are taken over them
+    std::vector<double> root_boxes;
 };
 
 // Input and output of a wide-BVH build (bvh_build.cu): triangles (tri_idx, vpos),
