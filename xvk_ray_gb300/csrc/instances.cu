@@ -7,13 +7,18 @@
 // ObjectToWorld / WorldToObject (Ray.rchit.hlsl:46-55).  Here:
 //   * each scene's BVH (xr_build_bvh, xr_upload_scenes) is a bottom-level BVH;
 //   * xr_set_instances takes object-to-world transforms, inverts them in double
-//     precision, bounds every instance in world space (the object box's corners
-//     through the exact inverse of the float world-to-object map, rounded
-//     outwards) and builds an 8-wide top-level BVH over those boxes with the same
-//     device builder as the scenes; its leaves are 64-byte instance records
-//     {world-to-object rows, instance, bottom-level root};
+//     precision, bounds every instance in world space (the corners of its scene's
+//     root-node child boxes through the exact inverse of the float world-to-object
+//     map, rounded outwards) and builds an 8-wide top-level BVH over those boxes
+//     with the same device builder as the scenes; its leaves are 64-byte instance
+//     records {world-to-object rows, instance, bottom-level root}.  The instance
+//     arrays keep their addresses while the count stays within their capacity, so
+//     the frame graphs captured over them stay valid;
 //   * xr_update_vertices writes new vertices and refits the scene's BVH on the
-//     device, one launch per level from the deepest (bvh_build.cu).
+//     device, one launch per level from the deepest (bvh_build.cu), in stream
+//     order without a host wait; with instances it marks the top-level BVH stale
+//     and the next trace, frame or statistics call rebuilds it (sync_tlas).
+// Scratch of builds and refits comes from the context's stream-ordered pool.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
