@@ -173,13 +173,14 @@ RELMSE_EVAL_FRAMES = (16, 24, 32, 40, 48)
 
 
 def _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, cache: bool, n_neighbours: int,
-                train_samples: int) -> dict:
+                train_samples: int, visibility: int = 1) -> dict:
     """One variant along the camera path: relMSE at the evaluation frames (FP64
     references computed once and shared) and its median frame time."""
     import numpy as np
     L = xr._lib
     r = xr.Renderer(W, H, device=device)
     p = xr.params_default(W, H, write_hdr=1, write_pt=1)
+    p.visibility = visibility
     if n_neighbours == 0:
         p.spatial_on = 0
     else:
@@ -209,7 +210,8 @@ def _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, cache: bool
             rel.append(relmse(hdr, refs[f + 1]))
             rel_pt.append(relmse(r.read_output(L.XR_OUT_PT), refs[f + 1]))
     entry = {"relmse": float(np.mean(rel)), "per_frame": [round(v, 4) for v in rel],
-             "ms_per_frame": round(statistics.median(ms[8:]), 4), "n_neighbours": n_neighbours}
+             "ms_per_frame": round(statistics.median(ms[8:]), 4), "n_neighbours": n_neighbours,
+             "shadow_rays": bool(visibility and n_neighbours)}
     if cache:
         cs = r.cache.stats()
         entry.update({"ms_infer": round(statistics.median(infer[8:]), 4),
@@ -224,23 +226,27 @@ def _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, cache: bool
 def measure_relmse(xr, scene, ubos, eval_frames, ref_spp: int, device: int, train_samples: int = 65536) -> dict:
     """relMSE against the FP64-accumulated reference (plain path tracer, `ref_spp`
     samples, at each evaluation frame's camera), averaged over the evaluation
-    frames, for: plain ReSTIR GI (5 neighbours), ReSTIR GI + learned radiance
-    cache with the same reuse settings, and ReSTIR GI + cache at equal frame
-    time -- the most spatial neighbours (5 .. 0) whose median frame time does not
-    exceed plain ReSTIR GI's."""
+    frames, for: plain ReSTIR GI (5 neighbours, shadow rays), ReSTIR GI + learned
+    radiance cache with the same reuse settings, and ReSTIR GI + cache at equal
+    frame time -- the first of: the same settings, then without the spatial
+    pass's shadow rays with 5, 4, .. 0 neighbours, whose median frame time does
+    not exceed plain ReSTIR GI's (the cache's own settings stay as configured)."""
     refs = {}
     plain = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, False, 5, train_samples)
     same = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, 5, train_samples)
     equal = same
-    for nb in (4, 3, 2, 1, 0):
+    for nb in (5, 4, 3, 2, 1, 0):
         if equal["ms_per_frame"] <= plain["ms_per_frame"]:
             break
-        equal = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, nb, train_samples)
+        equal = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, nb, train_samples, 0)
+    # for comparison: plain ReSTIR GI without the spatial shadow rays
+    plain_nv = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, False, 5, train_samples, 0)
     return {"restir_gi": plain["relmse"], "restir_gi_mlp_cache": same["relmse"], "pt_1spp": plain["pt_1spp"],
             "ratio_cache_over_plain": round(same["relmse"] / plain["relmse"], 4),
             "restir_gi_mlp_cache_equal_time": equal["relmse"],
             "ratio_equal_time": round(equal["relmse"] / plain["relmse"], 4),
-            "detail": {"restir_gi": plain, "restir_gi_mlp_cache": same, "restir_gi_mlp_cache_equal_time": equal},
+            "detail": {"restir_gi": plain, "restir_gi_mlp_cache": same, "restir_gi_mlp_cache_equal_time": equal,
+                       "restir_gi_no_shadow_rays": plain_nv},
             "reference": f"FP64-accumulated plain path tracer, {ref_spp} spp, same path depth, "
                          f"at frames {list(eval_frames)} of the camera path",
             "eps": RELMSE_EPS, "reference_seconds": round(refs.get("seconds", 0.0), 2)}
