@@ -24,8 +24,14 @@ namespace xr {
 
 constexpr uint32_t kTriGroupBit = 0x80000000u;   // stack entry holds a triangle group
 constexpr uint32_t kLevelBit = 0x40000000u;      // stack entry marks the return to the top-level BVH
-constexpr int kPostponeBelow = 8;                 // lanes; fewer testing triangles -> postpone
-constexpr int kRefillMin = 8;                     // idle lanes before a refill (swept 1..16: 1 is 9% slower)
+#ifndef XR_POSTPONE_BELOW
+#define XR_POSTPONE_BELOW 8
+#endif
+#ifndef XR_REFILL_MIN
+#define XR_REFILL_MIN 8
+#endif
+constexpr int kPostponeBelow = XR_POSTPONE_BELOW;  // lanes; fewer testing triangles -> postpone
+constexpr int kRefillMin = XR_REFILL_MIN;          // idle lanes before a refill (swept 1..16: 1 is 9% slower)
 constexpr float kMinDir = 1e-20f;                 // smallest direction component seen by the box test
 
 struct RayIn {
