@@ -1092,6 +1092,7 @@ done:
 }
 
 xr_status build_bvh(Context* ctx) {
+    NvtxRange nvtx_range("xr bvh build");
     if (ctx->d_nodes) { cudaFree(ctx->d_nodes); ctx->d_nodes = nullptr; }
     if (ctx->d_tris) { cudaFree(ctx->d_tris); ctx->d_tris = nullptr; }
     ctx->n_nodes = 0; ctx->n_tri_slots = 0; ctx->bvh_depth = 0;

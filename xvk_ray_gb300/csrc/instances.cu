@@ -187,6 +187,7 @@ void free_instances(Context* c) {
 }
 
 xr_status refit_part(Context* c, uint32_t k, int emin) {
+    NvtxRange nvtx_range("xr refit");
     ScenePart& p = c->parts[k];
     p.root_boxes.clear();   // new boxes below: read again on next use
     if (p.n_nodes == 0 || p.levels.size() < 2) { p.emin = emin; return XR_OK; }
@@ -219,6 +220,7 @@ xr_status sync_tlas(Context* c) {
 }
 
 xr_status rebuild_tlas(Context* c) {
+    NvtxRange nvtx_range("xr top-level build");
     const uint32_t n = (uint32_t)c->instances.size();
     c->tlas_stale = false;
     c->n_tlas_nodes = 0; c->n_inst_slots = 0;

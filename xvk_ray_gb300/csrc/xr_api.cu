@@ -629,6 +629,7 @@ static xr_status enqueue_frame(Context* c, uint32_t n_ubo, uint32_t nb, bool reu
 
 // One frame of the context's n views (n = 1 for xr_render_frame).
 static xr_status render_impl(Context* c, const XrUniformBufferObject* ubos, uint32_t n, const char* who) {
+    NvtxRange nvtx_range("xr frame");
     if (!c->params_set) return fail(c, XR_ERR_STATE, std::string(who) + ": set the parameters (extent) first");
     if (!c->bvh_ready) return fail(c, XR_ERR_STATE, std::string(who) + ": build the BVH first");
     const uint32_t nb = ubos[0].number_of_bounces;

@@ -35,8 +35,18 @@ struct __half2;
 #else
 #include <cuda_runtime_api.h>
 #endif
+#include <nvtx3/nvToolsExt.h>
 
 namespace xr {
+
+// An NVTX range over a host-side scope (frame, BVH build, top-level rebuild, refit, cache
+// step): visible to a profiler's timeline, a no-op call otherwise (NVTX v3 is header-only).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr int kStackSize = 40;
