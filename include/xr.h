@@ -409,7 +409,11 @@ typedef struct XrCacheStats {
 enum { XR_CACHE_MLP = 0, XR_CACHE_GRID = 1, XR_CACHE_MLP_GRAD = 2, XR_CACHE_GRID_GRAD = 3,
        XR_CACHE_MLP_M = 4, XR_CACHE_MLP_V = 5, XR_CACHE_GRID_M = 6, XR_CACHE_GRID_V = 7,
        XR_CACHE_QUERIES = 8,        /* last frame's query records, 8 words each */
-       XR_CACHE_TRAIN_RECORDS = 9   /* last frame's training records, 12 words each */ };
+       XR_CACHE_TRAIN_RECORDS = 9,  /* last frame's training records, 12 words each */
+       XR_CACHE_ADAM_STEP = 10      /* one uint32: Adam steps taken; writing it also sets the
+                                       bias-correction state (beta1^t, beta2^t of the current
+                                       parameters).  With arrays 0..7 the whole trained state,
+                                       for checkpoint and resume */ };
 /* MLP arrays: 17,408 floats, layer l < 4 at l * 4096 as [64 out][64 in], layer 4 at
    16384 as [16 out][64 in] (outputs 3..15 unused).  Table arrays: 16 x 2^19 x 2
    floats, level-major, 2 features per entry (the binary16 table is derived). */
@@ -427,7 +431,7 @@ xr_status xr_cache_train(XrContext* ctx, const XrCacheSample* s, uint32_t n, int
 /* One Adam step on the current gradients (e.g. written with xr_cache_write), which it then zeroes. */
 xr_status xr_cache_step(XrContext* ctx);
 xr_status xr_cache_read(XrContext* ctx, int which, void* host, size_t bytes, size_t* bytes_needed);
-xr_status xr_cache_write(XrContext* ctx, int which, const void* host, size_t bytes);   /* arrays 0..7 */
+xr_status xr_cache_write(XrContext* ctx, int which, const void* host, size_t bytes);   /* arrays 0..7, step 10 */
 xr_status xr_cache_get_stats(XrContext* ctx, XrCacheStats* out);
 
 const char* xr_last_error(const XrContext* ctx);   /* ctx may be NULL: last global error */

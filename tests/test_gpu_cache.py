@@ -147,3 +147,37 @@ def test_training_converges():
     assert np.all(np.isfinite(losses))
     assert np.mean(losses[-20:]) < 0.1 * np.mean(losses[:5])
     assert after < 0.1 * before, (before, after)
+
+
+def test_checkpoint_resume_is_exact():
+    """A trained cache saved with checkpoint() (arrays 0..7 and the Adam step count) and
+    restored into a fresh context predicts bit-identically, and the next Adam step
+    (which reads the step count for its bias correction) gives bit-identical state."""
+    r, oc = _pair(5)
+    with r:
+        _shared_state(r, oc)
+        s = _samples(np.random.default_rng(7), 4096)
+        for _ in range(3):
+            r.cache.train(s)
+        r.cache.train(s, apply=False)   # gradients pending, not yet applied
+        state = r.cache.checkpoint()
+        assert int(state[L.XR_CACHE_ADAM_STEP][0]) == 3 == r.cache.stats().steps
+        q = s[:1000]
+        before = r.cache.query(q)
+        with xr.Renderer(8, 8) as r2:
+            r2.set_params(xr.params_default(8, 8))
+            r2.cache.reset(99)                 # a different initialisation, overwritten below
+            r2.cache.set_bounds(LO, INV)
+            r2.cache.restore(state)
+            assert r2.cache.stats().steps == 3
+            for w in range(8):
+                assert np.array_equal(r2.cache.read(w), state[w]), w
+            assert np.array_equal(r2.cache.query(q), before)
+            r.cache.step()
+            r2.cache.step()
+            for w in (L.XR_CACHE_MLP, L.XR_CACHE_GRID, L.XR_CACHE_MLP_M, L.XR_CACHE_MLP_V, L.XR_CACHE_GRID_M,
+                      L.XR_CACHE_GRID_V):
+                assert np.array_equal(r2.cache.read(w), r.cache.read(w)), w
+            assert np.array_equal(r2.cache.query(q), r.cache.query(q))
+        with pytest.raises(xr.XrError):
+            r.cache.write(L.XR_CACHE_ADAM_STEP, np.zeros(2, np.uint32))   # one uint32 only

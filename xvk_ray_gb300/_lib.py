@@ -132,7 +132,7 @@ class XrTuning(C.Structure):
 
 XR_CACHE_MLP, XR_CACHE_GRID, XR_CACHE_MLP_GRAD, XR_CACHE_GRID_GRAD = 0, 1, 2, 3
 XR_CACHE_MLP_M, XR_CACHE_MLP_V, XR_CACHE_GRID_M, XR_CACHE_GRID_V = 4, 5, 6, 7
-XR_CACHE_QUERIES, XR_CACHE_TRAIN_RECORDS = 8, 9
+XR_CACHE_QUERIES, XR_CACHE_TRAIN_RECORDS, XR_CACHE_ADAM_STEP = 8, 9, 10
 XR_DEVFLAG_MMA_TIMEOUT = 8
 
 assert C.sizeof(XrCacheParams) == 32 and C.sizeof(XrCacheSample) == 72 and C.sizeof(XrCacheStats) == 40

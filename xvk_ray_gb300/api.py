@@ -389,13 +389,21 @@ class Cache:
             if n.value:
                 self._c(L.load().xr_cache_read(self._ctx, which, _ptr(out), out.nbytes, None))
             return out.reshape(-1, 8 if which == L.XR_CACHE_QUERIES else 12)
-        out = np.empty(n.value // 4, np.float32)
+        out = np.empty(n.value // 4, np.uint32 if which == L.XR_CACHE_ADAM_STEP else np.float32)
         self._c(L.load().xr_cache_read(self._ctx, which, _ptr(out), out.nbytes, None))
         return out
 
     def write(self, which: int, values: np.ndarray) -> None:
-        v = np.ascontiguousarray(values, np.float32)
+        v = np.ascontiguousarray(values, np.uint32 if which == L.XR_CACHE_ADAM_STEP else np.float32)
         self._c(L.load().xr_cache_write(self._ctx, which, _ptr(v), v.nbytes))
+
+    def checkpoint(self) -> dict:
+        """The cache's whole trained state: arrays 0..7 and the Adam step count."""
+        return {w: self.read(w).copy() for w in list(range(8)) + [L.XR_CACHE_ADAM_STEP]}
+
+    def restore(self, state: dict) -> None:
+        for w, v in state.items():
+            self.write(w, v)
 
     def stats(self) -> L.XrCacheStats:
         st = L.XrCacheStats()

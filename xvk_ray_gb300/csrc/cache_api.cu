@@ -357,6 +357,12 @@ xr_status xr_cache_read(XrContext* c, int which, void* host, size_t bytes, size_
             need = (size_t)cnt * 48;
             src = cs.train;
         }
+    } else if (which == XR_CACHE_ADAM_STEP) {
+        if (needed) *needed = 4;
+        if (!host) return XR_OK;
+        if (bytes < 4) return fail(c, XR_ERR_INVALID_ARGUMENT, "cache_read: host buffer too small");
+        std::memcpy(host, &cs.step, 4);
+        return XR_OK;
     } else {
         need = array_floats(which) * 4;
         src = array_ptr(cs, which);
@@ -375,8 +381,24 @@ xr_status xr_cache_write(XrContext* c, int which, const void* host, size_t bytes
     xr_status s = cache_alloc(c);
     if (s) return s;
     CacheState& cs = c->cache;
+    if (which == XR_CACHE_ADAM_STEP) {
+        if (bytes != 4) return fail(c, XR_ERR_INVALID_ARGUMENT, "cache_write: the step count is one uint32");
+        std::memcpy(&cs.step, host, 4);
+        // the device's bias-correction state after that many steps: the products
+        // k_cache_adam_advance forms, one float multiplication per step
+        float st[4] = {1.0f, 1.0f, 0.0f, 0.0f};
+        for (uint32_t i = 0; i < cs.step; i++) {
+            const float p1 = st[0] * cs.params.beta1, p2 = st[1] * cs.params.beta2;
+            st[0] = p1;
+            st[1] = p2;
+            st[2] = 1.0f - p1;
+            st[3] = 1.0f - p2;
+        }
+        if ((s = xr_sync(c))) return s;
+        return cuda_check(c, cudaMemcpy(cs.adam, st, sizeof(st), cudaMemcpyHostToDevice), "cache_write adam state");
+    }
     float* dst = array_ptr(cs, which);
-    if (!dst) return fail(c, XR_ERR_INVALID_ARGUMENT, "cache_write: arrays 0..7 only");
+    if (!dst) return fail(c, XR_ERR_INVALID_ARGUMENT, "cache_write: arrays 0..7 and the step count (10) only");
     if (bytes != array_floats(which) * 4) return fail(c, XR_ERR_INVALID_ARGUMENT, "cache_write: size mismatch");
     if ((s = xr_sync(c))) return s;
     if ((s = cuda_check(c, cudaMemcpy(dst, host, bytes, cudaMemcpyHostToDevice), "cache_write copy"))) return s;
