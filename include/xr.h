@@ -106,7 +106,7 @@ typedef struct XrParams {
     uint32_t write_hdr;          /* also write the linear radiance before tone mapping */
 } XrParams;
 
-/* Defaults for BASELINE-style corrected rendering: temporal + spatial on, M cap
+/* Defaults of the corrected pipeline (the benchmark's settings): temporal + spatial on, M cap
    20 / 120, 5 neighbours, 30 px, visibility on, seed 1. */
 void xr_params_default(XrParams* p, uint32_t width, uint32_t height);
 /* The reference's own constants (compat_reference = 1). */
