@@ -552,9 +552,15 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
     // Every pixel starts a path, so its queue slot is its index in tile order: the
     // view's first pixel, the full tile rows above (only the last can be short),
     // the tiles to the left in this row, the position inside the (possibly cut) tile.
+    // In a full tile the 32 slots a warp fetches first cover an 8 x 4 block (four blocks
+    // per tile) rather than two 16-pixel rows: squarer bundles of camera rays.
     if (alive) {
         const uint32_t rows = min(8u, VH - ty * 8u), cols = min(16u, VW - tx * 16u);
-        const uint32_t i = base + ty * 8u * VW + tx * 16u * rows + (threadIdx.x >> 4) * cols + (threadIdx.x & 15u);
+        const uint32_t xi = threadIdx.x & 15u, yi = threadIdx.x >> 4;
+        const uint32_t in_tile = (rows == 8u && cols == 16u)
+                                     ? ((yi >> 2) * 2u + (xi >> 3)) * 32u + (yi & 3u) * 8u + (xi & 7u)
+                                     : yi * cols + xi;
+        const uint32_t i = base + ty * 8u * VW + tx * 16u * rows + in_tile;
         fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
         fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
         fa.q_out[2][i] = f4(s.thr, s.pq);
