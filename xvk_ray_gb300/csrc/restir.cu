@@ -504,6 +504,12 @@ __device__ __forceinline__ bool cache_emit(const FrameArgs& fa, const CacheEmit&
     return alive && trained;
 }
 
+// Z-order of a pixel in an 8 x 4 block (x bits 0..2, y bits 0..1 interleaved from x):
+// runs of 8 consecutive slots are 4 x 2 pixel squares.
+__device__ __forceinline__ uint32_t morton_8x4(uint32_t x, uint32_t y) {
+    return (x & 1u) | ((y & 1u) << 1) | ((x & 2u) << 1) | ((y & 2u) << 2) | ((x & 4u) << 2);
+}
+
 // Camera rays (ReSTIRGIInitialSample.rgen.hlsl:41-52) for a 16 x 8 pixel tile per
 // block, appended to the queue of bounce 0 in tile order.
 template <bool COMPAT>
@@ -558,7 +564,7 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
         const uint32_t rows = min(8u, VH - ty * 8u), cols = min(16u, VW - tx * 16u);
         const uint32_t xi = threadIdx.x & 15u, yi = threadIdx.x >> 4;
         const uint32_t in_tile = (rows == 8u && cols == 16u)
-                                     ? ((yi >> 2) * 2u + (xi >> 3)) * 32u + (yi & 3u) * 8u + (xi & 7u)
+                                     ? ((yi >> 2) * 2u + (xi >> 3)) * 32u + morton_8x4(xi & 7u, yi & 3u)
                                      : yi * cols + xi;
         const uint32_t i = base + ty * 8u * VW + tx * 16u * rows + in_tile;
         fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
