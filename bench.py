@@ -44,7 +44,7 @@ TEMPORAL_BYTES_PER_PX = 140
 SPATIAL_BYTES_PER_PX = 104   # reads G-buffer 16+4, candidate 16, reservoir 32; writes reservoir 32 + RGBA8 4
 # DRAM bytes (read + write) of one k_temporal launch at 1920x1080 measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum): 185.2 MB + 47.7 MB
-TEMPORAL_DRAM_BYTES_1080P = 232.9e6
+TEMPORAL_DRAM_BYTES_1080P = 232.4e6
 # kernels per frame: raygen, (trace + shade) per bounce, temporal, spatial select,
 # shadow trace, spatial resolve
 FRAME_LAUNCHES = 1 + 2 * BOUNCES + 4
