@@ -45,7 +45,7 @@ typedef struct XrVertex {
     int32_t material_index;
 } XrVertex;
 
-/* src/Asset/Material.h:117-166 (AMaterial, 32 B) == Material.hlsl:7-14.
+/* src/Asset/Material.h:8-58 (AMaterial, 32 B) == Material.hlsl:7-14.
    material_model: 0 Lambertian, 1 Metallic (GGX conductor, roughness = fuzziness),
    4 DiffuseLight (emits base_color * 4, BSDF.hlsl:27-32), 5 Plastic (GGX coat
    over Lambert, roughness = fuzziness).  Models 1 and 5 are extensions of this
@@ -221,8 +221,12 @@ xr_status xr_trace_rays_device(XrContext* ctx, const float* d_rays, uint32_t n, 
    of this library (65536 rays, about 3 MiB, held on each GPU until exit), so at
    most 65536 rays per call; larger batches fail with XR_ERR_INVALID_ARGUMENT.
    Allocates nothing.  The first call on a device looks the array's address up
-   and should come before any stream capture.  Calls share the array: calls that
-   overlap on the GPU race, so serialise them.  Same results as xr_trace_rays. */
+   and should come before any stream capture; a device reset (cudaDeviceReset)
+   after it is not supported.  Calls share the array: calls that overlap on the
+   GPU race, so serialise them.  An instanced world whose top-level BVH is stale
+   after xr_update_vertices is refused with XR_ERR_STATE, because rebuilding it
+   allocates: render a frame or call xr_trace_rays / xr_get_stats once first.
+   Same results as xr_trace_rays. */
 xr_status xr_trace_rays_noalloc(XrContext* ctx, const float* rays, uint32_t n, int32_t any_hit,
                                 int32_t* prim, float* t, float* bary);
 
@@ -308,7 +312,7 @@ xr_status xr_read_view_output(XrContext* ctx, uint32_t view, uint32_t which, voi
 /* xr_render_reference for every view: host_rgb holds 3 doubles per pixel of all views, view by view. */
 xr_status xr_render_reference_views(XrContext* ctx, const XrUniformBufferObject* ubos, uint32_t frame0, uint32_t spp,
                                     double* host_rgb);
-xr_status xr_set_graphs(XrContext* ctx, int enabled);   /* CUDA-graph replay of frames (not with the cache) */
+xr_status xr_set_graphs(XrContext* ctx, int enabled);   /* CUDA-graph replay of frames */
 
 /* Launch configuration chosen by xr_autotune: persistent CTAs per SM of the
    traversal and shading kernels (0 = the occupancy maximum). */
@@ -430,6 +434,13 @@ xr_status xr_cache_query(XrContext* ctx, const XrCacheSample* s, uint32_t n, flo
 xr_status xr_cache_train(XrContext* ctx, const XrCacheSample* s, uint32_t n, int apply, float* loss);
 /* One Adam step on the current gradients (e.g. written with xr_cache_write), which it then zeroes. */
 xr_status xr_cache_step(XrContext* ctx);
+/* Self-test of the failure path of the cache's bounded tensor-core waits (no counterpart
+   in the reference): one CTA takes tensor memory and an mbarrier as the cache kernels do
+   and waits on a phase that nothing completes, with a limit of limit_us microseconds
+   (1 .. 1e6).  The wait gives up, the kernel raises XR_DEVFLAG_MMA_TIMEOUT, frees its
+   tensor memory and returns, and the call returns XR_ERR_TIMEOUT the first time the
+   context sees the flag.  The context stays usable. */
+xr_status xr_cache_selftest_wait(XrContext* ctx, uint32_t limit_us);
 xr_status xr_cache_read(XrContext* ctx, int which, void* host, size_t bytes, size_t* bytes_needed);
 xr_status xr_cache_write(XrContext* ctx, int which, const void* host, size_t bytes);   /* arrays 0..7, step 10 */
 xr_status xr_cache_get_stats(XrContext* ctx, XrCacheStats* out);

@@ -31,6 +31,16 @@ def load():
             "or_random_sequence": (None, [u32, u32, P, P]),
             "or_sincos": (None, [P, u32, P, P]),
             "or_oct_roundtrip": (None, [P, u32, u32, P, P]),
+            "or_units_onb": (None, [P, u32, P]),
+            "or_units_sample_hemisphere": (None, [P, u32, P]),
+            "or_units_sample_bsdf": (None, [P, P, P, P, u32, P]),
+            "or_units_update_list": (None, [P, P, u32, u32, P, P, P]),
+            "or_units_merge_list": (None, [P, P, u32, u32, P, P, P]),
+            "or_units_similar": (None, [P, P, u32, P]),
+            "or_units_aces": (None, [P, u32, P]),
+            "or_units_targets": (None, [P, P, P, u32, P]),
+            "or_units_world_to_screen_uv": (None, [P, u32, P, P, P]),
+            "or_units_neighbor_index": (None, [u32, u32, u32, u32, C.c_float, u32, u32, P]),
             "or_scene_create": (P, [P, u32, P, u32, P, u32]),
             "or_scene_destroy": (None, [P]),
             "or_scene_set_textures": (None, [P, P, u32, P]),

@@ -110,7 +110,7 @@ inline uint32_t pass_rng(bool compat, uint32_t x, uint32_t y, uint32_t w, uint32
 enum { MAT_LAMBERTIAN = 0, MAT_METALLIC = 1, MAT_DIELECTRIC = 2, MAT_ISOTROPIC = 3,
        MAT_DIFFUSE_LIGHT = 4, MAT_PLASTIC = 5 };
 
-struct Material {   // Material.hlsl:7-14 / src/Asset/Material.h:155-166, 32 B
+struct Material {   // Material.hlsl:7-14 / src/Asset/Material.h:44-57, 32 B
     float base[4];
     int32_t tex;
     float fuzz;
@@ -838,8 +838,11 @@ void initial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
             if (dot(pl.normal, pl.geo_normal) < 0.0f) pl.normal = -pl.normal;
         }
         if (mat.model == MAT_DIFFUSE_LIGHT) {
-            f3 Le = f3{mat.base[0], mat.base[1], mat.base[2]} * 4.0f;
-            f3 term = throughput * f3{mat.base[0], mat.base[1], mat.base[2]} * 4.0f;
+            // reference mode emits the light's untextured base colour (:117-121: mat.baseColor,
+            // not SampleDiffuseLight); corrected mode takes its base-colour texture
+            const Material& em = compat ? sc.mat[(uint32_t)pl.mat] : mat;
+            f3 Le = f3{em.base[0], em.base[1], em.base[2]} * 4.0f;
+            f3 term = throughput * f3{em.base[0], em.base[1], em.base[2]} * 4.0f;
             if (cache && bounce >= 2) {
                 // balance heuristic against the previous vertex's next-event estimate
                 const float lp = sc.light_prim.empty() ? 0.0f : sc.prim_light_pdf[h.prim];
@@ -1139,12 +1142,14 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
     uint32_t write_off = compat ? (1u - pingpong) * N : 0u;
     const Sample s_new = R.samples[p];
     if (compat) {
+        // background black, lights white, whatever `reuse` says (:80-89); only the
+        // shaded colour at the end is gated by it (:179-182)
         if (length(s_new.n_view) == 0.0f) {
-            if (u.reuse) write_output(R, p, f3{0, 0, 0}, false);
+            write_output(R, p, f3{0, 0, 0}, false);
             return;
         }
         if (length(s_new.n_sample) == 0.0f) {
-            if (u.reuse) write_output(R, p, f3{1, 1, 1}, false);
+            write_output(R, p, f3{1, 1, 1}, false);
             return;
         }
     } else {
@@ -1250,6 +1255,97 @@ void or_random_sequence(uint32_t state, uint32_t n, uint32_t* out_u32, float* ou
 }
 void or_sincos(const float* a, uint32_t n, float* s, float* c) {
     for (uint32_t i = 0; i < n; i++) sincos_xr(a[i], &s[i], &c[i]);
+}
+// ---- the restated helpers one by one (checked against the reference's own
+//      source, compiled by oracle/refpin, on the same inputs) ----
+void or_units_onb(const float* n3, uint32_t n, float* out6) {
+    for (uint32_t i = 0; i < n; i++) {
+        f3 b1, b2;
+        branchless_onb(f3{n3[3 * i], n3[3 * i + 1], n3[3 * i + 2]}, &b1, &b2);
+        float* o = out6 + 6 * (size_t)i;
+        o[0] = b1.x; o[1] = b1.y; o[2] = b1.z; o[3] = b2.x; o[4] = b2.y; o[5] = b2.z;
+    }
+}
+void or_units_sample_hemisphere(const float* xi2, uint32_t n, float* out3) {
+    for (uint32_t i = 0; i < n; i++) {
+        f3 v = sample_hemisphere(f2{xi2[2 * i], xi2[2 * i + 1]});
+        out3[3 * i] = v.x; out3[3 * i + 1] = v.y; out3[3 * i + 2] = v.z;
+    }
+}
+// reference-mode SampleBSDF: out 9 words {f.rgb, wi.xyz, pdf, cos, seed after}
+void or_units_sample_bsdf(const float* n3, const float* wo3, const uint32_t* materials8, const uint32_t* seeds,
+                          uint32_t n, float* out9) {
+    for (uint32_t i = 0; i < n; i++) {
+        Material m;
+        memcpy(&m, materials8 + 8 * (size_t)i, 32);
+        f3 wi;
+        float pdf, ct;
+        uint32_t seed = seeds[i];
+        f3 f = sample_bsdf(true, f3{n3[3 * i], n3[3 * i + 1], n3[3 * i + 2]}, m,
+                           f3{wo3[3 * i], wo3[3 * i + 1], wo3[3 * i + 2]}, &wi, &pdf, &ct, seed);
+        float* o = out9 + 9 * (size_t)i;
+        o[0] = f.x; o[1] = f.y; o[2] = f.z; o[3] = wi.x; o[4] = wi.y; o[5] = wi.z; o[6] = pdf; o[7] = ct;
+        memcpy(&o[8], &seed, 4);
+    }
+}
+void or_units_update_list(const uint32_t* samples24, const float* weights, uint32_t n, uint32_t k,
+                          const uint32_t* seeds, uint32_t* out28, uint32_t* seeds_out) {
+    for (uint32_t i = 0; i < n; i++) {
+        Reservoir r = init_reservoir();
+        uint32_t seed = seeds[i];
+        for (uint32_t j = 0; j < k; j++) {
+            Sample smp;
+            memcpy(&smp, samples24 + ((size_t)i * k + j) * 24, 96);
+            update_reservoir(r, smp, weights[(size_t)i * k + j], seed);
+        }
+        memcpy(out28 + (size_t)i * 28, &r, 112);
+        seeds_out[i] = seed;
+    }
+}
+void or_units_merge_list(const uint32_t* res28, const float* p_hats, uint32_t n, uint32_t k, const uint32_t* seeds,
+                         uint32_t* out28, uint32_t* seeds_out) {
+    for (uint32_t i = 0; i < n; i++) {
+        Reservoir t = init_reservoir();
+        uint32_t seed = seeds[i];
+        for (uint32_t j = 0; j < k; j++) {
+            Reservoir src;
+            memcpy(&src, res28 + ((size_t)i * k + j) * 28, 112);
+            merge_reservoir(t, src, p_hats[(size_t)i * k + j], seed);
+        }
+        memcpy(out28 + (size_t)i * 28, &t, 112);
+        seeds_out[i] = seed;
+    }
+}
+void or_units_similar(const uint32_t* a24, const uint32_t* b24, uint32_t n, uint32_t* out2) {
+    for (uint32_t i = 0; i < n; i++) {
+        Sample a, b;
+        memcpy(&a, a24 + 24 * (size_t)i, 96);
+        memcpy(&b, b24 + 24 * (size_t)i, 96);
+        out2[2 * i] = is_similar(a, b) ? 1u : 0u;
+        out2[2 * i + 1] = is_similar_geo(a.x_view, a.n_view, b.x_view, b.n_view) ? 1u : 0u;
+    }
+}
+void or_units_aces(const float* in3, uint32_t n, float* out3) {
+    for (uint32_t i = 0; i < 3 * n; i++) out3[i] = aces1(in3[i]);
+}
+// EvaluateTargetFunction of the temporal pass and p_hat of the spatial pass
+void or_units_targets(const uint32_t* samples24, const float* x3, const float* n3, uint32_t n, float* out2) {
+    for (uint32_t i = 0; i < n; i++) {
+        Sample smp;
+        memcpy(&smp, samples24 + 24 * (size_t)i, 96);
+        out2[2 * i] = eval_target(smp, f3{x3[3 * i], x3[3 * i + 1], x3[3 * i + 2]}, f3{n3[3 * i], n3[3 * i + 1], n3[3 * i + 2]});
+        out2[2 * i + 1] = p_hat_of(smp.L_out);
+    }
+}
+void or_units_world_to_screen_uv(const float* p3, uint32_t n, const float* view16, const float* proj16, float* out2) {
+    for (uint32_t i = 0; i < n; i++) {
+        f2 uv = world_to_screen_uv(f3{p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]}, view16, proj16);
+        out2[2 * i] = uv.x; out2[2 * i + 1] = uv.y;
+    }
+}
+void or_units_neighbor_index(uint32_t x, uint32_t y, uint32_t w, uint32_t h, float max_r, uint32_t seed, uint32_t k,
+                             uint32_t* out) {
+    for (uint32_t j = 0; j < k; j++) out[j] = neighbor_index(x, y, w, h, max_r, seed);
 }
 void or_oct_roundtrip(const float* n3, uint32_t count, uint32_t bits, float* out3, uint32_t* codes) {
     for (uint32_t i = 0; i < count; i++) {

@@ -78,6 +78,24 @@ uint32_t or_init_random_seed(uint32_t x, uint32_t y, uint32_t width, uint32_t fr
 void or_random_sequence(uint32_t state, uint32_t n, uint32_t* out_u32, float* out_f);
 void or_sincos(const float* a, uint32_t n, float* s, float* c);
 void or_oct_roundtrip(const float* n3, uint32_t count, uint32_t bits, float* out3, uint32_t* codes);
+/* The restated helpers one by one, for the check against the reference's own
+   source compiled by oracle/refpin (reference mode).  Layouts: samples 24 words,
+   reservoirs 28 words, materials 8 words; sample_bsdf writes {f.rgb, wi.xyz, pdf,
+   cos, seed after}; targets writes {EvaluateTargetFunction, p_hat}. */
+void or_units_onb(const float* n3, uint32_t n, float* out6);
+void or_units_sample_hemisphere(const float* xi2, uint32_t n, float* out3);
+void or_units_sample_bsdf(const float* n3, const float* wo3, const uint32_t* materials8, const uint32_t* seeds,
+                          uint32_t n, float* out9);
+void or_units_update_list(const uint32_t* samples24, const float* weights, uint32_t n, uint32_t k,
+                          const uint32_t* seeds, uint32_t* out28, uint32_t* seeds_out);
+void or_units_merge_list(const uint32_t* res28, const float* p_hats, uint32_t n, uint32_t k, const uint32_t* seeds,
+                         uint32_t* out28, uint32_t* seeds_out);
+void or_units_similar(const uint32_t* a24, const uint32_t* b24, uint32_t n, uint32_t* out2);
+void or_units_aces(const float* in3, uint32_t n, float* out3);
+void or_units_targets(const uint32_t* samples24, const float* x3, const float* n3, uint32_t n, float* out2);
+void or_units_world_to_screen_uv(const float* p3, uint32_t n, const float* view16, const float* proj16, float* out2);
+void or_units_neighbor_index(uint32_t x, uint32_t y, uint32_t w, uint32_t h, float max_r, uint32_t seed, uint32_t k,
+                             uint32_t* out);
 
 /* ---- scene + traversal ---- */
 void* or_scene_create(const float* vertices, uint32_t nv, const uint32_t* indices, uint32_t ntri,

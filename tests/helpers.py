@@ -15,6 +15,44 @@ RES_FIELDS = {              # word ranges of ReSTIRGIReservoir (ReSTIRGICommon.h
     "w_sum": slice(0, 1), "W": slice(1, 2), "m": slice(2, 3),
     "x_sample": slice(12, 15), "n_sample": slice(16, 19), "L_out": slice(20, 23), "f": slice(24, 27),
 }
+# the reservoir's copy of the rest of its sample (ReSTIRGIReservoir.s)
+RES_SAMPLE_FIELDS = {"s.x_view": slice(4, 7), "s.materialID": slice(7, 8), "s.n_view": slice(8, 11),
+                     "s.randSeed": slice(11, 12), "s.p_q": slice(15, 16)}
+SAMPLE_INT_WORDS = [3, 7, 15, 19, 23]                        # materialID, randSeed, pad1..pad3
+RES_INT_WORDS = [2, 3] + [4 + w for w in SAMPLE_INT_WORDS]   # m, pad, the sample's integer words
+
+
+def canon(words: np.ndarray, int_words) -> np.ndarray:
+    """Record words with every float -0.0 turned into +0.0 (integer words as they
+    are).  The reference maps normals through its identity instance transform,
+    whose products with zeros make the sign of a zero the driver's choice; every
+    other bit is compared."""
+    w = np.array(words, np.uint32, copy=True)
+    neg0 = w == 0x80000000
+    neg0[:, list(int_words)] = False
+    w[neg0] = 0
+    return w
+
+
+def canon_floats(a: np.ndarray) -> np.ndarray:
+    """Float array bits with -0.0 as +0.0."""
+    w = np.array(a, np.float32, copy=True).view(np.uint32)
+    w[w == 0x80000000] = 0
+    return w
+
+
+def field_digests(words: np.ndarray, fields: dict, int_words) -> dict:
+    """SHA-1 of each field's canonical words (see canon)."""
+    import hashlib
+    c = canon(words, int_words)
+    return {k: hashlib.sha1(np.ascontiguousarray(c[:, sl]).tobytes()).hexdigest() for k, sl in fields.items()}
+
+
+def unorm8(v: np.ndarray) -> np.ndarray:
+    """An RGBA8 UNORM store of float colours: clamp to [0, 1], * 255 + 0.5, truncate
+    (float32 arithmetic, the oracle's and the kernels' conversion)."""
+    v = np.clip(np.asarray(v, np.float32), np.float32(0), np.float32(1))
+    return (v * np.float32(255.0) + np.float32(0.5)).astype(np.int32).astype(np.uint8)
 
 
 def random_rays(rng: np.random.Generator, n: int, lo, hi, tmin=1e-4, tmax=1e4) -> np.ndarray:

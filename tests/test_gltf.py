@@ -180,7 +180,8 @@ def test_gltf_fixture(tmp_path, glb):
 
 def test_gltf_reference_cornell_box():
     """The reference's bundled Cornell box (asset/model/cb2) when the asset is present."""
-    p = Path("/root/reference/asset/model/cb2/scene.gltf")
+    from oracle.refpin import REFERENCE_ROOT
+    p = REFERENCE_ROOT / "asset" / "model" / "cb2" / "scene.gltf"
     if not p.exists():
         pytest.skip("reference assets not present")
     s = load_gltf(p)

@@ -150,8 +150,8 @@ def test_training_converges():
 
 
 def test_checkpoint_resume_is_exact():
-    """A trained cache saved with checkpoint() (arrays 0..7 and the Adam step count) and
-    restored into a fresh context predicts bit-identically, and the next Adam step
+    """A trained cache saved with checkpoint() (arrays 0..7, the Adam step count and the
+    encoding bounds) and restored into a fresh context predicts bit-identically, and the next Adam step
     (which reads the step count for its bias correction) gives bit-identical state."""
     r, oc = _pair(5)
     with r:
@@ -167,9 +167,11 @@ def test_checkpoint_resume_is_exact():
         with xr.Renderer(8, 8) as r2:
             r2.set_params(xr.params_default(8, 8))
             r2.cache.reset(99)                 # a different initialisation, overwritten below
-            r2.cache.set_bounds(LO, INV)
+            r2.cache.set_bounds([0.0, 0.0, 0.0], 0.25)   # another scene cube: restore() brings LO, INV back
             r2.cache.restore(state)
-            assert r2.cache.stats().steps == 3
+            st2 = r2.cache.stats()
+            assert st2.steps == 3
+            assert list(st2.bounds_lo) == LO and st2.inv_extent == INV
             for w in range(8):
                 assert np.array_equal(r2.cache.read(w), state[w]), w
             assert np.array_equal(r2.cache.query(q), before)
@@ -181,3 +183,27 @@ def test_checkpoint_resume_is_exact():
             assert np.array_equal(r2.cache.query(q), r.cache.query(q))
         with pytest.raises(xr.XrError):
             r.cache.write(L.XR_CACHE_ADAM_STEP, np.zeros(2, np.uint32))   # one uint32 only
+
+
+def test_bounded_tensor_core_wait_gives_up():
+    """The failure path of the cache kernels' bounded waits: a CTA holding tensor
+    memory waits on an mbarrier phase that nothing completes (no MMA issued), gives
+    up after 2 ms, raises XR_DEVFLAG_MMA_TIMEOUT and frees its tensor memory; the
+    call reports XR_ERR_TIMEOUT and the context goes on rendering."""
+    lib = L.load()
+    scene = xr.Scene.cornell()
+    with xr.Renderer(32, 32) as r:
+        r.set_params(xr.params_default(32, 32))
+        r.upload_scene(scene)
+        r.build_bvh()
+        assert r.stats().error_flags == 0
+        st = lib.xr_cache_selftest_wait(r.ctx, 2000)
+        assert st == L.XR_ERR_TIMEOUT, lib.xr_last_error(r.ctx)
+        assert b"timed out" in lib.xr_last_error(r.ctx)
+        assert r.stats().error_flags & L.XR_DEVFLAG_MMA_TIMEOUT
+        assert lib.xr_cache_selftest_wait(r.ctx, 0) == L.XR_ERR_INVALID_ARGUMENT
+        from tests.helpers import camera_sequence
+        for u in camera_sequence(scene, 32, 32, 2, 4):
+            r.render(u)                   # the context is still usable: the flag was seen once
+        img = r.read_output(L.XR_OUT_LDR8)
+        assert img.reshape(-1, 4)[:, :3].mean() > 1.0

@@ -196,6 +196,7 @@ _SIGS = {
     "xr_cache_query": (_i32, [_P, _P, _u32, _P]),
     "xr_cache_train": (_i32, [_P, _P, _u32, C.c_int, C.POINTER(C.c_float)]),
     "xr_cache_step": (_i32, [_P]),
+    "xr_cache_selftest_wait": (_i32, [_P, _u32]),
     "xr_cache_read": (_i32, [_P, C.c_int, _P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "xr_cache_write": (_i32, [_P, C.c_int, _P, C.c_size_t]),
     "xr_cache_get_stats": (_i32, [_P, C.POINTER(XrCacheStats)]),

@@ -398,12 +398,23 @@ class Cache:
         self._c(L.load().xr_cache_write(self._ctx, which, _ptr(v), v.nbytes))
 
     def checkpoint(self) -> dict:
-        """The cache's whole trained state: arrays 0..7 and the Adam step count."""
-        return {w: self.read(w).copy() for w in list(range(8)) + [L.XR_CACHE_ADAM_STEP]}
+        """The cache's whole trained state: arrays 0..7, the Adam step count and the
+        hash encoding's bounds (the scene cube the positions are normalised to)."""
+        state = {w: self.read(w).copy() for w in list(range(8)) + [L.XR_CACHE_ADAM_STEP]}
+        st = self.stats()
+        state["bounds"] = (tuple(float(v) for v in st.bounds_lo), float(st.inv_extent))
+        return state
 
     def restore(self, state: dict) -> None:
+        """Writes a checkpoint back.  The bounds are restored too, so a context with
+        another scene (another scene cube) predicts as the checkpointed one did."""
         for w, v in state.items():
+            if w == "bounds":
+                continue
             self.write(w, v)
+        if "bounds" in state:
+            lo, inv = state["bounds"]
+            self.set_bounds(lo, inv)
 
     def stats(self) -> L.XrCacheStats:
         st = L.XrCacheStats()

@@ -331,6 +331,17 @@ xr_status xr_cache_step(XrContext* c) {
     return xr_sync(c);
 }
 
+xr_status xr_cache_selftest_wait(XrContext* c, uint32_t limit_us) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "cache_selftest_wait: null context");
+    if (limit_us == 0 || limit_us > 1000000u)
+        return fail(c, XR_ERR_INVALID_ARGUMENT, "cache_selftest_wait: limit_us must be in [1, 1000000]");
+    DeviceGuard g(c->device);
+    launch_cache_wait_selftest((uint64_t)limit_us * 1000ull, c->d_counters + kCntError, c->stream);
+    xr_status s = cuda_check(c, cudaGetLastError(), "cache_selftest_wait launch");
+    if (s) return s;
+    return xr_sync(c);   // the raised flag comes back as XR_ERR_TIMEOUT
+}
+
 xr_status xr_cache_read(XrContext* c, int which, void* host, size_t bytes, size_t* needed) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "cache_read: null context");
     CacheState& cs = c->cache;

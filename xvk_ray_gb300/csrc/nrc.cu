@@ -471,6 +471,29 @@ __global__ void k_cache_pack(const XrCacheSample* s, uint32_t n, uint4* rec, uin
                                                  __float_as_uint(q.target[2]), 0u);
 }
 
+// The failure path of the bounded tensor-core waits, on its own: the CTA takes
+// tensor memory and an mbarrier exactly as the cache kernels do, then waits on a
+// phase that nothing completes (no MMA is issued and nothing arrives), so the
+// wait gives up after limit_ns, the flag is raised and the tensor memory is
+// freed -- the steps wait_mma's callers take on expiry.
+__global__ void __launch_bounds__(128) k_cache_wait_selftest(uint64_t limit_ns, uint32_t* err) {
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) umma::tmem_alloc(&tslot, 32);
+    if (tid == 0) { umma::mbar_init(&bar, 1); umma::mbar_fence_init(); }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot;
+    bool ok = umma::mbar_wait(&bar, 0u, limit_ns);
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && tid == 0) atomicOr(err, (uint32_t)XR_DEVFLAG_MMA_TIMEOUT);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 32);
+}
+
 }  // namespace nrc
 
 // ---------------------------------------------------------------------------
@@ -553,6 +576,10 @@ void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_
                                                      cs.w_bwd, cs.mlp_grad, reinterpret_cast<float2*>(cs.grid_grad),
                                                      cs.loss, err);
     if (apply) launch_cache_adam(cs, st);
+}
+
+void launch_cache_wait_selftest(uint64_t limit_ns, uint32_t* err, cudaStream_t st) {
+    k_cache_wait_selftest<<<1, 128, 0, st>>>(limit_ns, err);
 }
 
 void launch_cache_adam_reset(CacheState& cs, cudaStream_t st) {

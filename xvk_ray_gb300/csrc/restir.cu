@@ -320,7 +320,10 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
         if (dot(pl.normal, pl.geo) < 0.0f) pl.normal = -pl.normal;
     }
     if (mat.material_model == XR_MAT_DIFFUSE_LIGHT) {
-        float3 base = f3(mat.base_color[0], mat.base_color[1], mat.base_color[2]);
+        // reference mode: the light's own base colour, untextured, as the reference's
+        // initial pass emits it (ReSTIRGIInitialSample.rgen.hlsl:117-121)
+        const float* bc = COMPAT ? fa.sc.mats[pl.mat].base_color : mat.base_color;
+        float3 base = f3(bc[0], bc[1], bc[2]);
         float3 term = s.thr * base * 4.0f;
         if (bounce == 0) {
             write_invalid<COMPAT>(fa, p, pl.pos, pl.normal, base * 4.0f);
@@ -852,8 +855,9 @@ __global__ void __launch_bounds__(256) k_spatial_compat(FrameArgs fa, const XrUn
     const uint32_t read_off = pp * N, write_off = (1u - pp) * N;
     const bool reuse = u->reuse != 0u;
     float4 xv = fa.s_xv[p], nv = fa.s_nv[p], ns = fa.s_ns[p];
-    if (length(xyz(nv)) == 0.0f) { if (reuse) write_out(fa, p, f3(0, 0, 0), false); return; }
-    if (length(xyz(ns)) == 0.0f) { if (reuse) write_out(fa, p, f3(1, 1, 1), false); return; }
+    // background black, lights white: written whatever `reuse` says (ReSTIRGISpatialReuse.rgen.hlsl:80-89)
+    if (length(xyz(nv)) == 0.0f) { write_out(fa, p, f3(0, 0, 0), false); return; }
+    if (length(xyz(ns)) == 0.0f) { write_out(fa, p, f3(1, 1, 1), false); return; }
     const uint32_t mat = __float_as_uint(xv.w);
     Res center; load_wide(fa, fa.rw, read_off + p, center);
     Res r; res_init(r);

@@ -12,12 +12,19 @@
 // The array's host-side name is only a stand-in for the symbol, so its device
 // address is looked up once per device with that device current
 // (cudaGetSymbolAddress) and cached; the first call on a device does this
-// set-up, so make that first call before any stream capture.  Every call
-// shares the array and it keeps the last call's contents; the error word is
-// cleared at the start of each call.  Calls that overlap on the GPU (several
-// host threads, or contexts on different streams of one device) race on the
-// array: serialise them.  The error word and the kernel's ray-fetch counter
-// must start at zero and are cleared at the start of every call.
+// set-up, so make that first call before any stream capture.  The cached
+// address belongs to the device's context of that moment: a host that resets
+// the device (cudaDeviceReset) and goes on using the library is not supported.
+// Every call shares the array and it keeps the last call's contents.  Calls
+// that overlap on the GPU (several host threads, or contexts on different
+// streams of one device) race on the array: serialise them.  The error word and
+// the kernel's ray-fetch counter must start at zero and are cleared at the
+// start of every call.
+//
+// An instanced world whose top-level BVH went stale (xr_update_vertices moved
+// instanced geometry) is refused with XR_ERR_STATE: rebuilding it allocates
+// build scratch, so this entry point leaves the rebuild to the next frame,
+// xr_trace_rays or xr_get_stats call.
 #include <mutex>
 #include <string>
 
@@ -80,26 +87,39 @@ extern "C" xr_status xr_trace_rays_noalloc(XrContext* c, const float* rays, uint
     if (n == 0) return XR_OK;
     if (!rays || !prim || !t || !bary) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace_rays_noalloc: null array");
     if (!c->bvh_ready) return fail(c, XR_ERR_STATE, "trace_rays_noalloc: build the BVH first");
+    if (c->tlas_stale)
+        return fail(c, XR_ERR_STATE,
+                    "trace_rays_noalloc: the top-level BVH is stale after xr_update_vertices; rebuilding it "
+                    "allocates, so render a frame or call xr_trace_rays / xr_get_stats once first");
     int prev = -1;
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     if (prev != c->device) cudaSetDevice(c->device);
     TraceScratch* s = nullptr;
-    xr_status st = sync_tlas(c);   // a stale top level is rebuilt first (the only allocation on this path)
-    if (!st) st = scratch_for(c, &s);
+    uint32_t flags = 0;
+    xr_status st = scratch_for(c, &s);
+    cudaStream_t sm = c->stream;
+    if (!st) st = cuda_check(c, cudaMemsetAsync(&s->flags, 0, 2 * sizeof(uint32_t), sm), "trace_rays_noalloc: clear");
+    if (!st)
+        st = cuda_check(c, cudaMemcpyAsync(s->rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, sm),
+                        "trace_rays_noalloc: ray upload");
     if (!st) {
-        cudaStream_t sm = c->stream;
-        cudaMemsetAsync(&s->flags, 0, 2 * sizeof(uint32_t), sm);   // flags and fetch
-        cudaMemcpyAsync(s->rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, sm);
         launch_trace(c->fa.sc, reinterpret_cast<const float*>(s->rays), n, any_hit, s->prim, nullptr, s->t,
                      reinterpret_cast<float*>(s->bary), &s->fetch, &s->flags, nullptr, c->sm_count, sm);
-        cudaMemcpyAsync(prim, s->prim, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);
-        cudaMemcpyAsync(t, s->t, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);
-        cudaMemcpyAsync(bary, s->bary, (size_t)n * 8, cudaMemcpyDeviceToHost, sm);
-        uint32_t flags = 0;
-        cudaMemcpyAsync(&flags, &s->flags, 4, cudaMemcpyDeviceToHost, sm);
-        st = cuda_check(c, cudaStreamSynchronize(sm), "trace_rays_noalloc");
-        if (!st && flags) st = fail(c, XR_ERR_OVERFLOW, "trace_rays_noalloc: traversal stack overflow or malformed BVH");
+        st = cuda_check(c, cudaGetLastError(), "trace_rays_noalloc: launch");
     }
+    if (!st) st = cuda_check(c, cudaMemcpyAsync(prim, s->prim, (size_t)n * 4, cudaMemcpyDeviceToHost, sm),
+                             "trace_rays_noalloc: read back");
+    if (!st) st = cuda_check(c, cudaMemcpyAsync(t, s->t, (size_t)n * 4, cudaMemcpyDeviceToHost, sm),
+                             "trace_rays_noalloc: read back");
+    if (!st) st = cuda_check(c, cudaMemcpyAsync(bary, s->bary, (size_t)n * 8, cudaMemcpyDeviceToHost, sm),
+                             "trace_rays_noalloc: read back");
+    if (!st) st = cuda_check(c, cudaMemcpyAsync(&flags, &s->flags, 4, cudaMemcpyDeviceToHost, sm),
+                             "trace_rays_noalloc: read back");
+    if (s) {   // whatever was queued completes before the outputs are handed back
+        const xr_status ss = cuda_check(c, cudaStreamSynchronize(sm), "trace_rays_noalloc");
+        if (!st) st = ss;
+    }
+    if (!st && flags) st = fail(c, XR_ERR_OVERFLOW, "trace_rays_noalloc: traversal stack overflow or malformed BVH");
     if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
     return st;
 }

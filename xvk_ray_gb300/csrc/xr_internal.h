@@ -408,6 +408,7 @@ void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_
                         uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st);
 void launch_cache_adam(CacheState& cs, cudaStream_t st);   // one Adam step on the gradients (bias correction on the device)
 void launch_cache_adam_reset(CacheState& cs, cudaStream_t st);
+void launch_cache_wait_selftest(uint64_t limit_ns, uint32_t* err, cudaStream_t st);   // a wait that runs out
 // ---- cache_api.cu ----
 xr_status cache_prepare_frame(Context* c, uint32_t frame);   // capacities; sets the FrameArgs cache fields
 void cache_after_paths(Context* c);           // inference (+ training) after the bounce loop
