@@ -213,7 +213,8 @@ def units():
 def _surface_case(rng, W=16, H=16):
     """A gently curved surface seen head on: neighbours within a few pixels are
     similar (|dx|^2 <= 0.1, n.n' >= 0.8, same material), so the spatial pass's
-    Jacobian and merges run for most of them."""
+    Jacobian and merges run for most of them.  Materials are the Cornell box's
+    Lambertian ones (the scene the passes run with)."""
     n = W * H
     s = np.zeros((n, 24), np.uint32)
     f = s.view(np.float32)
@@ -232,7 +233,9 @@ def _surface_case(rng, W=16, H=16):
     ns[:, 1] -= 1.0                                   # sample normals mostly face the surface
     f[:, 12:15] = ns / np.linalg.norm(ns, axis=1, keepdims=True)
     f[:, 16:19] = rng.uniform(0, 3, (n, 3))
-    f[:, 20:23] = rng.uniform(0.05, 0.25, (n, 3))
+    # f of a Lambertian visible point is its material's albedo / pi (BSDF.hlsl:22-24)
+    albedo = xr.Scene.cornell().materials[:, :3]
+    f[:, 20:23] = albedo[s[:, 3]] * np.float32(1.0 / 3.14159265359)
     hole = rng.random(n) < 0.05                      # a few misses and lights
     s[hole] = 0
     s[hole, 3] = 0xFFFFFFFF
