@@ -127,3 +127,23 @@ def test_png_roundtrip(tmp_path):
         write_png(str(p), px, w, h)
         back, bw, bh = read_png_rgba(str(p))
         assert (bw, bh) == (w, h) and np.array_equal(back, px)
+
+
+def test_workload_library_generates_the_benchmark_inputs():
+    """oracle/_build/libworkload.so (the generator built without libxr.so, for the
+    CPU baseline) yields the benchmark scene and camera path bit for bit."""
+    from oracle import workload as wl
+    kw = dict(seed=1, n_objects=64, n_lights=4, extent=8.0, sphere_subdiv=2)
+    a, b = wl.procedural(**kw), xr.Scene.procedural(**kw)
+    for k in ("vertices", "indices", "materials"):
+        assert np.array_equal(getattr(a, k).view(np.uint32), getattr(b, k).view(np.uint32)), k
+    assert bytes(a.camera) == bytes(b.camera)
+    assert np.array_equal(wl.cornell().vertices.view(np.uint32), xr.Scene.cornell().vertices.view(np.uint32))
+    cam = xr._lib.XrCamera.from_buffer_copy(a.camera)
+    pa = pb = None
+    for f in range(3):
+        cam.position[2] -= 0.01
+        cam.yaw_deg += 0.2
+        ua, ub = wl.camera_ubo(cam, 1920, 1080, pa, f, 4), xr.camera_ubo(cam, 1920, 1080, pb, f, 4)
+        assert xr.ubo_bytes(ua) == xr.ubo_bytes(ub)
+        pa, pb = ua, ub

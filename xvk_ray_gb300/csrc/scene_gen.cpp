@@ -6,11 +6,22 @@
 // (src/Editor/Camera.cpp:21-27), previous matrices carried from the last frame.
 // The scenes are the synthetic inputs of the benchmark configurations: the
 // reference renders glTF files, which are not part of this workload.
+//
+// Host C++ only, on the public header alone: the CPU oracle's build compiles
+// this same file into its own workload library, so that the CPU baseline renders
+// the identical scene and camera path without loading libxr.so.  Errors go
+// through xr::fail (the library's last-error string; a plain status there).
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
-#include "xr_internal.h"
+#include "xr.h"
+
+namespace xr {
+struct Context;
+xr_status fail(const Context* ctx, xr_status code, const std::string& msg);
+}  // namespace xr
 
 namespace {
 
@@ -198,6 +209,30 @@ xr_status emit(Builder& b, XrSceneData* out) {
 }  // namespace
 
 extern "C" {
+
+// The two parameter presets (the benchmark's corrected pipeline; the reference's constants).
+void xr_params_default(XrParams* p, uint32_t width, uint32_t height) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->width = width; p->height = height;
+    p->compat_reference = 0;
+    p->temporal_on = 1; p->spatial_on = 1;
+    p->m_cap_temporal = 20; p->m_cap_spatial = 120;
+    p->n_neighbours = 5; p->radius_px = 30.0f;
+    p->visibility = 1; p->seed = 1;
+}
+
+void xr_params_reference(XrParams* p, uint32_t width, uint32_t height) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->width = width; p->height = height;
+    p->compat_reference = 1;
+    p->temporal_on = 1; p->spatial_on = 1;
+    p->m_cap_temporal = 30; p->m_cap_spatial = 300;   // ReSTIRGITemporalReuse.rgen.hlsl:3, ReSTIRGISpatialReuse.rgen.hlsl:6
+    p->n_neighbours = 6; p->radius_px = 5.0f;         // ReSTIRGISpatialReuse.rgen.hlsl:4-5
+    p->visibility = 0; p->seed = 0;
+}
+
 
 xr_status xr_camera_ubo(const XrCamera* cam, uint32_t width, uint32_t height, const XrUniformBufferObject* prev,
                         uint32_t current_frame, uint32_t number_of_bounces, uint32_t has_sky_box, uint32_t reuse,

@@ -278,28 +278,6 @@ const char* xr_last_error(const XrContext* ctx) {
     return t_err_copy.c_str();
 }
 
-void xr_params_default(XrParams* p, uint32_t width, uint32_t height) {
-    if (!p) return;
-    memset(p, 0, sizeof(*p));
-    p->width = width; p->height = height;
-    p->compat_reference = 0;
-    p->temporal_on = 1; p->spatial_on = 1;
-    p->m_cap_temporal = 20; p->m_cap_spatial = 120;
-    p->n_neighbours = 5; p->radius_px = 30.0f;
-    p->visibility = 1; p->seed = 1;
-}
-
-void xr_params_reference(XrParams* p, uint32_t width, uint32_t height) {
-    if (!p) return;
-    memset(p, 0, sizeof(*p));
-    p->width = width; p->height = height;
-    p->compat_reference = 1;
-    p->temporal_on = 1; p->spatial_on = 1;
-    p->m_cap_temporal = 30; p->m_cap_spatial = 300;   // ReSTIRGITemporalReuse.rgen.hlsl:3, ReSTIRGISpatialReuse.rgen.hlsl:6
-    p->n_neighbours = 6; p->radius_px = 5.0f;         // ReSTIRGISpatialReuse.rgen.hlsl:4-5
-    p->visibility = 0; p->seed = 0;
-}
-
 xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     if (!desc || !out) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "create: null argument");
     *out = nullptr;
