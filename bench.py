@@ -20,6 +20,7 @@ pipeline has no cross-GPU exchange); value = max rank time / (K * N).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -41,10 +42,16 @@ METRIC = "ms/frame 1080p & relMSE vs FP64 ref: plain ReSTIR GI vs ReSTIR GI+MLP 
 # reads G-buffer 16+4, candidate 16+16, reprojected pixel index 4, previous G-buffer 4+16,
 # previous reservoir 32; writes reservoir 32
 TEMPORAL_BYTES_PER_PX = 140
-SPATIAL_BYTES_PER_PX = 104   # reads G-buffer 16+4, candidate 16, reservoir 32; writes reservoir 32 + RGBA8 4
+# spatial reuse, each pixel counted once: reservoir 32 + G-buffer 20 read, reservoir 32 + RGBA16F-sized output 8
+# written (the recommended layout's figure; the RGBA8 image written here is 4 B)
+SPATIAL_BYTES_PER_PX = 92
+RESERVOIR_BYTES_PER_PX = TEMPORAL_BYTES_PER_PX + SPATIAL_BYTES_PER_PX   # 232
 # DRAM bytes (read + write) of one k_temporal launch at 1920x1080 measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum): 185.2 MB + 47.7 MB
 TEMPORAL_DRAM_BYTES_1080P = 232.4e6
+# DRAM bytes of one frame's four reservoir-pass kernels (ncu): k_temporal 232.4 MB, k_spatial_select
+# 128.2 MB, k_spatial_resolve 215.9 MB; k_trace_shadow's DRAM traffic is not in a committed capture yet
+PASSES_DRAM_BYTES_1080P = None
 # kernels per frame: raygen, (trace + shade) per bounce, temporal, spatial select,
 # shadow trace, spatial resolve
 FRAME_LAUNCHES = 1 + 2 * BOUNCES + 4
@@ -241,12 +248,31 @@ def measure_relmse(xr, scene, ubos, eval_frames, ref_spp: int, device: int, trai
         equal = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, nb, train_samples, 0)
     # for comparison: plain ReSTIR GI without the spatial shadow rays
     plain_nv = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, False, 5, train_samples, 0)
+    # error decomposition: the cache replaces the path beyond the first secondary vertex
+    # x_s; at depth 2 a path ends at x_s (its emission only), so plain ReSTIR GI at depth 2
+    # against the depth-2 reference is the error of the part the cache cannot change --
+    # its ratio to the depth-4 error bounds what a cache at x_s can achieve
+    ubos2 = []
+    for u in ubos:
+        u2 = type(u).from_buffer_copy(u)
+        u2.number_of_bounces = 2
+        ubos2.append(u2)
+    refs2 = {}
+    depth2 = _relmse_run(xr, scene, ubos2, eval_frames, ref_spp, device, refs2, False, 5, train_samples)
     return {"restir_gi": plain["relmse"], "restir_gi_mlp_cache": same["relmse"], "pt_1spp": plain["pt_1spp"],
             "ratio_cache_over_plain": round(same["relmse"] / plain["relmse"], 4),
             "restir_gi_mlp_cache_equal_time": equal["relmse"],
             "ratio_equal_time": round(equal["relmse"] / plain["relmse"], 4),
             "detail": {"restir_gi": plain, "restir_gi_mlp_cache": same, "restir_gi_mlp_cache_equal_time": equal,
                        "restir_gi_no_shadow_rays": plain_nv},
+            "decomposition": {
+                "restir_gi_depth2_vs_depth2_reference": depth2["relmse"],
+                "restir_gi_depth4": plain["relmse"],
+                "bound_on_cache_ratio": round(depth2["relmse"] / plain["relmse"], 4),
+                "note": "depth 2 keeps what the cache at the first secondary vertex cannot change (the "
+                        "visible point's candidate sampling up to x_s); its error over the depth-4 error "
+                        "bounds the relMSE ratio a perfect cache could reach",
+                "ms_per_frame_depth2": depth2["ms_per_frame"]},
             "reference": f"FP64-accumulated plain path tracer, {ref_spp} spp, same path depth, "
                          f"at frames {list(eval_frames)} of the camera path",
             "eps": RELMSE_EPS, "reference_seconds": round(refs.get("seconds", 0.0), 2)}
@@ -428,6 +454,8 @@ def run_ours(args):
     hbm = hbm or 6800.0
     N = W * H
     temporal_gbs = TEMPORAL_BYTES_PER_PX * N / (ms_temp * 1e-3) / 1e9
+    spatial_gbs = SPATIAL_BYTES_PER_PX * N / (ms_spat * 1e-3) / 1e9
+    passes_gbs = RESERVOIR_BYTES_PER_PX * N / ((ms_temp + ms_spat) * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": round(ms_per_frame, 4), "unit": "ms/frame", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_frame, 4), "higher_is_better": False, "scaling": "weak",
@@ -439,11 +467,19 @@ def run_ours(args):
         "passes_ms": {"initial_sample": round(ms_init, 4), "temporal": round(ms_temp, 4), "spatial": round(ms_spat, 4)},
         "rays_per_frame": rays_pf, "shadow_rays_per_frame": shadow_pf,
         "rays_per_s": (rays_pf + shadow_pf) / ((ms_init + ms_spat) * 1e-3),
-        "roofline": {"kernel": "temporal reuse (k_temporal)", "bound": "hbm", "achieved": round(temporal_gbs, 1),
-                     "peak": hbm, "unit": "GB/s", "frac": round(temporal_gbs / hbm, 4),
-                     "traffic": TEMPORAL_DRAM_BYTES_1080P if (W, H) == (1920, 1080) else None,
-                     "traffic_unit": "bytes per launch (ncu)", "peak_source": peak_note,
-                     "algorithmic_bytes_per_px": TEMPORAL_BYTES_PER_PX},
+        # the reservoir passes as one unit (232 B per pixel over temporal + spatial time, the
+        # spatial pass with its shadow-ray traversal), and each pass on its own
+        "roofline": {"kernel": "reservoir passes (k_temporal + k_spatial_select + k_trace_shadow + k_spatial_resolve)",
+                     "bound": "hbm", "achieved": round(passes_gbs, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(passes_gbs / hbm, 4),
+                     "traffic": PASSES_DRAM_BYTES_1080P if (W, H) == (1920, 1080) else None,
+                     "traffic_unit": "bytes per frame (ncu, the four kernels)", "peak_source": peak_note,
+                     "algorithmic_bytes_per_px": RESERVOIR_BYTES_PER_PX,
+                     "passes": {"temporal": {"achieved": round(temporal_gbs, 1), "frac": round(temporal_gbs / hbm, 4),
+                                             "algorithmic_bytes_per_px": TEMPORAL_BYTES_PER_PX, "ms": round(ms_temp, 4),
+                                             "traffic": TEMPORAL_DRAM_BYTES_1080P if (W, H) == (1920, 1080) else None},
+                                "spatial": {"achieved": round(spatial_gbs, 1), "frac": round(spatial_gbs / hbm, 4),
+                                            "algorithmic_bytes_per_px": SPATIAL_BYTES_PER_PX, "ms": round(ms_spat, 4)}}},
         "bvh": bvh,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/frame", "h2d_bytes_per_step": C.sizeof(L.XrUniformBufferObject),
                 "d2h_bytes_per_step": W * H * 4},
@@ -455,6 +491,76 @@ def run_ours(args):
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene, ubos, seconds_budget=args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+# Configuration 0: the Cornell box at 256x256 (34 triangles of walls and boxes plus
+# the light quad), 8 frames of a static camera, 1 spp, depth 4, the benchmark's reuse
+# settings; relMSE against an FP64-accumulated reference of 65,536 spp.
+CORNELL_FRAMES = 8
+CORNELL_REF_SPP = 65536
+
+
+def run_cornell(args):
+    import numpy as np
+
+    import xvk_ray_gb300 as xr
+    from xvk_ray_gb300 import _build
+    _build.build_library()
+    L = xr._lib
+    lib = L.load()
+    w = h = 256
+    scene = xr.Scene.cornell()
+    cam = L.XrCamera.from_buffer_copy(scene.camera)
+    ubos, prev = [], None
+    n_frames = max(CORNELL_FRAMES, args.warmup + args.steps)
+    for f in range(n_frames):
+        prev = xr.camera_ubo(cam, w, h, prev, f, BOUNCES, sky=False, reuse=True)
+        ubos.append(prev)
+    res = {}
+    for variant in ("restir_gi", "restir_gi_mlp_cache"):
+        r = xr.Renderer(w, h)
+        r.set_params(xr.params_default(w, h, write_hdr=1, write_pt=1))
+        r.upload_scene(scene)
+        r.build_bvh()
+        if variant != "restir_gi":
+            cp = xr.cache_params_default()
+            cp.enabled = 1
+            cp.train_samples = 8192
+            r.cache.set_params(cp)
+        if variant == "restir_gi":
+            t0 = time.perf_counter()
+            ref = r.render_reference(ubos[0], 1_000_000, CORNELL_REF_SPP)
+            ref_s = time.perf_counter() - t0
+        per_frame, pt = [], []
+        for u in ubos[:CORNELL_FRAMES]:
+            r.render(u)
+            per_frame.append(relmse(r.read_output(L.XR_OUT_HDR), ref))
+            pt.append(relmse(r.read_output(L.XR_OUT_PT), ref))
+        # timing: the configuration's frames repeated along the same static camera
+        r.sync()
+        L.check(lib.xr_event_record(r.ctx, 0), r.ctx)
+        for u in ubos[:args.steps]:
+            r.render(u)
+        L.check(lib.xr_event_record(r.ctx, 1), r.ctx)
+        ms = ctypes.c_float()
+        L.check(lib.xr_event_elapsed(r.ctx, 0, 1, ctypes.byref(ms)), r.ctx)
+        res[variant] = {"relmse_per_frame": [round(v, 5) for v in per_frame], "relmse_frame8": per_frame[-1],
+                        "pt_1spp": float(np.mean(pt)), "ms_per_frame": round(ms.value / args.steps, 5)}
+        r.close()
+    line = {"metric": METRIC, "value": res["restir_gi"]["ms_per_frame"], "unit": "ms/frame", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["restir_gi"]["ms_per_frame"],
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (procedural Cornell box)",
+            "config": {"workload": "Cornell box 256x256, 34 + 2 triangles, 8 static frames, 1 spp, depth 4, "
+                                   "corrected ReSTIR GI (M cap 20, 5 neighbours, 30 px, shadow rays)",
+                       "reference": f"FP64-accumulated plain path tracer, {CORNELL_REF_SPP} spp "
+                                    f"({ref_s:.1f} s on the GPU)"},
+            "relmse": {"restir_gi": res["restir_gi"]["relmse_frame8"],
+                       "restir_gi_mlp_cache": res["restir_gi_mlp_cache"]["relmse_frame8"],
+                       "ratio_cache_over_plain": round(res["restir_gi_mlp_cache"]["relmse_frame8"] /
+                                                       res["restir_gi"]["relmse_frame8"], 4),
+                       "pt_1spp": res["restir_gi"]["pt_1spp"], "detail": res, "eps": RELMSE_EPS}}
     print(json.dumps(line), flush=True)
 
 
@@ -783,8 +889,9 @@ def main():
     ap.add_argument("--width", type=int, default=1920, help="smaller extents are for profiling only")
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--objects", type=int, default=4096, help="scene objects (4096 -> 998,442 triangles)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "4k", "dynamic"],
-                    help="frame: 1080p / 1M triangles (the headline); batch: 64 views over 8 scenes; "
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "4k", "dynamic", "cornell"],
+                    help="frame: 1080p / 1M triangles (the headline); cornell: configuration 0 (256x256, "
+                         "8 frames, FP64 reference of 65,536 spp); batch: 64 views over 8 scenes; "
                          "4k: 4 x 3840x2160 streams, 8M triangles, learned cache; "
                          "dynamic: moving instances and a refitted mesh")
     args = ap.parse_args()
@@ -801,6 +908,8 @@ def main():
         run_4k(args)
     elif args.workload == "dynamic":
         run_dynamic(args)
+    elif args.workload == "cornell":
+        run_cornell(args)
     else:
         run_ours(args)
 

@@ -374,14 +374,18 @@ xr_status xr_trace_rays_instanced(XrContext* ctx, const float* rays, uint32_t n,
    normal, direction, roughness, albedo, material kind -> 4 x 64 ReLU layers ->
    RGB; bfloat16 weights, FP32 accumulation on the tensor cores; Adam.
    With `enabled`, corrected-mode paths end at their first secondary vertex x_s
-   and the ReSTIR GI candidate takes L_out = Le(x_s) + cache(x_s); the
-   `train_samples` training paths of a frame continue to full depth and their
+   and the ReSTIR GI candidate takes L_out = Le(x_s) + cache(x_s); about
+   `train_samples` training paths a frame continue to full depth and their
    suffix radiance at x_s is the training target (relative L2 loss); one Adam
-   step per frame when `train` is set.  xr_render_reference never uses the cache. */
+   step per frame when `train` is set.  A training path needs a surface at its
+   first bounce, so the number of pixels selected for training adapts frame by
+   frame (the previous frame's selected pixels x train_samples / its training
+   records, at least train_samples) to yield about train_samples records.
+   xr_render_reference never uses the cache. */
 typedef struct XrCacheParams {
     uint32_t enabled;            /* paths terminate into the cache (corrected mode only) */
     uint32_t train;              /* one Adam step per rendered frame */
-    uint32_t train_samples;      /* training paths per frame, <= 1,048,576 (default 65,536) */
+    uint32_t train_samples;      /* training paths wanted per frame, <= 1,048,576 (default 65,536) */
     float learning_rate;         /* Adam step size (default 1e-2) */
     float beta1, beta2, epsilon; /* Adam (defaults 0.9, 0.99, 1e-15) */
     uint32_t seed;               /* parameter initialisation used by xr_cache_reset */

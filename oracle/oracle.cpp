@@ -755,7 +755,8 @@ struct Renderer {
     // learned radiance cache (corrected mode, or_renderer_set_cache): per pixel the
     // query record (8 words) and training record (12 words) of the last frame
     bool cache_on = false;
-    uint32_t cache_sel_n = 0;
+    uint32_t cache_sel_n = 0;      // training pixels of this frame (adapted after every frame)
+    uint32_t cache_target = 0;     // training records wanted per frame
     void* nrc = nullptr;
     std::vector<uint32_t> cache_q, cache_t;
     std::vector<uint8_t> cache_q_valid, cache_t_valid;
@@ -1588,6 +1589,15 @@ int or_render_frame(void* rp, const OrUBO* u) {
 #pragma omp parallel for schedule(dynamic, 2)
     for (int64_t y = 0; y < (int64_t)R.H; y++)
         for (uint32_t x = 0; x < R.W; x++) initial_pixel(R, x, (uint32_t)y, *u);
+    if (R.cache_on && R.cache_target) {
+        // the next frame's training pixels: sel * target / got clamped to [target, N]
+        // (all pixels when no record came out), as the kernels' k_cache_select_next
+        uint64_t got = 0;
+        for (uint32_t p = 0; p < R.N; p++) got += R.cache_t_valid[p] ? 1u : 0u;
+        uint64_t next = got ? (uint64_t)R.cache_sel_n * R.cache_target / got : (uint64_t)R.N;
+        next = std::min<uint64_t>(std::max<uint64_t>(next, R.cache_target), R.N);
+        R.cache_sel_n = (uint32_t)next;
+    }
     if (R.P.write_pt) {
         for (uint32_t p = 0; p < R.N; p++) {
             const Sample& s = R.samples[p];
@@ -1646,7 +1656,8 @@ int or_renderer_set_cache(void* rp, int enabled, uint32_t train_samples, void* n
     Renderer& R = *(Renderer*)rp;
     if (enabled && R.compat) return 1;
     R.cache_on = enabled != 0;
-    R.cache_sel_n = enabled ? std::min(train_samples, R.N) : 0u;
+    R.cache_target = enabled ? std::min(train_samples, R.N) : 0u;
+    R.cache_sel_n = R.cache_target;
     R.nrc = nrc;
     if (R.cache_on && R.cache_q.empty()) {
         R.cache_q.assign((size_t)R.N * 8, 0u);

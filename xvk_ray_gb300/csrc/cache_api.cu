@@ -73,6 +73,7 @@ xr_status cache_init(Context* c, uint32_t seed) {
     cudaMemsetAsync(cs.grid_v, 0, nrc::kGridParams * 4, c->stream);
     cs.step = 0;
     cs.grads_dirty = false;
+    cs.sel_target = 0;   // the next frame selects `target` training pixels again
     launch_cache_init(cs, seed, c->stream);
     launch_cache_adam_reset(cs, c->stream);
     s = cuda_check(c, cudaGetLastError(), "cache init launch");
@@ -97,6 +98,8 @@ xr_status cache_alloc(Context* c) {
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.w_bwd, nrc::kImageBytes), "cache alloc"))) return s;
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.loss, sizeof(float)), "cache alloc"))) return s;
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.adam, 4 * sizeof(float)), "cache alloc"))) return s;
+    if ((s = cuda_check(c, cudaMalloc((void**)&cs.sel, sizeof(uint32_t)), "cache alloc"))) return s;
+    cs.sel_target = 0;
     cs.allocated = true;
     return cache_init(c, cs.params.seed);
 }
@@ -153,7 +156,7 @@ xr_status upload_samples(Context* c, const XrCacheSample* s, uint32_t n, uint32_
 void cache_free(Context* c) {
     CacheState& cs = c->cache;
     void* ptrs[] = {cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.grid, cs.grid_grad, cs.grid_m, cs.grid_v,
-                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.adam, cs.queries, cs.train, cs.nee};
+                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.adam, cs.queries, cs.train, cs.nee, cs.sel};
     for (void* p : ptrs) cudaFree(p);
     cs = CacheState{};
 }
@@ -181,7 +184,7 @@ xr_status cache_prepare_frame(Context* c, uint32_t frame) {
     CacheState& cs = c->cache;
     FrameArgs& fa = c->fa;
     fa.cache_on = 0;
-    fa.cache_sel_n = 0;
+    fa.cache_sel = nullptr;
     cs.frame_used = false;
     cs.frame_trained = false;
     if (!cs.params.enabled) return XR_OK;
@@ -189,8 +192,15 @@ xr_status cache_prepare_frame(Context* c, uint32_t frame) {
         return fail(c, XR_ERR_UNSUPPORTED, "render_frame: the radiance cache runs in corrected mode only");
     xr_status s = cache_alloc(c);
     if (s) return s;
-    const uint32_t tcap = cs.params.train ? cs.params.train_samples : 0u;
+    // the training records of a frame: about `target` (adaptive selection), at most one per pixel
+    const uint32_t target = cs.params.train ? (cs.params.train_samples < c->N ? cs.params.train_samples : c->N) : 0u;
+    const uint32_t tcap = target ? c->N : 0u;
     if ((s = ensure_records(c, c->N, tcap > 0 ? tcap : 1u))) return s;
+    if (target && (cs.sel_target != target || cs.sel_pixels != c->N)) {   // new target or extent: select `target`
+        launch_cache_select_next(cs.sel, nullptr, target, c->N, target, c->stream);
+        cs.sel_target = target;
+        cs.sel_pixels = c->N;
+    }
     if (cs.grads_dirty) {
         cudaMemsetAsync(cs.mlp_grad, 0, (size_t)nrc::kMlpParams * 4, c->stream);
         cudaMemsetAsync(cs.grid_grad, 0, nrc::kGridParams * 4, c->stream);
@@ -201,7 +211,7 @@ xr_status cache_prepare_frame(Context* c, uint32_t frame) {
     fa.cache_t = cs.train;
     fa.cache_nee = cs.nee;
     fa.cache_t_cap = tcap;
-    fa.cache_sel_n = tcap < c->N ? tcap : c->N;
+    fa.cache_sel = target ? cs.sel : nullptr;
     (void)frame;
     cs.frame_used = true;
     cs.frame_trained = tcap > 0;
@@ -216,9 +226,11 @@ void cache_after_paths(Context* c) {
     launch_cache_infer(cs, cs.queries, c->d_counters + kCntCacheQuery, 0u, nullptr, c->fa.cand_b, err, c->sm_count,
                        c->stream);
     record_event(c, c->ev[7]);
-    if (cs.frame_trained)
+    if (cs.frame_trained) {
         launch_cache_train(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap, true, err, c->sm_count,
                            c->stream);
+        launch_cache_select_next(cs.sel, c->d_counters + kCntCacheTrain, cs.sel_target, c->N, 0u, c->stream);
+    }
 }
 
 }  // namespace xr

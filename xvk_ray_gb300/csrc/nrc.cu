@@ -471,6 +471,22 @@ __global__ void k_cache_pack(const XrCacheSample* s, uint32_t n, uint4* rec, uin
                                                  __float_as_uint(q.target[2]), 0u);
 }
 
+// The training-path selection of the next frame.  A frame selects `sel` pixels
+// (cache_training_pixel); those whose first bounce reaches a surface take a
+// training record, `got` of them.  The next frame selects sel * target / got
+// pixels (at least target, at most n; all of them when got is 0), so that about
+// `target` records come out of a frame whatever share of the paths escapes the
+// scene.  Integer arithmetic, replayed exactly by the oracle.
+__global__ void k_cache_select_next(uint32_t* sel, const uint32_t* got_ptr, uint32_t target, uint32_t n,
+                                    uint32_t set_to) {
+    if (set_to) { *sel = set_to; return; }
+    const uint64_t got = *got_ptr, cur = *sel;
+    uint64_t next = got ? cur * target / got : (uint64_t)n;
+    if (next < target) next = target;
+    if (next > n) next = n;
+    *sel = (uint32_t)next;
+}
+
 // The failure path of the bounded tensor-core waits, on its own: the CTA takes
 // tensor memory and an mbarrier exactly as the cache kernels do, then waits on a
 // phase that nothing completes (no MMA is issued and nothing arrives), so the
@@ -576,6 +592,11 @@ void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_
                                                      cs.w_bwd, cs.mlp_grad, reinterpret_cast<float2*>(cs.grid_grad),
                                                      cs.loss, err);
     if (apply) launch_cache_adam(cs, st);
+}
+
+void launch_cache_select_next(uint32_t* sel, const uint32_t* got, uint32_t target, uint32_t n, uint32_t set_to,
+                              cudaStream_t st) {
+    k_cache_select_next<<<1, 1, 0, st>>>(sel, got, target, n, set_to);
 }
 
 void launch_cache_wait_selftest(uint64_t limit_ns, uint32_t* err, cudaStream_t st) {

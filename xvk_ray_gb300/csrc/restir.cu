@@ -271,14 +271,16 @@ struct CacheEmit {
     NeeRay nee;        // training paths: the next-event ray of this vertex
 };
 
-// Training pixels of a frame: (pixel * (2^31 - 1) + off) mod N < cache_sel_n with
+// Training pixels of a frame: (pixel * (2^31 - 1) + off) mod N < sel with
 // off = frame * 2654435761 mod N -- a permutation of the pixels that changes every
 // frame (the frame index is read on the device, so a replayed graph follows it).
+// sel is the device word of k_cache_select_next (adapted every frame).
 __device__ __forceinline__ bool cache_training_pixel(const FrameArgs& fa, uint32_t pixel) {
-    if (fa.cache_sel_n == 0u) return false;
+    if (!fa.cache_sel) return false;
+    const uint32_t sel = *fa.cache_sel;
     const uint64_t off = ((uint64_t)fa.ubo[0].current_frame * 2654435761ull) % (uint64_t)fa.N;
     const uint64_t k = ((uint64_t)pixel * 2147483647ull + off) % (uint64_t)fa.N;
-    return k < fa.cache_sel_n;
+    return k < sel;
 }
 
 // Shades the traced hit `h` of one path: records the bounce's sample fields,

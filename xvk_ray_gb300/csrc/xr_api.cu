@@ -800,7 +800,7 @@ static xr_status render_reference_impl(XrContext* c, const XrUniformBufferObject
         if ((s = stage_ubos(c, u.data(), n)) || (s = enqueue_ubos(c, n))) break;
         set_frame_pointers(c, u[0].current_frame % 2u);
         c->fa.cache_on = 0;   // the converged reference is the plain path tracer
-        c->fa.cache_sel_n = 0;
+        c->fa.cache_sel = nullptr;
         c->cache.frame_used = false;
         cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);
         launch_initial(c->fa, u[0].number_of_bounces, c->stream);

@@ -167,7 +167,8 @@ struct FrameArgs {
     uint4* cache_q;           // query records, 2 uint4 each (capacity N)
     uint4* cache_t;           // training records, 3 uint4 each (capacity cache_t_cap)
     uint32_t cache_t_cap;
-    uint32_t cache_sel_n;     // training pixels per frame (selection in restir.cu: cache_training_pixel)
+    const uint32_t* cache_sel; // device word: pixels selected for training this frame (nullptr: none;
+                               // restir.cu: cache_training_pixel), set per frame by k_cache_select_next
     float4* cache_nee;        // next-event rays: 3 float4 each {o, record}, {d, tmax}, {contribution, 0}
 };
 
@@ -196,6 +197,8 @@ struct CacheState {
     uint4* train = nullptr;          // training records (capacity train_cap)
     float4* nee = nullptr;           // next-event rays of one bounce (capacity train_cap)
     uint32_t query_cap = 0, train_cap = 0;
+    uint32_t* sel = nullptr;         // device word: training pixels of the next frame (adaptive)
+    uint32_t sel_target = 0, sel_pixels = 0;   // the target and extent it was last set for (0: to be set)
     bool frame_used = false;         // the last frame ran with the cache
     bool frame_trained = false;
 };
@@ -409,6 +412,10 @@ void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_
 void launch_cache_adam(CacheState& cs, cudaStream_t st);   // one Adam step on the gradients (bias correction on the device)
 void launch_cache_adam_reset(CacheState& cs, cudaStream_t st);
 void launch_cache_wait_selftest(uint64_t limit_ns, uint32_t* err, cudaStream_t st);   // a wait that runs out
+// Training pixels of the next frame from this frame's training records: sel * target / got,
+// clamped to [target, n] (set_to != 0: set the word to set_to instead)
+void launch_cache_select_next(uint32_t* sel, const uint32_t* got, uint32_t target, uint32_t n, uint32_t set_to,
+                              cudaStream_t st);
 // ---- cache_api.cu ----
 xr_status cache_prepare_frame(Context* c, uint32_t frame);   // capacities; sets the FrameArgs cache fields
 void cache_after_paths(Context* c);           // inference (+ training) after the bounce loop
