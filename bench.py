@@ -180,9 +180,10 @@ RELMSE_EVAL_FRAMES = (16, 24, 32, 40, 48)
 
 
 def _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, cache: bool, n_neighbours: int,
-                train_samples: int, visibility: int = 1) -> dict:
+                train_samples: int, visibility: int = 1, keep_images: dict | None = None) -> dict:
     """One variant along the camera path: relMSE at the evaluation frames (FP64
-    references computed once and shared) and its median frame time."""
+    references computed once and shared) and its median frame time; the HDR
+    images of the evaluation frames go into keep_images when given."""
     import numpy as np
     L = xr._lib
     r = xr.Renderer(W, H, device=device)
@@ -215,6 +216,8 @@ def _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, cache: bool
                 refs[f + 1] = r.render_reference(u, 1_000_000, ref_spp)
                 refs["seconds"] = refs.get("seconds", 0.0) + time.perf_counter() - t0
             rel.append(relmse(hdr, refs[f + 1]))
+            if keep_images is not None:
+                keep_images[f + 1] = hdr[:, :3].astype(np.float64)
             rel_pt.append(relmse(r.read_output(L.XR_OUT_PT), refs[f + 1]))
     entry = {"relmse": float(np.mean(rel)), "per_frame": [round(v, 4) for v in rel],
              "ms_per_frame": round(statistics.median(ms[8:]), 4), "n_neighbours": n_neighbours,
@@ -235,17 +238,26 @@ def measure_relmse(xr, scene, ubos, eval_frames, ref_spp: int, device: int, trai
     samples, at each evaluation frame's camera), averaged over the evaluation
     frames, for: plain ReSTIR GI (5 neighbours, shadow rays), ReSTIR GI + learned
     radiance cache with the same reuse settings, and ReSTIR GI + cache at equal
-    frame time -- the first of: the same settings, then without the spatial
-    pass's shadow rays with 5, 4, .. 0 neighbours, whose median frame time does
-    not exceed plain ReSTIR GI's (the cache's own settings stay as configured)."""
+    frame time -- of the reuse settings tried (5 .. 1 neighbours with and without
+    the spatial pass's shadow rays, no spatial pass) the one with the lowest relMSE
+    whose median frame time does not exceed plain ReSTIR GI's (the cache's own
+    settings stay as configured).  Also the error decomposition."""
     refs = {}
     plain = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, False, 5, train_samples)
     same = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, 5, train_samples)
-    equal = same
-    for nb in (5, 4, 3, 2, 1, 0):
-        if equal["ms_per_frame"] <= plain["ms_per_frame"]:
-            break
-        equal = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, nb, train_samples, 0)
+    # equal time: of the cache variant's reuse settings (5 .. 1 neighbours with and without the
+    # spatial shadow rays, no spatial pass) the one with the lowest relMSE whose median frame
+    # time does not exceed plain ReSTIR GI's
+    tried = [same]
+    for vis in (1, 0):
+        for nb in (5, 4, 3, 2, 1):
+            if vis and nb == 5:
+                continue
+            tried.append(_relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, nb, train_samples,
+                                     vis))
+    tried.append(_relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, True, 0, train_samples, 0))
+    fits = [t for t in tried if t["ms_per_frame"] <= plain["ms_per_frame"]]
+    equal = min(fits, key=lambda t: t["relmse"]) if fits else min(tried, key=lambda t: t["ms_per_frame"])
     # for comparison: plain ReSTIR GI without the spatial shadow rays
     plain_nv = _relmse_run(xr, scene, ubos, eval_frames, ref_spp, device, refs, False, 5, train_samples, 0)
     # error decomposition: the cache replaces the path beyond the first secondary vertex
@@ -257,21 +269,32 @@ def measure_relmse(xr, scene, ubos, eval_frames, ref_spp: int, device: int, trai
         u2 = type(u).from_buffer_copy(u)
         u2.number_of_bounces = 2
         ubos2.append(u2)
-    refs2 = {}
-    depth2 = _relmse_run(xr, scene, ubos2, eval_frames, ref_spp, device, refs2, False, 5, train_samples)
+    refs2, img2 = {}, {}
+    depth2 = _relmse_run(xr, scene, ubos2, eval_frames, ref_spp, device, refs2, False, 5, train_samples,
+                         keep_images=img2)
+    import numpy as np
+    # a perfect cache: the depth-2 estimate plus the exact (noise-free) suffix radiance ref4 - ref2,
+    # against the same depth-4 reference as every variant
+    ideal = float(np.mean([relmse(img2[f] + (refs[f] - refs2[f]), refs[f]) for f in eval_frames]))
+    suffix_share = float(np.mean([np.mean(refs[f] - refs2[f]) / max(np.mean(refs[f]), 1e-30) for f in eval_frames]))
     return {"restir_gi": plain["relmse"], "restir_gi_mlp_cache": same["relmse"], "pt_1spp": plain["pt_1spp"],
             "ratio_cache_over_plain": round(same["relmse"] / plain["relmse"], 4),
             "restir_gi_mlp_cache_equal_time": equal["relmse"],
             "ratio_equal_time": round(equal["relmse"] / plain["relmse"], 4),
             "detail": {"restir_gi": plain, "restir_gi_mlp_cache": same, "restir_gi_mlp_cache_equal_time": equal,
-                       "restir_gi_no_shadow_rays": plain_nv},
+                       "restir_gi_no_shadow_rays": plain_nv,
+                       "cache_settings_tried": [{k: t[k] for k in ("n_neighbours", "shadow_rays", "relmse", "ms_per_frame")}
+                                                for t in tried]},
             "decomposition": {
-                "restir_gi_depth2_vs_depth2_reference": depth2["relmse"],
                 "restir_gi_depth4": plain["relmse"],
-                "bound_on_cache_ratio": round(depth2["relmse"] / plain["relmse"], 4),
-                "note": "depth 2 keeps what the cache at the first secondary vertex cannot change (the "
-                        "visible point's candidate sampling up to x_s); its error over the depth-4 error "
-                        "bounds the relMSE ratio a perfect cache could reach",
+                "restir_gi_depth2_vs_depth2_reference": depth2["relmse"],
+                "perfect_cache": ideal,
+                "perfect_cache_ratio": round(ideal / plain["relmse"], 4),
+                "suffix_share_of_radiance": round(suffix_share, 4),
+                "note": "the cache replaces the path beyond the first secondary vertex x_s; a perfect cache "
+                        "leaves the depth-2 estimate (paths ending at x_s) plus the exact suffix radiance "
+                        "(depth-4 minus depth-2 reference), whose relMSE against the depth-4 reference is "
+                        "what any cache at x_s can reach at these settings",
                 "ms_per_frame_depth2": depth2["ms_per_frame"]},
             "reference": f"FP64-accumulated plain path tracer, {ref_spp} spp, same path depth, "
                          f"at frames {list(eval_frames)} of the camera path",
@@ -561,6 +584,83 @@ def run_cornell(args):
                        "ratio_cache_over_plain": round(res["restir_gi_mlp_cache"]["relmse_frame8"] /
                                                        res["restir_gi"]["relmse_frame8"], 4),
                        "pt_1spp": res["restir_gi"]["pt_1spp"], "detail": res, "eps": RELMSE_EPS}}
+    print(json.dumps(line), flush=True)
+
+
+# The README's Scene1: Sibenik (asset/model/sb2, 75,277 triangles, 3 base-colour
+# textures) at 1920x1080 from the reference's default camera, converted from the
+# reference checkout by oracle/refpin/scenes.py.  Two settings: the reference's own
+# (reference mode: 10 bounces, M caps 30/300, 6 neighbours in 5 px, no-op
+# visibility) and the benchmark's corrected pipeline (depth 4, shadow rays).  Per
+# pass: the initial sample alone is the 1-spp path tracer's work, + temporal, +
+# spatial -- the README's three columns (its ReSTIR figures are the UI's frame time
+# divided by 3, src/Editor/UI.cpp:169, on RT cores of an unstated GPU).
+
+
+def run_sibenik(args):
+    import numpy as np
+
+    import xvk_ray_gb300 as xr
+    from xvk_ray_gb300 import _build
+    from oracle.refpin import scenes
+    _build.build_library()
+    L = xr._lib
+    lib = L.load()
+    scene = scenes.load("sibenik")
+    out = {}
+    for mode, pf, nb in (("reference_settings", xr.params_reference, 10), ("corrected", xr.params_default, BOUNCES)):
+        cam = L.XrCamera.from_buffer_copy(scene.camera)
+        ubos, prev = [], None
+        for f in range(args.warmup + args.steps):
+            cam.position[0] += 0.01
+            cam.yaw_deg += 0.2
+            prev = xr.camera_ubo(cam, W, H, prev, f, nb, sky=False, reuse=True)
+            ubos.append(prev)
+        r = xr.Renderer(W, H)
+        r.set_params(pf(W, H))
+        r.upload_scene(scene)
+        r.build_bvh()
+        r.set_graphs(True)
+        for u in ubos[:args.warmup]:
+            r.render(u)
+        r.sync()
+        clocks = ClockSampler(0)
+        clocks.start()
+        L.check(lib.xr_event_record(r.ctx, 0), r.ctx)
+        for u in ubos[args.warmup:]:
+            r.render(u)
+        L.check(lib.xr_event_record(r.ctx, 1), r.ctx)
+        ms = ctypes.c_float()
+        L.check(lib.xr_event_elapsed(r.ctx, 0, 1, ctypes.byref(ms)), r.ctx)
+        clk = clocks.stop()
+        r.set_graphs(False)
+        t_i, t_t, t_s = [], [], []
+        for u in ubos[args.warmup:args.warmup + min(args.steps, 16)]:
+            r.render(u)
+            st = r.stats()
+            t_i.append(st.ms_initial); t_t.append(st.ms_temporal); t_s.append(st.ms_spatial)
+        img = r.read_output(L.XR_OUT_LDR8)
+        out[mode] = {"ms_per_frame": round(ms.value / args.steps, 4), "bounces": nb,
+                     "passes_ms": {"initial_sample_1spp_pt": round(statistics.mean(t_i), 4),
+                                   "temporal": round(statistics.mean(t_t), 4),
+                                   "spatial": round(statistics.mean(t_s), 4)},
+                     "cumulative_ms": {"1spp_pt": round(statistics.mean(t_i), 4),
+                                       "restir_temporal": round(statistics.mean(t_i) + statistics.mean(t_t), 4),
+                                       "restir_spatial": round(statistics.mean(t_i) + statistics.mean(t_t) +
+                                                               statistics.mean(t_s), 4)},
+                     "rays_per_frame": st.rays_traced, "clocks": clk,
+                     "image_mean_ldr": round(float(np.asarray(img).reshape(-1, 4)[:, :3].mean()), 3)}
+        r.close()
+    line = {"metric": METRIC, "value": out["reference_settings"]["ms_per_frame"], "unit": "ms/frame", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["reference_settings"]["ms_per_frame"],
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "the reference's bundled Sibenik scene (asset/model/sb2, CC-BY-4.0)",
+            "config": {"workload": f"Sibenik 1920x1080, {scene.n_triangles} triangles, 3 textures, the "
+                                   "reference's default camera moving 0.01 units and 0.2 degrees per frame",
+                       "readme_published_ms": {"1spp_pt": 2.8, "restir_temporal": 2.9, "restir_spatial": 3.3,
+                                               "note": "README.md:7, RT cores on an unstated GPU, ReSTIR columns "
+                                                       "= UI frame time / 3 (src/Editor/UI.cpp:169): not comparable"}},
+            "modes": out}
     print(json.dumps(line), flush=True)
 
 
@@ -889,7 +989,7 @@ def main():
     ap.add_argument("--width", type=int, default=1920, help="smaller extents are for profiling only")
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--objects", type=int, default=4096, help="scene objects (4096 -> 998,442 triangles)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "4k", "dynamic", "cornell"],
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "4k", "dynamic", "cornell", "sibenik"],
                     help="frame: 1080p / 1M triangles (the headline); cornell: configuration 0 (256x256, "
                          "8 frames, FP64 reference of 65,536 spp); batch: 64 views over 8 scenes; "
                          "4k: 4 x 3840x2160 streams, 8M triangles, learned cache; "
@@ -910,6 +1010,8 @@ def main():
         run_dynamic(args)
     elif args.workload == "cornell":
         run_cornell(args)
+    elif args.workload == "sibenik":
+        run_sibenik(args)
     else:
         run_ours(args)
 

@@ -38,7 +38,7 @@ sys.path.insert(0, str(ROOT))
 import xvk_ray_gb300 as xr  # noqa: E402
 from oracle import refpin  # noqa: E402
 from tests.helpers import (RES_FIELDS, RES_INT_WORDS, RES_SAMPLE_FIELDS, SAMPLE_FIELDS,  # noqa: E402
-                           SAMPLE_INT_WORDS, box_scene, camera_sequence, field_digests, unorm8)
+                           SAMPLE_INT_WORDS, box_scene, camera_sequence, field_digests, scene_digest, unorm8)
 
 HERE = Path(__file__).resolve().parent
 C = xr._lib
@@ -336,6 +336,9 @@ SEQUENCES = [
     ("cornell_noreuse", "cornell", 64, 48, 3, 4, 1, False, False),
     ("textured_sky", "textured", 48, 40, 3, 4, 0, True, True),
     ("two_models_8_bounces", "two_models", 48, 40, 3, 8, 1, False, True),
+    # the README's Scene1 (asset/model/sb2) with the reference's own settings (10 bounces, its
+    # default camera): the scene is not stored here, only its SHA-1 (oracle/refpin/scenes.py)
+    ("sibenik_reference_settings", "ext:sibenik", 96, 54, 3, 10, 1, False, True),
 ]
 
 
@@ -351,8 +354,13 @@ def frames():
         for t, tex in enumerate(sc.textures):
             out[f"scene_{key}_texture{t}"] = tex
         out[f"scene_{key}_ntex"] = len(sc.textures)
+    from oracle.refpin import scenes as ref_scenes
     for name, key, W, H, nf, bounces, move_at, sky, reuse in SEQUENCES:
-        sc = scenes[key]
+        if key.startswith("ext:"):
+            sc = ref_scenes.load(key[4:])
+            out[f"{name}_scene_sha1"] = np.array(scene_digest(sc))
+        else:
+            sc = scenes[key]
         ubos = camera_sequence(sc, W, H, nf, bounces, move=_move_after(move_at), sky=sky, reuse=reuse)
         rs = refpin.RefScene(sc)
         rr = refpin.RefRenderer(rs, W, H)

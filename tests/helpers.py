@@ -175,3 +175,14 @@ def bake_instances(scenes, instances) -> "tuple[xr.Scene, np.ndarray, np.ndarray
     sc = xr.Scene(np.concatenate(verts), np.concatenate(idx).astype(np.uint32), np.concatenate(mats),
                   np.zeros((1, 2), np.uint32), scenes[0].camera)
     return sc, np.concatenate(inst_of), np.concatenate(prim_of)
+
+
+def scene_digest(sc) -> str:
+    """SHA-1 of a scene's arrays and textures."""
+    import hashlib
+    h = hashlib.sha1()
+    for a in (sc.vertices, sc.indices, sc.materials, sc.ranges):
+        h.update(np.ascontiguousarray(a).tobytes())
+    for t in sc.textures:
+        h.update(np.ascontiguousarray(t).tobytes())
+    return h.hexdigest()

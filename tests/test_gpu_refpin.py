@@ -29,7 +29,7 @@ GPU_SAMPLE_FIELDS = {k: SAMPLE_FIELDS[k] for k in ("x_view", "materialID", "n_vi
 def test_frames_match_reference_source(name):
     g = load_fixture("ref_frames.npz")
     meta = json.loads(str(g[f"{name}_meta"]))
-    scene = frame_scene(g, meta["scene"])
+    scene = frame_scene(g, meta["scene"], name)
     W, H = meta["width"], meta["height"]
     digests = json.loads(str(g[f"{name}_digests"]))
     with xr.Renderer(W, H) as r:

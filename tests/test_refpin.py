@@ -23,7 +23,7 @@ import xvk_ray_gb300 as xr
 from oracle import binding as ob
 from oracle import refpin
 from tests.helpers import (RES_FIELDS, RES_INT_WORDS, RES_SAMPLE_FIELDS, SAMPLE_FIELDS, SAMPLE_INT_WORDS,
-                           box_scene, camera_sequence, canon, canon_floats, field_digests)
+                           box_scene, camera_sequence, canon, canon_floats, field_digests, scene_digest)
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 XR = xr._lib
@@ -157,7 +157,18 @@ def test_python_restatement_agrees_with_reference_source():
 # ---------------------------------------------------------------------------
 # whole frames
 # ---------------------------------------------------------------------------
-def frame_scene(g, key) -> "xr.Scene":
+def frame_scene(g, key, name=None) -> "xr.Scene":
+    """A sequence's scene: stored in the fixture, or (`ext:<name>`) one of the
+    reference's glTF scenes converted by oracle/refpin/scenes.py, checked against
+    the SHA-1 the fixture recorded; skips when that scene is not available."""
+    if key.startswith("ext:"):
+        from oracle.refpin import scenes
+        try:
+            sc = scenes.load(key[4:])
+        except FileNotFoundError as e:
+            pytest.skip(str(e))
+        assert scene_digest(sc) == str(g[f"{name}_scene_sha1"]), "converted scene differs from the fixture's"
+        return sc
     cam = XR.XrCamera.from_buffer_copy(g[f"scene_{key}_camera"].tobytes())
     tex = [g[f"scene_{key}_texture{t}"] for t in range(int(g[f"scene_{key}_ntex"]))]
     return xr.Scene(g[f"scene_{key}_vertices"], g[f"scene_{key}_indices"], g[f"scene_{key}_materials"],
@@ -179,7 +190,7 @@ def frame_digests(samples, temporal, spatial, res_fields=ALL_RES_FIELDS) -> dict
 def test_frames_match_reference_source(name):
     g = load_fixture("ref_frames.npz")
     meta = json.loads(str(g[f"{name}_meta"]))
-    scene = frame_scene(g, meta["scene"])
+    scene = frame_scene(g, meta["scene"], name)
     W, H = meta["width"], meta["height"]
     o = ob.OracleRenderer(ob.OracleScene.from_scene(scene), xr.params_reference(W, H))
     digests = json.loads(str(g[f"{name}_digests"]))

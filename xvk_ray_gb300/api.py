@@ -45,6 +45,23 @@ class Scene:
             out[offs[r]:offs[r + 1]] += self.ranges[r, 1]
         return out
 
+    def save(self, path) -> None:
+        """Writes the scene (arrays, camera, RGBA8 textures) to one .npz file, e.g. to
+        keep a glTF scene in the upload layout and skip parsing it again."""
+        tex = {f"texture{i}": t for i, t in enumerate(self.textures)}
+        np.savez_compressed(path, vertices=self.vertices, indices=self.indices, materials=self.materials,
+                            ranges=self.ranges, camera=np.frombuffer(bytes(self.camera), np.uint8),
+                            n_textures=len(self.textures), **tex)
+
+    @staticmethod
+    def load(path) -> "Scene":
+        """A scene written by Scene.save."""
+        with np.load(path) as z:
+            cam = L.XrCamera.from_buffer_copy(z["camera"].tobytes())
+            tex = [np.ascontiguousarray(z[f"texture{i}"]) for i in range(int(z["n_textures"]))]
+            return Scene(np.ascontiguousarray(z["vertices"]), np.ascontiguousarray(z["indices"]),
+                         np.ascontiguousarray(z["materials"]), np.ascontiguousarray(z["ranges"]), cam, tex)
+
     @staticmethod
     def _generate(fn, *args) -> "Scene":
         lib = L.load()
