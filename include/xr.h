@@ -314,16 +314,26 @@ xr_status xr_render_reference_views(XrContext* ctx, const XrUniformBufferObject*
                                     double* host_rgb);
 xr_status xr_set_graphs(XrContext* ctx, int enabled);   /* CUDA-graph replay of frames */
 
-/* Launch configuration chosen by xr_autotune: persistent CTAs per SM of the
-   traversal and shading kernels (0 = the occupancy maximum). */
+/* Launch configuration chosen by xr_autotune.  0 in any field = its default.
+   Launch shapes never change results: every configuration renders bit-identically. */
 typedef struct XrTuning {
-    uint32_t trace_ctas_per_sm, shade_ctas_per_sm;
-    float ms_per_frame;          /* best measured configuration */
-    float ms_default;            /* the occupancy-maximum configuration */
+    uint32_t trace_ctas_per_sm;  /* persistent traversal CTAs per SM (default: occupancy maximum) */
+    uint32_t shade_ctas_per_sm;  /* persistent shading CTAs per SM (default: occupancy maximum) */
+    float ms_per_frame;          /* xr_autotune: best measured configuration */
+    float ms_default;            /* xr_autotune: the all-defaults configuration */
     uint32_t configs_tried;
+    /* ray queues of the persistent traversal: a warp refills from its queue once this many
+       lanes are idle (default 8), and postpones triangle tests that fewer lanes than this
+       have (default 8) */
+    uint32_t refill_min, postpone_below;
+    uint32_t ray_bundle;         /* camera rays of a 16 x 8 tile per warp: 0 8x4 blocks (default), 1 16x2 rows, 2 4x8 */
+    uint32_t temporal_block;     /* threads per block of the temporal pass: 32, 64 (default), 128, 256 */
+    uint32_t spatial_block;      /* threads per block of the spatial passes: 64, 128 (default), 256 */
 } XrTuning;
-/* Times `frames` frames of every candidate configuration (ubos: frames x views, in
-   frame order) and keeps the fastest for the context's later frames. */
+/* Coordinate descent over the fields above (in the order listed): for each, the
+   value whose `frames` frames run shortest (ubos: frames x views, in frame order)
+   with the others at the best so far.  The choice stays for the context's later
+   frames and is written to *out. */
 xr_status xr_autotune(XrContext* ctx, const XrUniformBufferObject* ubos, uint32_t frames, XrTuning* out);
 /* Applies a launch configuration (e.g. one xr_autotune chose earlier); 0 = occupancy maximum. */
 xr_status xr_set_tuning(XrContext* ctx, const XrTuning* tuning);

@@ -49,7 +49,10 @@ def _batch(scenes, seqs, params_fn, frames, graphs=False, tuning=None):
     if graphs:
         r.set_graphs(True)
     if tuning is not None:
-        r.set_tuning(*tuning)
+        if isinstance(tuning, dict):
+            r.set_tuning(**tuning)
+        else:
+            r.set_tuning(tuning=tuning) if hasattr(tuning, "refill_min") else r.set_tuning(*tuning)
     for f in range(frames):
         r.render_views([seqs[v][f] for v in range(len(VIEWS))])
     out = [r.read_view_output(v, L.XR_OUT_HDR) for v in range(len(VIEWS))]
@@ -91,8 +94,10 @@ def test_autotuned_launches_do_not_change_results():
         r.upload_scenes(scenes)
         r.set_views(VIEWS, xr.params_default(8, 8, write_hdr=1))
         t = r.autotune([[seqs[v][f] for v in range(len(VIEWS))] for f in range(frames)])
-    assert t.configs_tried >= 2 and t.ms_per_frame > 0 and t.ms_default > 0
-    for tuning in ((t.trace_ctas_per_sm, t.shade_ctas_per_sm), (3, 1)):
+    assert t.configs_tried >= 15 and 0 < t.ms_per_frame <= t.ms_default
+    # the tuner's choice, fewer persistent CTAs, and every tile / queue knob away from its default
+    knobs = dict(refill_min=4, postpone_below=16, ray_bundle=2, temporal_block=256, spatial_block=64)
+    for tuning in (t, (3, 1), knobs, dict(ray_bundle=1, temporal_block=32, spatial_block=256, refill_min=12)):
         tuned, _ = _batch(scenes, seqs, xr.params_default, frames, tuning=tuning)
         for k in range(len(VIEWS)):
             assert np.array_equal(plain[k].view(np.uint32), tuned[k].view(np.uint32)), (tuning, k)

@@ -127,7 +127,9 @@ class XrView(C.Structure):
 
 class XrTuning(C.Structure):
     _fields_ = [("trace_ctas_per_sm", C.c_uint32), ("shade_ctas_per_sm", C.c_uint32), ("ms_per_frame", C.c_float),
-                ("ms_default", C.c_float), ("configs_tried", C.c_uint32)]
+                ("ms_default", C.c_float), ("configs_tried", C.c_uint32), ("refill_min", C.c_uint32),
+                ("postpone_below", C.c_uint32), ("ray_bundle", C.c_uint32), ("temporal_block", C.c_uint32),
+                ("spatial_block", C.c_uint32)]
 
 
 XR_CACHE_MLP, XR_CACHE_GRID, XR_CACHE_MLP_GRAD, XR_CACHE_GRID_GRAD = 0, 1, 2, 3

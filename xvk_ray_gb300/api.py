@@ -234,8 +234,12 @@ class Renderer:
         self._c(self._lib.xr_autotune(self.ctx, C.cast(arr, C.c_void_p), len(frames), C.byref(t)))
         return t
 
-    def set_tuning(self, trace_ctas_per_sm: int, shade_ctas_per_sm: int) -> None:
-        t = L.XrTuning(trace_ctas_per_sm, shade_ctas_per_sm, 0.0, 0.0, 0)
+    def set_tuning(self, trace_ctas_per_sm: int = 0, shade_ctas_per_sm: int = 0, *, refill_min: int = 0,
+                   postpone_below: int = 0, ray_bundle: int = 0, temporal_block: int = 0, spatial_block: int = 0,
+                   tuning: "L.XrTuning | None" = None) -> None:
+        """A launch configuration (0 = the default of each knob), or one xr_autotune chose."""
+        t = tuning if tuning is not None else L.XrTuning(trace_ctas_per_sm, shade_ctas_per_sm, 0.0, 0.0, 0, refill_min,
+                                                         postpone_below, ray_bundle, temporal_block, spatial_block)
         self._c(self._lib.xr_set_tuning(self.ctx, C.byref(t)))
 
     def render(self, ubo: L.XrUniformBufferObject) -> None:

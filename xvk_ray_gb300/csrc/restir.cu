@@ -564,13 +564,16 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
     // view's first pixel, the full tile rows above (only the last can be short),
     // the tiles to the left in this row, the position inside the (possibly cut) tile.
     // In a full tile the 32 slots a warp fetches first cover an 8 x 4 block (four blocks
-    // per tile) rather than two 16-pixel rows: squarer bundles of camera rays.
+    // per tile) rather than two 16-pixel rows: squarer bundles of camera rays (the
+    // default bundle; the tuner may pick 16 x 2 rows or 4 x 8 blocks instead).
     if (alive) {
         const uint32_t rows = min(8u, VH - ty * 8u), cols = min(16u, VW - tx * 16u);
         const uint32_t xi = threadIdx.x & 15u, yi = threadIdx.x >> 4;
-        const uint32_t in_tile = (rows == 8u && cols == 16u)
-                                     ? ((yi >> 2) * 2u + (xi >> 3)) * 32u + morton_8x4(xi & 7u, yi & 3u)
-                                     : yi * cols + xi;
+        uint32_t in_tile = yi * cols + xi;   // a cut tile, and bundle 1 (16 x 2 rows): row order
+        if (rows == 8u && cols == 16u) {
+            if (fa.ray_bundle == 0u) in_tile = ((yi >> 2) * 2u + (xi >> 3)) * 32u + morton_8x4(xi & 7u, yi & 3u);
+            else if (fa.ray_bundle == 2u) in_tile = (xi >> 2) * 32u + yi * 4u + (xi & 3u);   // 4 x 8 blocks
+        }
         const uint32_t i = base + ty * 8u * VW + tx * 16u * rows + in_tile;
         fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
         fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
@@ -981,7 +984,8 @@ __device__ __forceinline__ void rng_skip(uint32_t& st, uint32_t n) {
 #ifndef XR_TEMPORAL_BLOCK
 #define XR_TEMPORAL_BLOCK 64
 #endif
-__global__ void __launch_bounds__(XR_TEMPORAL_BLOCK) k_temporal(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
+// launch bounds: blocks of up to 256 threads (the block size is a tuning parameter, default XR_TEMPORAL_BLOCK)
+__global__ void __launch_bounds__(256) k_temporal(FrameArgs fa, const XrUniformBufferObject* __restrict__ u, bool out_here) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
     const PixView pv = pix_view(fa, p);
@@ -1067,7 +1071,9 @@ __global__ void __launch_bounds__(XR_TEMPORAL_BLOCK) k_temporal(FrameArgs fa, co
 #ifndef XR_SPATIAL_BLOCK
 #define XR_SPATIAL_BLOCK 128
 #endif
-__global__ void __launch_bounds__(XR_SPATIAL_BLOCK, XR_SELECT_MIN_BLOCKS * 256 / XR_SPATIAL_BLOCK) k_spatial_select(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+// launch bounds: blocks of up to 256 threads (the block size is a tuning parameter, default XR_SPATIAL_BLOCK),
+// XR_SELECT_MIN_BLOCKS x 256 threads resident per SM
+__global__ void __launch_bounds__(256, XR_SELECT_MIN_BLOCKS) k_spatial_select(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = lane_id();
     uint32_t emit_mask = 0u;
@@ -1203,7 +1209,7 @@ __global__ void __launch_bounds__(kTraceBlock, 1) k_trace_nee(FrameArgs fa) {
 #ifndef XR_RESOLVE_MIN_BLOCKS
 #define XR_RESOLVE_MIN_BLOCKS 5
 #endif
-__global__ void __launch_bounds__(XR_SPATIAL_BLOCK, XR_RESOLVE_MIN_BLOCKS * 256 / XR_SPATIAL_BLOCK) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
+__global__ void __launch_bounds__(256, XR_RESOLVE_MIN_BLOCKS) k_spatial_resolve(FrameArgs fa, const XrUniformBufferObject* __restrict__ u) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= fa.N) return;
     const PixView pv = pix_view(fa, p);
@@ -1450,7 +1456,10 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
 void launch_temporal(const FrameArgs& fa, bool write_image, cudaStream_t st) {
     uint32_t blocks = (fa.N + 255u) / 256u;
     if (fa.compat) k_temporal_compat<<<blocks, 256, 0, st>>>(fa, fa.ubo, write_image);
-    else k_temporal<<<(fa.N + XR_TEMPORAL_BLOCK - 1u) / XR_TEMPORAL_BLOCK, XR_TEMPORAL_BLOCK, 0, st>>>(fa, fa.ubo, write_image);
+    else {
+        const uint32_t tb = fa.blk_temporal ? fa.blk_temporal : (uint32_t)XR_TEMPORAL_BLOCK;
+        k_temporal<<<(fa.N + tb - 1u) / tb, tb, 0, st>>>(fa, fa.ubo, write_image);
+    }
 }
 
 void launch_export_samples(const FrameArgs& fa, uint32_t* out, cudaStream_t st) {
@@ -1487,13 +1496,14 @@ void launch_spatial(const FrameArgs& fa, cudaStream_t st) {
         k_spatial_compat<<<blocks, 256, 0, st>>>(fa, fa.ubo);
         return;
     }
-    const uint32_t sblocks = (fa.N + XR_SPATIAL_BLOCK - 1u) / XR_SPATIAL_BLOCK;
-    k_spatial_select<<<sblocks, XR_SPATIAL_BLOCK, 0, st>>>(fa, fa.ubo);
+    const uint32_t sb = fa.blk_spatial ? fa.blk_spatial : (uint32_t)XR_SPATIAL_BLOCK;
+    const uint32_t sblocks = (fa.N + sb - 1u) / sb;
+    k_spatial_select<<<sblocks, sb, 0, st>>>(fa, fa.ubo);
     if (fa.visibility) {
         if (fa.sc.n_inst) k_trace_shadow<true><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(fa);
         else k_trace_shadow<false><<<fa.grid_trace, kTraceBlock, 0, st>>>(fa);
     }
-    k_spatial_resolve<<<sblocks, XR_SPATIAL_BLOCK, 0, st>>>(fa, fa.ubo);
+    k_spatial_resolve<<<sblocks, sb, 0, st>>>(fa, fa.ubo);
 }
 
 }  // namespace xr

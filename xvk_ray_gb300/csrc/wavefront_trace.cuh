@@ -2,7 +2,7 @@
 //
 // Software replacement of the hardware TraceRay (opaque triangles, no culling,
 // closest hit with ties to the lowest primitive id, or first hit for shadow
-// rays).  Each warp keeps 32 rays in flight; once at least kRefillMin lanes have
+// rays).  Each warp keeps 32 rays in flight; once at least refill_min lanes have
 // finished (or all have), the warp refills them from the ray queue with one
 // atomic (Aila and Laine, "Understanding the Efficiency of Ray Traversal on
 // GPUs", HPG 2009): the per-ray set-up (reciprocals, shear constants) then runs
@@ -30,8 +30,8 @@ constexpr uint32_t kLevelBit = 0x40000000u;      // stack entry marks the return
 #ifndef XR_REFILL_MIN
 #define XR_REFILL_MIN 8
 #endif
-constexpr int kPostponeBelow = XR_POSTPONE_BELOW;  // lanes; fewer testing triangles -> postpone
-constexpr int kRefillMin = XR_REFILL_MIN;          // idle lanes before a refill (swept 1..16: 1 is 9% slower)
+constexpr int kPostponeBelow = XR_POSTPONE_BELOW;  // default: lanes; fewer testing triangles -> postpone
+constexpr int kRefillMin = XR_REFILL_MIN;          // default: idle lanes before a refill (swept 1..16: 1 is 9% slower)
 constexpr float kMinDir = 1e-20f;                 // smallest direction component seen by the box test
 
 struct RayIn {
@@ -82,6 +82,9 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                                                  unsigned long long* work = nullptr, uint32_t* nonfinite = nullptr) {
     const uint32_t FULL = 0xFFFFFFFFu;
     uint32_t n_visits = 0, n_tests = 0, n_nonfinite = 0;
+    // queue tuning of the context (0: the defaults kRefillMin / kPostponeBelow)
+    const int refill_min = sc.refill_min ? (int)sc.refill_min : kRefillMin;
+    const int postpone_below = sc.postpone_below ? (int)sc.postpone_below : kPostponeBelow;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
     bool active = false, drained = false;
@@ -117,7 +120,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
     while (true) {
         // ---- refill idle lanes ----
         const uint32_t idle = __ballot_sync(FULL, !active);
-        if (idle && !drained && (__popc(idle) >= kRefillMin || idle == FULL)) {
+        if (idle && !drained && (__popc(idle) >= refill_min || idle == FULL)) {
             const uint32_t n_idle = __popc(idle);
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(next, n_idle);
@@ -246,7 +249,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
             const bool want = active && tg_mask != 0u;
             const uint32_t m = __ballot_sync(FULL, want);
             if (!m) break;
-            if (!first && (int)__popc(m) < kPostponeBelow) {
+            if (!first && (int)__popc(m) < postpone_below) {
                 if (want && sp < kStackSize) {
                     stack[sp++] = make_uint2(tg_base, tg_mask | kTriGroupBit);
                     tg_mask = 0u;

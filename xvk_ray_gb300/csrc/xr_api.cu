@@ -186,6 +186,7 @@ void set_frame_pointers(Context* c, uint32_t parity) {
     fa.grid_persistent = c->tune_shade_ctas ? c->tune_shade_ctas * (uint32_t)c->sm_count
                                             : persistent_grid(c->sm_count, P.compat_reference != 0);
     fa.grid_trace = c->tune_trace_ctas ? c->tune_trace_ctas * (uint32_t)c->sm_count : trace_grid(c->sm_count, !c->instances.empty());
+    apply_tuning(c);
 }
 
 // Host side of a frame's UBO upload: wait until the previous frame's transfer has
@@ -218,6 +219,20 @@ xr_status enqueue_ubos(Context* c, uint32_t n) {
     if (s) return s;
     return cuda_check(c, record_event(c, c->ev[5]), "ubo event");
 }
+
+}  // namespace
+
+// Launch-shape tuning of the context into the kernel arguments (0 = the default of each).
+void apply_tuning(Context* c) {
+    FrameArgs& fa = c->fa;
+    fa.sc.refill_min = c->tune_refill;
+    fa.sc.postpone_below = c->tune_postpone;
+    fa.ray_bundle = c->tune_bundle;
+    fa.blk_temporal = c->tune_temporal_block;
+    fa.blk_spatial = c->tune_spatial_block;
+}
+
+namespace {
 
 xr_status upload_ubo(Context* c, const XrUniformBufferObject* ubo) {
     xr_status s = stage_ubos(c, ubo, 1u);
@@ -712,16 +727,35 @@ xr_status xr_set_graphs(XrContext* c, int enabled) {
     return XR_OK;
 }
 
+static bool valid_block(uint32_t b) { return b == 0 || b == 32 || b == 64 || b == 128 || b == 256; }
+
 xr_status xr_set_tuning(XrContext* c, const XrTuning* t) {
     if (!c || !t) return fail(c, XR_ERR_INVALID_ARGUMENT, "set_tuning: null argument");
     if (t->trace_ctas_per_sm > 64 || t->shade_ctas_per_sm > 64)
         return fail(c, XR_ERR_INVALID_ARGUMENT, "set_tuning: at most 64 CTAs per SM");
+    if (t->refill_min > 32 || t->postpone_below > 32 || t->ray_bundle > 2 || !valid_block(t->temporal_block) ||
+        !valid_block(t->spatial_block))
+        return fail(c, XR_ERR_INVALID_ARGUMENT,
+                    "set_tuning: refill_min / postpone_below <= 32, ray_bundle <= 2, blocks of 32 .. 256 threads");
     DeviceGuard g(c->device);
     c->tune_trace_ctas = t->trace_ctas_per_sm;
     c->tune_shade_ctas = t->shade_ctas_per_sm;
+    c->tune_refill = t->refill_min;
+    c->tune_postpone = t->postpone_below;
+    c->tune_bundle = t->ray_bundle;
+    c->tune_temporal_block = t->temporal_block;
+    c->tune_spatial_block = t->spatial_block;
     invalidate_graphs(c);
     return XR_OK;
 }
+
+// The tuning knobs, one field of XrTuning each, in the order the tuner visits them.
+namespace {
+struct Knob {
+    uint32_t* field;
+    std::vector<uint32_t> values;   // the first is the current default
+};
+}  // namespace
 
 xr_status xr_autotune(XrContext* c, const XrUniformBufferObject* ubos, uint32_t frames, XrTuning* out) {
     if (!c || !ubos || frames == 0) return fail(c, XR_ERR_INVALID_ARGUMENT, "autotune: bad argument");
@@ -729,50 +763,75 @@ xr_status xr_autotune(XrContext* c, const XrUniformBufferObject* ubos, uint32_t 
     const uint32_t n = c->fa.n_views;
     int occ_t = 0, occ_s = 0;
     {
-        // the occupancy maxima are what grid 0 (the default) resolves to
+        // the occupancy maxima are what 0 (the default) resolves to
         const uint32_t t0 = trace_grid(c->sm_count, !c->instances.empty()), s0 = persistent_grid(c->sm_count, c->params.compat_reference != 0);
         occ_t = (int)(t0 / (uint32_t)c->sm_count);
         occ_s = (int)(s0 / (uint32_t)c->sm_count);
     }
-    std::vector<std::pair<uint32_t, uint32_t>> cands;
-    for (int t : {0, occ_t * 3 / 4, occ_t / 2})
-        for (int sh : {0, occ_s / 2}) {
-            // 0 is the occupancy maximum; fractions that round to it or to nothing are skipped
-            const std::pair<uint32_t, uint32_t> cand{(uint32_t)(t == occ_t ? 0 : t), (uint32_t)(sh == occ_s ? 0 : sh)};
-            if ((t == 0 || t >= 1) && (sh == 0 || sh >= 1) &&
-                std::find(cands.begin(), cands.end(), cand) == cands.end())
-                cands.push_back(cand);
-        }
-    float best = 1e30f, dflt = 0.0f;
-    std::pair<uint32_t, uint32_t> pick{0u, 0u};
+    auto fractions = [](int occ) {
+        std::vector<uint32_t> v{0u};
+        for (int x : {occ * 3 / 4, occ / 2})
+            if (x >= 1 && x != occ && std::find(v.begin(), v.end(), (uint32_t)x) == v.end()) v.push_back((uint32_t)x);
+        return v;
+    };
+    // coordinate descent: each knob in turn takes the value with the shortest frames, the
+    // others held at the best so far (0 = the built-in default of every knob)
+    std::vector<Knob> knobs = {
+        {&c->tune_trace_ctas, fractions(occ_t)},                       // persistent traversal CTAs per SM
+        {&c->tune_shade_ctas, fractions(occ_s)},                       // persistent shading CTAs per SM
+        {&c->tune_refill, {0u, 4u, 6u, 12u, 16u}},                     // ray-queue refill: idle lanes per fetch
+        {&c->tune_postpone, {0u, 4u, 12u, 16u}},                       // triangle tests postponed below this many lanes
+        {&c->tune_bundle, {0u, 1u, 2u}},                               // camera-ray bundle: 8x4, 16x2, 4x8 pixels
+        {&c->tune_temporal_block, {0u, 32u, 128u, 256u}},              // temporal pass block (default 64)
+        {&c->tune_spatial_block, {0u, 64u, 256u}},                     // spatial passes' block (default 128)
+    };
+    for (Knob& k : knobs) *k.field = 0u;
     xr_status s = XR_OK;
-    for (const auto& cand : cands) {
-        c->tune_trace_ctas = cand.first;
-        c->tune_shade_ctas = cand.second;
+    uint32_t tried = 0;
+    float best = 1e30f, dflt = 0.0f;
+    auto time_frames = [&](float* ms) -> xr_status {
         invalidate_graphs(c);
         // one untimed frame (graph capture, caches), then the timed frames
-        if ((s = render_impl(c, ubos, n, "autotune"))) break;
+        xr_status e = render_impl(c, ubos, n, "autotune");
+        if (e) return e;
         cudaEventRecord(c->user_ev[6], c->stream);
-        for (uint32_t f = 0; f < frames && !s; f++) s = render_impl(c, ubos + (size_t)f * n, n, "autotune");
-        if (s) break;
+        for (uint32_t f = 0; f < frames && !e; f++) e = render_impl(c, ubos + (size_t)f * n, n, "autotune");
+        if (e) return e;
         cudaEventRecord(c->user_ev[7], c->stream);
-        if ((s = xr_sync(c))) break;
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, c->user_ev[6], c->user_ev[7]);
-        ms /= (float)frames;
-        if (cand.first == 0 && cand.second == 0) dflt = ms;
-        if (ms < best) { best = ms; pick = cand; }
+        if ((e = xr_sync(c))) return e;
+        cudaEventElapsedTime(ms, c->user_ev[6], c->user_ev[7]);
+        *ms /= (float)frames;
+        tried++;
+        return XR_OK;
+    };
+    if ((s = time_frames(&dflt))) return s;
+    best = dflt;
+    for (Knob& k : knobs) {
+        const uint32_t keep = *k.field;
+        uint32_t pick = keep;
+        for (uint32_t v : k.values) {
+            if (v == keep) continue;
+            *k.field = v;
+            float ms = 0.0f;
+            if ((s = time_frames(&ms))) break;
+            if (ms < best) { best = ms; pick = v; }
+        }
+        *k.field = pick;
+        if (s) break;
     }
-    c->tune_trace_ctas = pick.first;
-    c->tune_shade_ctas = pick.second;
     invalidate_graphs(c);
     if (s) return s;
     if (out) {
-        out->trace_ctas_per_sm = pick.first ? pick.first : (uint32_t)occ_t;
-        out->shade_ctas_per_sm = pick.second ? pick.second : (uint32_t)occ_s;
+        out->trace_ctas_per_sm = c->tune_trace_ctas ? c->tune_trace_ctas : (uint32_t)occ_t;
+        out->shade_ctas_per_sm = c->tune_shade_ctas ? c->tune_shade_ctas : (uint32_t)occ_s;
         out->ms_per_frame = best;
         out->ms_default = dflt;
-        out->configs_tried = (uint32_t)cands.size();
+        out->configs_tried = tried;
+        out->refill_min = c->tune_refill;
+        out->postpone_below = c->tune_postpone;
+        out->ray_bundle = c->tune_bundle;
+        out->temporal_block = c->tune_temporal_block;
+        out->spatial_block = c->tune_spatial_block;
     }
     return XR_OK;
 }
@@ -1001,6 +1060,7 @@ static xr_status trace_device(XrContext* c, const float* d_rays, uint32_t n, int
     if (n && (!d_rays || !d_prim || !d_t || !d_bary)) return fail(c, XR_ERR_INVALID_ARGUMENT, "trace: null array");
     DeviceGuard g(c->device);
     if (xr_status s0 = sync_tlas(c)) return s0;
+    apply_tuning(c);
     cudaMemsetAsync(c->d_counters + kCntFetchQuery, 0, 4, c->stream);
     cudaMemsetAsync(c->d_work, 0, 2 * sizeof(unsigned long long), c->stream);
     c->query_rays = n;

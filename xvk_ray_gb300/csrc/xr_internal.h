@@ -112,6 +112,9 @@ struct DeviceScene {
     uint32_t n_inst_slots;
     const float4* inst_xform;        // 6 float4 per instance: object-to-world rows, world-to-object rows
     uint32_t n_inst;                 // 0: no instances
+    // traversal queue tuning (xr_set_tuning / xr_autotune): idle lanes before a warp refills
+    // from the ray queue, and lanes with triangles below which a warp postpones its tests
+    uint32_t refill_min, postpone_below;
 };
 
 // One view of a multi-view context: its pixels are [pix_off, pix_off + W H) of the
@@ -162,6 +165,8 @@ struct FrameArgs {
                               // of a similar neighbour, {kInvalid, 0} otherwise
     uint32_t* counters;       // [b] paths entering bounce b, then the kCnt* words above
     uint32_t grid_persistent, grid_trace;
+    uint32_t ray_bundle;      // camera-ray slot order in a 16 x 8 tile: 0 8x4 blocks, 1 16x2 rows, 2 4x8 blocks
+    uint32_t blk_temporal, blk_spatial;   // threads per block of the temporal and spatial kernels
     // learned radiance cache (corrected mode): paths end at x_s unless selected for training
     uint32_t cache_on;
     uint4* cache_q;           // query records, 2 uint4 each (capacity N)
@@ -333,6 +338,7 @@ struct Context {
     uint32_t graph_bounces[2] = {0, 0};
     // launch configuration (xr_autotune): persistent CTAs per SM, 0 = occupancy maximum
     uint32_t tune_trace_ctas = 0, tune_shade_ctas = 0;
+    uint32_t tune_refill = 0, tune_postpone = 0, tune_bundle = 0, tune_temporal_block = 0, tune_spatial_block = 0;
 };
 
 constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
@@ -377,7 +383,8 @@ void free_lights(Context* c);
 xr_status upload_lights(Context* c, const std::vector<uint4>& tri, const std::vector<float4>& pos,
                         const XrMaterial* m, uint32_t nm);
 xr_status rebuild_tlas(Context* c);                           // instances.cu
-xr_status sync_tlas(Context* c);   // instances.cu: rebuild a stale top level (no-op otherwise)
+xr_status sync_tlas(Context* c);
+void apply_tuning(Context* c);     // xr_api.cu: the context's tuning into fa (and fa.sc) before launches   // instances.cu: rebuild a stale top level (no-op otherwise)
 void free_instances(Context* c);                              // instances.cu
 
 // ---- launch wrappers (trace.cu) ----
