@@ -761,7 +761,11 @@ def run_batch(args):
         "ms_per_frame_direct_launches": round(ms_direct, 4),
         "graph_speedup": round(ms_direct / ms_graph, 4),
         "tuning": {"trace_ctas_per_sm": tuning.trace_ctas_per_sm, "shade_ctas_per_sm": tuning.shade_ctas_per_sm,
-                   "ms_tuned": round(tuning.ms_per_frame, 4), "ms_occupancy_default": round(tuning.ms_default, 4),
+                   "refill_min": tuning.refill_min or "default (8)", "postpone_below": tuning.postpone_below or "default (8)",
+                   "ray_bundle": ["8x4", "16x2", "4x8"][tuning.ray_bundle],
+                   "temporal_block": tuning.temporal_block or "default (64)",
+                   "spatial_block": tuning.spatial_block or "default (128)",
+                   "ms_tuned": round(tuning.ms_per_frame, 4), "ms_all_defaults": round(tuning.ms_default, 4),
                    "configs_tried": tuning.configs_tried},
         "scene_build_s": round(build_s, 3),
         "gpu_launches": FRAME_LAUNCHES * args.steps,
