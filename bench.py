@@ -49,9 +49,10 @@ RESERVOIR_BYTES_PER_PX = TEMPORAL_BYTES_PER_PX + SPATIAL_BYTES_PER_PX   # 232
 # DRAM bytes (read + write) of one k_temporal launch at 1920x1080 measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum): 185.2 MB + 47.7 MB
 TEMPORAL_DRAM_BYTES_1080P = 232.4e6
-# DRAM bytes of one frame's four reservoir-pass kernels (ncu): k_temporal 232.4 MB, k_spatial_select
-# 128.2 MB, k_spatial_resolve 215.9 MB; k_trace_shadow's DRAM traffic is not in a committed capture yet
-PASSES_DRAM_BYTES_1080P = None
+# DRAM bytes of one 1080p frame's four reservoir-pass kernels (ncu): k_temporal 232.4 MB, k_spatial_select
+# 128.2 MB, k_spatial_resolve 215.9 MB (1080p captures), k_trace_shadow about 44 MB (its 960x540 capture
+# scaled by the shadow rays traced)
+PASSES_DRAM_BYTES_1080P = 621e6
 # kernels per frame: raygen, (trace + shade) per bounce, temporal, spatial select,
 # shadow trace, spatial resolve
 FRAME_LAUNCHES = 1 + 2 * BOUNCES + 4
