@@ -1214,7 +1214,14 @@ void spatial_pixel(Renderer& R, uint32_t x, uint32_t y, const OrUBO& u) {
             occluded = hh.prim >= 0;
             if (occluded) ph = 0.0f;
         }
-        merge_reservoir(r_s, r_nb, ph, rng);
+        if (occluded) {
+            // corrected: an occluded neighbour merges with weight 0 (its M below)
+            const uint32_t M0 = r_s.m;
+            update_reservoir(r_s, r_nb.s, 0.0f, rng);
+            r_s.m = M0 + r_nb.m;
+        } else {
+            merge_reservoir(r_s, r_nb, ph, rng);
+        }
         // reference: a neighbour whose weight is zero does not count towards M
         // (ReSTIRGISpatialReuse.rgen.hlsl:140-143); corrected: every similar
         // neighbour counts (1/M normalisation) except one whose sample is occluded

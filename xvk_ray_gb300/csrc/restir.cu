@@ -1110,17 +1110,22 @@ __global__ void __launch_bounds__(256, XR_SELECT_MIN_BLOCKS) k_spatial_select(Fr
                     nx_mat = fa.gb_mat_cur[nx_i];
                     nx_g = fa.gb_pos_cur[nx_i];
                 }
+                uint32_t nm = 0u;
                 if (nmat != kInvalid && nmat == mat) {
                     const float3 dd = x_view - xyz(ng);
                     if (!(dot(dd, dd) > 0.1f) && !(dot(n_view, oct_decode(__float_as_uint(ng.w), 16)) < 0.8f)) {
                         Res rn;
                         load_packed(fa.rt_cur0, fa.rt_cur1, nbi, rn);
                         const float ph = target_corrected(P, rn.xs, rn.L) * jacobian_of(xyz(ng), x_view, rn.xs, rn.ns);
-                        slot = make_uint2(nbi, __float_as_uint(ph));
+                        // the merge weight of MergeReservoir (ReSTIRGICommon.hlsl:68): resolve merges
+                        // from the slots and gathers only the reservoir that wins
+                        slot = make_uint2(nbi, __float_as_uint(ph * rn.W * (float)rn.m));
+                        nm = rn.m;
                         if (fa.visibility && ph > 0.0f) { emit_mask |= 1u << i; nb_of[i] = nbi; }
                     }
                 }
                 fa.nb_slot[(size_t)i * fa.N + p] = slot;
+                fa.nb_m[(size_t)i * fa.N + p] = (uint8_t)nm;
             }
         }
     }
@@ -1236,19 +1241,32 @@ __global__ void __launch_bounds__(256, XR_RESOLVE_MIN_BLOCKS) k_spatial_resolve(
     Res r; res_init(r);
     const float tp_center = target_corrected(P, center.xs, center.L);
     float tp_sel = res_merge(r, center, tp_center, rng) ? tp_center : -1.0f;
+    // MergeReservoir of every similar neighbour with its weight from step 1 (0 when its
+    // shadow ray was occluded); only the winning neighbour's reservoir is gathered, after the loop
+    uint32_t win = kInvalid;
     for (uint32_t i = 0; i < nn; i++) {
         const uint2 slot = fa.nb_slot[(size_t)i * fa.N + p];
         if (slot.x == kInvalid) continue;   // not similar: no merge, no draw
-        Res rn;
-        load_packed(fa.rt_cur0, fa.rt_cur1, slot.x, rn, false);
-        float ph = __uint_as_float(slot.y);
-        const bool occluded = ph > 0.0f && ((occ >> i) & 1u);
-        if (occluded) ph = 0.0f;
-        if (res_merge(r, rn, ph, rng)) tp_sel = -1.0f;   // a neighbour's sample: its target is re-evaluated
+        const uint32_t mi = fa.nb_m[(size_t)i * fa.N + p];
+        const bool occluded = (occ >> i) & 1u;   // set only for the rays step 1 emitted (weight > 0)
+        const float w_new = occluded ? 0.0f : __uint_as_float(slot.y);
+        const uint32_t M0 = r.m;
+        r.w_sum += w_new;
+        r.m++;
+        if (random_float(rng) < w_new / fmaxf(1e-10f, r.w_sum)) {
+            win = slot.x;
+            tp_sel = -1.0f;   // a neighbour's sample: its target is re-evaluated
+        }
+        r.m = M0 + mi;
         // every similar neighbour counts towards M (1/M normalisation) except one
         // whose sample is occluded; the reference also drops zero-weight neighbours
         // (ReSTIRGISpatialReuse.rgen.hlsl:140-143), which biases the estimate upwards
-        if (occluded) r.m -= rn.m;
+        if (occluded) r.m -= mi;
+    }
+    if (win != kInvalid) {
+        Res rn;
+        load_packed(fa.rt_cur0, fa.rt_cur1, win, rn, false);
+        r.xs = rn.xs; r.L = rn.L; r.ns = rn.ns; r.f = rn.f; r.code = rn.code;
     }
     const float3 col = finish_corrected(P, r, tp_sel, fa.m_cap_s, true);
     store_packed(fa.rs0, fa.rs1, p, r);

@@ -120,6 +120,7 @@ xr_status alloc_pixels(Context* c) {
         add((void**)&fa.occ, N * 4);
         add((void**)&fa.shadow_q, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
         add((void**)&fa.nb_slot, N * std::max<uint32_t>(P.n_neighbours, 1u) * 8);
+        add((void**)&fa.nb_m, N * std::max<uint32_t>(P.n_neighbours, 1u));
         add((void**)&fa.reproj, N * 4);
     }
     add((void**)&fa.hits, N * 16);

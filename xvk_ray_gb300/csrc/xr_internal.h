@@ -161,8 +161,9 @@ struct FrameArgs {
     uint2* shadow_q;          // corrected spatial pass: {pixel << 5 | slot, neighbour pixel}
     uint32_t* occ;            // per pixel: occluded neighbour slots
     uint32_t* reproj;         // corrected mode, per pixel: its visible point's pixel in the previous frame (kInvalid: none)
-    uint2* nb_slot;           // corrected spatial pass, plane per slot: {neighbour pixel, target * Jacobian}
-                              // of a similar neighbour, {kInvalid, 0} otherwise
+    uint2* nb_slot;           // corrected spatial pass, plane per slot: {neighbour pixel, merge weight
+                              // target * Jacobian * W * M} of a similar neighbour, {kInvalid, 0} otherwise
+    uint8_t* nb_m;            // and plane per slot: that neighbour's M
     uint32_t* counters;       // [b] paths entering bounce b, then the kCnt* words above
     uint32_t grid_persistent, grid_trace;
     uint32_t ray_bundle;      // camera-ray slot order in a 16 x 8 tile: 0 8x4 blocks, 1 16x2 rows, 2 4x8 blocks
