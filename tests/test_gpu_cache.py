@@ -64,9 +64,12 @@ def test_query_matches_oracle(n):
     assert _rel(gpu, ref) < OUT_TOL, _rel(gpu, ref)
 
 
-def test_gradients_match_oracle():
+# 16,384 uniform samples overflow the per-chunk shared-memory sums of the finer
+# aggregated levels (more distinct entries per 2,048-sample chunk than slots), so
+# both the summed and the direct paths of the table gradient are covered.
+@pytest.mark.parametrize("n", [1024, 16384])
+def test_gradients_match_oracle(n):
     r, oc = _pair(5)
-    n = 1024
     with r:
         _shared_state(r, oc, seed=1)
         s = _samples(np.random.default_rng(7), n)

@@ -99,6 +99,7 @@ xr_status cache_alloc(Context* c) {
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.loss, sizeof(float)), "cache alloc"))) return s;
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.adam, 4 * sizeof(float)), "cache alloc"))) return s;
     if ((s = cuda_check(c, cudaMalloc((void**)&cs.sel, sizeof(uint32_t)), "cache alloc"))) return s;
+    if ((s = cuda_check(c, cudaMalloc((void**)&cs.order_hist, 256 * 128 * sizeof(uint32_t)), "cache alloc"))) return s;
     cs.sel_target = 0;
     cs.allocated = true;
     return cache_init(c, cs.params.seed);
@@ -116,11 +117,17 @@ xr_status ensure_records(Context* c, uint32_t queries, uint32_t train) {
     }
     if (train > cs.train_cap) {
         cudaFree(cs.train);
+        cudaFree(cs.tiles);
+        cudaFree(cs.order);
         cudaFree(cs.nee);
         cs.train = nullptr;
+        cs.tiles = nullptr;
+        cs.order = nullptr;
         cs.nee = nullptr;
         cs.train_cap = 0;
         if ((s = cuda_check(c, cudaMalloc((void**)&cs.train, (size_t)train * 48), "cache training records"))) return s;
+        if ((s = cuda_check(c, cudaMalloc((void**)&cs.tiles, (size_t)train * 128), "cache training tiles"))) return s;
+        if ((s = cuda_check(c, cudaMalloc((void**)&cs.order, (size_t)train * 32), "cache training order"))) return s;
         if ((s = cuda_check(c, cudaMalloc((void**)&cs.nee, (size_t)train * 48), "cache next-event rays"))) return s;
         cs.train_cap = train;
     }
@@ -156,7 +163,8 @@ xr_status upload_samples(Context* c, const XrCacheSample* s, uint32_t n, uint32_
 void cache_free(Context* c) {
     CacheState& cs = c->cache;
     void* ptrs[] = {cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.grid, cs.grid_grad, cs.grid_m, cs.grid_v,
-                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.adam, cs.queries, cs.train, cs.nee, cs.sel};
+                    cs.table, cs.w_fwd, cs.w_bwd, cs.loss, cs.adam, cs.queries, cs.train, cs.tiles, cs.order,
+                    cs.order_hist, cs.nee, cs.sel};
     for (void* p : ptrs) cudaFree(p);
     cs = CacheState{};
 }

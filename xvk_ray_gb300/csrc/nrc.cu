@@ -10,14 +10,23 @@
 // mbarrier, and every thread reads its accumulator row back with tcgen05.ld,
 // applies ReLU and writes the next layer's activations.
 //
-// Training (forward + backward fused per tile) keeps every layer's activations
-// in shared memory and accumulates the weight gradients of all tiles a CTA
-// processes in tensor memory (dW_l = dZ_l^T H_l, M = 128 with the rows beyond
-// the layer's outputs zero); the hash-table gradients are scattered with
-// vector atomics.  Every wait on the tensor core is bounded (1 s of wall time);
+// Training runs as three launches over the same 128-sample tiles:
+//  * k_cache_encode (many warps per SM): the hash-grid gathers; writes each
+//    tile's bfloat16 inputs in the shared-memory image layout (16 KB a tile);
+//  * k_cache_train (one CTA per SM): copies a tile's inputs, forward + backward
+//    fused, every layer's activations kept in shared memory, the weight
+//    gradients of all its tiles accumulated in tensor memory (dW_l = dZ_l^T H_l,
+//    M = 128 with the rows beyond the layer's outputs zero); writes the input
+//    gradient of the 32 encoding features over the tile's inputs;
+//  * k_cache_scatter (many warps per SM): the hash-table gradients through the
+//    trilinear weights, with vector atomics.
+// The latency of the gathers and the atomics is hidden by occupancy in the two
+// outer launches instead of stalling the four warps that drive the tensor core.
+// Every wait on the tensor core is bounded (1 s of wall time);
 // on expiry the kernel sets XR_DEVFLAG_MMA_TIMEOUT, stops and frees its tensor
 // memory.
 #include <cmath>
+#include <utility>
 
 #include "nrc.cuh"
 #include "umma.cuh"
@@ -204,23 +213,280 @@ __global__ void __launch_bounds__(128) k_cache_infer(const uint4* __restrict__ r
 }
 
 // ---------------------------------------------------------------------------
-// training: forward + backward of every tile, gradients of the mean relative
-// L2 loss over n = min(count, cap) rounded down to a multiple of 128 samples.
+// training: gradients of the mean relative L2 loss over n = min(count, cap)
+// rounded down to a multiple of 128 samples.  `tiles` holds 16 KB per tile:
+// the inputs [128][64] bf16 in the K-major image layout (k_cache_encode), then
+// the input gradients [32][128] fp32 of the encoding features, feature-major
+// (k_cache_train), read by k_cache_scatter.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t train_samples(const uint32_t* count_ptr, uint32_t count_host, uint32_t cap) {
+    uint32_t count = count_ptr ? *(volatile const uint32_t*)count_ptr : count_host;
+    if (count > cap) count = cap;
+    return count & ~(kTile - 1u);
+}
+
+// Sample j of the tiles is record perm[j] (the spatial order below); its unit
+// position goes to upos[j] for k_cache_scatter.
+__global__ void __launch_bounds__(256) k_cache_encode(const uint4* __restrict__ rec, const uint32_t* __restrict__ perm,
+                                                      const uint32_t* count_ptr, uint32_t count_host, uint32_t cap,
+                                                      Bounds bnd, const __half2* __restrict__ table,
+                                                      uint8_t* __restrict__ tiles, float4* __restrict__ upos) {
+    const uint32_t n = train_samples(count_ptr, count_host, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float v[kIn];
+        float4 ra;
+        uint4 rb;
+        inputs_of(bnd, table, rec, 3u, perm[i], ra, rb, v);
+        const float3 p = unit_pos(bnd, xyz(ra));
+        upos[i] = make_float4(p.x, p.y, p.z, 0.0f);
+        store_row<kIn>(tiles + (size_t)(i / kTile) * kActBytes, i % kTile, v);
+    }
+}
+
+// ---- spatial order of the training samples ----
+// The samples lie on the scene's surfaces, so at the coarse levels a few table
+// entries take most of the gradient updates (1080p, 65,536 samples: 36K updates
+// of one entry at level 0, 4K at level 8, 180 at level 15), and atomics on one
+// address serialise in L2.  The samples are therefore taken in the order of the
+// 24-bit Morton code of their unit position (stable LSD radix sort, 3 passes of
+// 8 bits, kOrderBlocks blocks sharing the device-side sample count): the 32
+// samples of a warp are then neighbours, and k_cache_scatter sums runs of equal
+// table entries across the warp before one atomic per run (the hottest entry
+// takes ~30x fewer atomics).  The training loss and gradients are sums over the
+// samples, so the order changes their rounding only.
+constexpr uint32_t kOrderBlocks = 128, kOrderThreads = 256;
+
+__device__ __forceinline__ void order_span(uint32_t n, uint32_t b, uint32_t& beg, uint32_t& end) {
+    uint32_t chunk = (n + kOrderBlocks - 1u) / kOrderBlocks;
+    chunk = (chunk + kOrderThreads - 1u) / kOrderThreads * kOrderThreads;
+    beg = b * chunk < n ? b * chunk : n;
+    end = beg + chunk < n ? beg + chunk : n;
+}
+
+__device__ __forceinline__ uint32_t spread8(uint32_t x) {   // bit j of x -> bit 3 j
+    x &= 0xFFu;
+    x = (x | (x << 8)) & 0x0000F00Fu;
+    x = (x | (x << 4)) & 0x000C30C3u;
+    x = (x | (x << 2)) & 0x00249249u;
+    return x;
+}
+
+// Adds the digits of one row of 256 samples (d >= 256: past the end) to the
+// block's counts, one shared-memory atomic per distinct digit of a warp.
+__device__ __forceinline__ void count_digit(uint32_t* h, uint32_t d) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    if (d < 256u && (peers & ((1u << lane) - 1u)) == 0u) atomicAdd(&h[d], (uint32_t)__popc(peers));
+}
+
+// Keys (24-bit Morton code of the unit position) and the counts of their low digit.
+__global__ void __launch_bounds__(kOrderThreads) k_cache_order_keys(const uint4* __restrict__ rec,
+                                                                    const uint32_t* count_ptr, uint32_t count_host,
+                                                                    uint32_t cap, Bounds bnd,
+                                                                    uint32_t* __restrict__ keys,
+                                                                    uint32_t* __restrict__ vals,
+                                                                    uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t beg, end;
+    order_span(train_samples(count_ptr, count_host, cap), blockIdx.x, beg, end);
+    for (uint32_t t = beg; t < end; t += kOrderThreads) {   // spans are whole multiples of the block
+        const uint32_t i = t + threadIdx.x;
+        uint32_t d = 256u + (threadIdx.x & 31u);
+        if (i < end) {
+            const uint4 a = rec[(size_t)i * 3];
+            const float3 p = unit_pos(bnd, f3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z)));
+            const uint32_t qx = min((uint32_t)(p.x * 256.0f), 255u), qy = min((uint32_t)(p.y * 256.0f), 255u);
+            const uint32_t qz = min((uint32_t)(p.z * 256.0f), 255u);
+            const uint32_t key = spread8(qx) | (spread8(qy) << 1) | (spread8(qz) << 2);
+            keys[i] = key;
+            vals[i] = i;
+            d = key & 0xFFu;
+        }
+        count_digit(h, d);
+    }
+    __syncthreads();
+    hist[blockIdx.x * 256u + threadIdx.x] = h[threadIdx.x];
+}
+
+// per-block digit counts, block-major: hist[b * 256 + d]
+__global__ void __launch_bounds__(kOrderThreads) k_cache_order_hist(const uint32_t* __restrict__ keys,
+                                                                    const uint32_t* count_ptr, uint32_t count_host,
+                                                                    uint32_t cap, uint32_t shift,
+                                                                    uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t beg, end;
+    order_span(train_samples(count_ptr, count_host, cap), blockIdx.x, beg, end);
+    for (uint32_t t = beg; t < end; t += kOrderThreads) {
+        const uint32_t i = t + threadIdx.x;
+        count_digit(h, i < end ? (keys[i] >> shift) & 0xFFu : 256u + (threadIdx.x & 31u));
+    }
+    __syncthreads();
+    hist[blockIdx.x * 256u + threadIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter.  Block b places digit d after every sample of a smaller digit
+// and after the samples of digit d in blocks before b: thread d sums the counts
+// of all blocks (read coalesced, from L2), the digit totals are scanned across
+// the block, and a sample's rank among the block's earlier samples of its digit
+// comes from the warps' match masks.
+__global__ void __launch_bounds__(kOrderThreads) k_cache_order_scatter(const uint32_t* __restrict__ kin,
+                                                                       const uint32_t* __restrict__ vin,
+                                                                       uint32_t* __restrict__ kout,
+                                                                       uint32_t* __restrict__ vout,
+                                                                       const uint32_t* count_ptr, uint32_t count_host,
+                                                                       uint32_t cap, uint32_t shift,
+                                                                       const uint32_t* __restrict__ hist) {
+    constexpr uint32_t kWarps = kOrderThreads / 32u;
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wcnt[kWarps][256];
+    __shared__ uint32_t wtot[kWarps];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    {
+        uint32_t total = 0, before = 0;
+#pragma unroll 16
+        for (uint32_t b = 0; b < kOrderBlocks; ++b) {
+            const uint32_t c = hist[b * 256u + threadIdx.x];
+            total += c;
+            before += b < blockIdx.x ? c : 0u;
+        }
+        uint32_t incl = total;   // exclusive scan of the digit totals: warps, then across the 8 warps
+#pragma unroll
+        for (uint32_t d = 1; d < 32u; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= d) incl += t;
+        }
+        if (lane == 31u) wtot[warp] = incl;
+        __syncthreads();
+        uint32_t off = 0;
+        for (uint32_t w = 0; w < warp; ++w) off += wtot[w];
+        base[threadIdx.x] = off + incl - total + before;
+    }
+    uint32_t beg, end;
+    order_span(train_samples(count_ptr, count_host, cap), blockIdx.x, beg, end);
+    for (uint32_t t = beg; t < end; t += kOrderThreads) {
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; ++w) wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        const uint32_t i = t + threadIdx.x;
+        const bool valid = i < end;
+        const uint32_t key = valid ? kin[i] : 0u, val = valid ? vin[i] : 0u;
+        const uint32_t d = valid ? (key >> shift) & 0xFFu : 256u + lane;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0u) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t before = 0;
+            for (uint32_t w = 0; w < warp; ++w) before += wcnt[w][d];
+            const uint32_t pos = base[d] + before + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        uint32_t tot = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; ++w) tot += wcnt[w][threadIdx.x];
+        base[threadIdx.x] += tot;
+        __syncthreads();
+    }
+}
+
+// *p += (x, y) as one reduction without a return value (red): unlike atomicAdd
+// on a float2, whose result the thread has to wait for, the thread goes on at once.
+__device__ __forceinline__ void red_add2(float2* p, float x, float y) {
+    asm volatile("red.relaxed.gpu.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(x), "f"(y) : "memory");
+}
+
+// p[0] += (x0, y0), p[1] += (x1, y1): one 16-byte reduction; p 16-byte aligned.
+__device__ __forceinline__ void red_add4(float2* p, float x0, float y0, float x1, float y1) {
+    asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x0), "f"(y0), "f"(x1),
+                 "f"(y1)
+                 : "memory");
+}
+
+// Table gradients, one thread per (sample, level): the 32 threads of a warp take
+// 32 neighbouring samples (spatial order) of one tile at one level, so the
+// gradient loads are coalesced and samples in the same cell come in runs.  The
+// samples of a run share all 8 table entries; each entry's updates are summed
+// across the run (segmented scan, steps up to the warp's longest run) and added
+// by the run's last thread.  A warp without runs (most warps of the fine levels)
+// adds directly.
+__global__ void __launch_bounds__(256) k_cache_scatter(const float4* __restrict__ upos, const uint32_t* count_ptr,
+                                                       uint32_t count_host, uint32_t cap,
+                                                       const float* __restrict__ tiles, float2* grid_grad,
+                                                       const uint32_t* err) {
+    if (*(volatile const uint32_t*)err & (uint32_t)XR_DEVFLAG_MMA_TIMEOUT) return;   // gradients incomplete
+    const uint32_t n = train_samples(count_ptr, count_host, cap);
+    const uint32_t units = n * (uint32_t)kLevels, lane = threadIdx.x & 31u;
+    // units is a multiple of 32 and so is the stride: every warp runs the loop whole
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < units; u += gridDim.x * blockDim.x) {
+        const uint32_t lv = (u / kTile) % kLevels, s = u % kTile;
+        const uint32_t i = u / (kTile * kLevels) * kTile + s;
+        const float4 q = upos[i];
+        const float* g = tiles + (size_t)(i / kTile) * (kActBytes / 4) + 2u * lv * kTile + s;
+        const float g0 = g[0], g1 = g[kTile];
+        const LevelCell cell = level_cell((int)lv, f3(q.x, q.y, q.z));
+        const uint64_t key = (uint64_t)cell.i0[0] | ((uint64_t)cell.i0[1] << 21) | ((uint64_t)cell.i0[2] << 42);
+        const uint64_t prev = __shfl_up_sync(0xFFFFFFFFu, key, 1);
+        const uint32_t heads = __ballot_sync(0xFFFFFFFFu, lane == 0u || prev != key);
+        const uint32_t start = 31u - (uint32_t)__clz(heads & (0xFFFFFFFFu >> (31u - lane)));
+        const uint32_t longest = __reduce_max_sync(0xFFFFFFFFu, lane - start + 1u);
+        const bool last = lane == 31u || ((heads >> (lane + 1u)) & 1u);
+        LevelCorners c;
+        cell_corners((int)lv, cell, c);
+        float2* glv = grid_grad + (size_t)lv * kT;
+        float v[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            v[2 * k] = c.w[k] * g0;
+            v[2 * k + 1] = c.w[k] * g1;
+        }
+        if (longest > 1u) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                for (uint32_t d = 1; d < longest; d <<= 1) {
+                    const float t = __shfl_up_sync(0xFFFFFFFFu, v[j], d);
+                    if (lane >= start + d) v[j] += t;
+                }
+            }
+        }
+        if (last) {
+            // corners k and k + 1 differ in x only; where their entries are the two halves of one
+            // 16-byte pair (always for an even x in a hashed level), one reduction adds both
+#pragma unroll
+            for (int k = 0; k < 8; k += 2) {
+                const uint32_t a = c.idx[k], b = c.idx[k + 1];
+                if (b == (a ^ 1u)) {
+                    if (a & 1u) red_add4(glv + b, v[2 * k + 2], v[2 * k + 3], v[2 * k], v[2 * k + 1]);
+                    else red_add4(glv + a, v[2 * k], v[2 * k + 1], v[2 * k + 2], v[2 * k + 3]);
+                } else {
+                    red_add2(glv + a, v[2 * k], v[2 * k + 1]);
+                    red_add2(glv + b, v[2 * k + 2], v[2 * k + 3]);
+                }
+            }
+        }
+    }
+}
+
+// Forward + backward of every tile.
 // Shared memory (217,088 B): forward image, backward image, H_0..H_4, dZ,
 // dZ^T [128][128] (rows beyond the layer's outputs zero), H^T [64][128].
 // Tensor memory (512 columns): 0..63 forward / dX accumulator, 64 + 64 l: dW_l.
-// ---------------------------------------------------------------------------
 constexpr uint32_t kOffWf = 0, kOffWb = kImageBytes, kOffX = 2 * kImageBytes;
 constexpr uint32_t kOffDZ = kOffX + 5 * kActBytes, kOffDZT = kOffDZ + kActBytes, kOffHT = kOffDZT + 2 * kActBytes;
 constexpr uint32_t kTrainSmem = kOffHT + kActBytes;
 static_assert(kTrainSmem == 217088, "training shared memory layout");
 
-__global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict__ rec, const uint32_t* count_ptr,
-                                                        uint32_t count_host, uint32_t cap, Bounds bnd,
-                                                        const __half2* __restrict__ table,
+__global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict__ rec, const uint32_t* __restrict__ perm,
+                                                        const uint32_t* count_ptr,
+                                                        uint32_t count_host, uint32_t cap, uint8_t* tiles,
                                                         const uint8_t* __restrict__ w_fwd,
                                                         const uint8_t* __restrict__ w_bwd, float* mlp_grad,
-                                                        float2* grid_grad, float* loss_acc, uint32_t* err) {
+                                                        float* loss_acc, uint32_t* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* sWf = smem + kOffWf;
     uint8_t* sWb = smem + kOffWb;
@@ -231,9 +497,7 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict_
     __shared__ uint64_t bar;
     __shared__ uint32_t tslot;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    uint32_t count = count_ptr ? *(volatile const uint32_t*)count_ptr : count_host;
-    if (count > cap) count = cap;
-    const uint32_t n = count & ~(kTile - 1u);
+    const uint32_t n = train_samples(count_ptr, count_host, cap);
     const uint32_t ntiles = n / kTile;
     if (blockIdx.x >= ntiles) return;
     const float inv_count = 1.0f / (float)(3u * n);
@@ -257,12 +521,19 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict_
 
     for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const uint32_t i = tile * kTile + tid;
+        uint8_t* tile_mem = tiles + (size_t)tile * kActBytes;
+        {
+            // the tile's inputs, 8 x 16 B per thread; plain loads: this launch rewrites the tile below
+            uint4 q[kActBytes / 16 / kTile];
+#pragma unroll
+            for (uint32_t k = 0; k < kActBytes / 16 / kTile; ++k)
+                q[k] = reinterpret_cast<const uint4*>(tile_mem)[k * kTile + tid];
+#pragma unroll
+            for (uint32_t k = 0; k < kActBytes / 16 / kTile; ++k)
+                reinterpret_cast<uint4*>(sX)[k * kTile + tid] = q[k];
+        }
+        const uint4 rt = rec[(size_t)perm[i] * 3 + 2];
         float v[kIn];
-        float4 ra;
-        uint4 rb;
-        inputs_of(bnd, table, rec, 3u, i, ra, rb, v);
-        const uint4 rt = rec[(size_t)i * 3 + 2];
-        store_row<kIn>(sX, tid, v);
         // ---- forward, keeping H_0..H_4 ----
         float y[16];
         for (int l = 0; l <= kHidden && ok; ++l) {
@@ -330,17 +601,11 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict_
                 for (int j = 0; j < kWidth; ++j) dz[j] = umma::bf16_value(umma::bf16_bits(dz[j]));
                 store_col128<64>(sDZT, tid, dz);
             } else {
-                // hash-table gradients through the trilinear interpolation
-                const float3 p = unit_pos(bnd, xyz(ra));
-#pragma unroll 1
-                for (int lv = 0; lv < kLevels; ++lv) {
-                    LevelCorners c;
-                    level_corners(lv, p, c);
-                    const float g0 = dx[2 * lv], g1 = dx[2 * lv + 1];
+                // gradients of the 32 encoding features, feature-major over the tile's inputs (every
+                // thread's loads of the tile completed before the first barrier of this tile)
+                float* g = reinterpret_cast<float*>(tile_mem) + tid;
 #pragma unroll
-                    for (int k = 0; k < 8; ++k)
-                        atomicAdd(grid_grad + (size_t)lv * kT + c.idx[k], make_float2(c.w[k] * g0, c.w[k] * g1));
-                }
+                for (int j = 0; j < 2 * kLevels; ++j) g[j * kTile] = dx[j];
             }
         }
         first = false;
@@ -587,10 +852,32 @@ void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_
         if (tiles < grid) grid = tiles;
     }
     cudaMemsetAsync(cs.loss, 0, sizeof(float), st);
-    if (grid)
-        k_cache_train<<<grid, 128, kTrainSmem, st>>>(rec, count_ptr, count_host, cap, bounds_of(cs), cs.table, cs.w_fwd,
-                                                     cs.w_bwd, cs.mlp_grad, reinterpret_cast<float2*>(cs.grid_grad),
-                                                     cs.loss, err);
+    if (grid) {
+        const nrc::Bounds bnd = bounds_of(cs);
+        const uint32_t wide = (uint32_t)sm_count * 8u;   // 8 x 256 threads per SM, grid-stride
+        uint32_t* k0 = cs.order;
+        uint32_t* v0 = cs.order + cs.train_cap;
+        uint32_t* k1 = cs.order + 2 * (size_t)cs.train_cap;
+        uint32_t* v1 = cs.order + 3 * (size_t)cs.train_cap;
+        k_cache_order_keys<<<kOrderBlocks, kOrderThreads, 0, st>>>(rec, count_ptr, count_host, cap, bnd, k0, v0,
+                                                                   cs.order_hist);
+        for (uint32_t shift = 0; shift < 24u; shift += 8u) {
+            if (shift)
+                k_cache_order_hist<<<kOrderBlocks, kOrderThreads, 0, st>>>(k0, count_ptr, count_host, cap, shift,
+                                                                           cs.order_hist);
+            k_cache_order_scatter<<<kOrderBlocks, kOrderThreads, 0, st>>>(k0, v0, k1, v1, count_ptr, count_host, cap,
+                                                                          shift, cs.order_hist);
+            std::swap(k0, k1);
+            std::swap(v0, v1);
+        }
+        const uint32_t* perm = v0;   // the last pass's output
+        float4* upos = reinterpret_cast<float4*>(cs.order + 4 * (size_t)cs.train_cap);
+        k_cache_encode<<<wide, 256, 0, st>>>(rec, perm, count_ptr, count_host, cap, bnd, cs.table, cs.tiles, upos);
+        k_cache_train<<<grid, 128, kTrainSmem, st>>>(rec, perm, count_ptr, count_host, cap, cs.tiles, cs.w_fwd,
+                                                     cs.w_bwd, cs.mlp_grad, cs.loss, err);
+        k_cache_scatter<<<wide, 256, 0, st>>>(upos, count_ptr, count_host, cap, reinterpret_cast<const float*>(cs.tiles),
+                                              reinterpret_cast<float2*>(cs.grid_grad), err);
+    }
     if (apply) launch_cache_adam(cs, st);
 }
 

@@ -75,31 +75,47 @@ struct LevelCorners {
     float w[8];
 };
 
-__device__ __forceinline__ void level_corners(int l, float3 p, LevelCorners& c) {
+// The cell of level l that holds the unit position p: its lowest corner and the
+// position's fractions inside it.
+struct LevelCell {
+    uint32_t i0[3];
+    float f[3];
+};
+
+__device__ __forceinline__ LevelCell level_cell(int l, float3 p) {
     const uint32_t res = kRes[l];
     const float fr = (float)res;
     const float s[3] = {p.x * fr, p.y * fr, p.z * fr};
-    uint32_t i0[3];
-    float f[3];
+    LevelCell c;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         int ii = (int)floorf(s[a]);
         if (ii > (int)res - 1) ii = (int)res - 1;
         if (ii < 0) ii = 0;
-        i0[a] = (uint32_t)ii;
-        f[a] = s[a] - (float)ii;
+        c.i0[a] = (uint32_t)ii;
+        c.f[a] = s[a] - (float)ii;
     }
+    return c;
+}
+
+// The 8 table entries of a cell and their trilinear weights.
+__device__ __forceinline__ void cell_corners(int l, const LevelCell& cell, LevelCorners& c) {
+    const uint32_t res = kRes[l];
     const bool dense = (uint64_t)(res + 1u) * (res + 1u) * (res + 1u) <= (uint64_t)kT;
     const uint32_t st = res + 1u;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        const uint32_t cx = i0[0] + (k & 1), cy = i0[1] + ((k >> 1) & 1), cz = i0[2] + ((k >> 2) & 1);
-        const float wx = (k & 1) ? f[0] : 1.0f - f[0];
-        const float wy = (k & 2) ? f[1] : 1.0f - f[1];
-        const float wz = (k & 4) ? f[2] : 1.0f - f[2];
+        const uint32_t cx = cell.i0[0] + (k & 1), cy = cell.i0[1] + ((k >> 1) & 1), cz = cell.i0[2] + ((k >> 2) & 1);
+        const float wx = (k & 1) ? cell.f[0] : 1.0f - cell.f[0];
+        const float wy = (k & 2) ? cell.f[1] : 1.0f - cell.f[1];
+        const float wz = (k & 4) ? cell.f[2] : 1.0f - cell.f[2];
         c.w[k] = (wx * wy) * wz;
         c.idx[k] = dense ? cx + st * (cy + st * cz) : ((cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (kT - 1u);
     }
+}
+
+__device__ __forceinline__ void level_corners(int l, float3 p, LevelCorners& c) {
+    cell_corners(l, level_cell(l, p), c);
 }
 
 __device__ __forceinline__ float3 unit_pos(const Bounds& b, float3 x) {

@@ -201,6 +201,10 @@ struct CacheState {
     float* adam = nullptr;           // device Adam state {beta1^t, beta2^t, 1 - beta1^t, 1 - beta2^t}
     uint4* queries = nullptr;        // query records (capacity query_cap)
     uint4* train = nullptr;          // training records (capacity train_cap)
+    uint8_t* tiles = nullptr;        // training tiles: inputs, then input gradients (128 B a record)
+    uint32_t* order = nullptr;       // spatial order of the records (8 x train_cap words): keys, values, twice;
+                                     // then the unit positions in that order (float4)
+    uint32_t* order_hist = nullptr;  // radix-sort digit counts (128 x 256 words)
     float4* nee = nullptr;           // next-event rays of one bounce (capacity train_cap)
     uint32_t query_cap = 0, train_cap = 0;
     uint32_t* sel = nullptr;         // device word: training pixels of the next frame (adaptive)
