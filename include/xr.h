@@ -8,8 +8,9 @@
  * failure is available from xr_last_error().
  *
  * Threading: one context per host thread.  All work of a context is ordered on
- * its own CUDA stream; xr_render_frame() is asynchronous, xr_read_output(),
- * xr_read_buffer() and xr_sync() synchronise.
+ * its own CUDA stream; xr_render_frame() and xr_read_output_async() are
+ * asynchronous, xr_read_output(), xr_wait_output(), xr_read_buffer() and
+ * xr_sync() synchronise.
  */
 #ifndef XR_H
 #define XR_H
@@ -182,7 +183,20 @@ enum {
     XR_OUT_PT = 2      /* width*height float4: plain 1-spp path-traced radiance (write_pt) */
 };
 xr_status xr_read_output(XrContext* ctx, uint32_t which, void* host, size_t bytes);
-/* Device pointer of an output image (valid until the next xr_set_params/xr_destroy). */
+/* Frames in flight (the reference's per-frame fences and asynchronous present,
+   src/Vulkan/ApplicationRZ.cpp:125-195): enqueues the copy of the last rendered
+   frame's RGBA8 image (width*height*4 bytes) into `host` on the context's copy
+   stream and returns at once; the next frames render while it runs.  The RGBA8
+   image alternates between two device buffers by frame parity, and a frame that
+   would overwrite a buffer still being read waits for that read on the device.
+   `host` must stay valid, and should be page-locked for the copy to overlap,
+   until xr_wait_output() returns.  Device error flags are reported by xr_sync(). */
+xr_status xr_read_output_async(XrContext* ctx, void* host, size_t bytes);
+/* Blocks until the last xr_read_output_async() copy has landed in host memory. */
+xr_status xr_wait_output(XrContext* ctx);
+/* Device pointer of an output image as the last frame wrote it (valid until the
+   next xr_set_params/xr_destroy; the RGBA8 image's buffer alternates with the
+   frame parity). */
 xr_status xr_output_device_ptr(XrContext* ctx, uint32_t which, void** device_ptr);
 xr_status xr_sync(XrContext* ctx);
 xr_status xr_get_stats(XrContext* ctx, XrStats* stats);

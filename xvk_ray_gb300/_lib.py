@@ -160,6 +160,8 @@ _SIGS = {
     "xr_read_output": (_i32, [_P, _u32, _P, C.c_size_t]),
     "xr_render_reference": (_i32, [_P, C.POINTER(XrUniformBufferObject), _u32, _u32, _P]),
     "xr_output_device_ptr": (_i32, [_P, _u32, C.POINTER(_P)]),
+    "xr_read_output_async": (_i32, [_P, _P, C.c_size_t]),
+    "xr_wait_output": (_i32, [_P]),
     "xr_sync": (_i32, [_P]),
     "xr_get_stats": (_i32, [_P, C.POINTER(XrStats)]),
     "xr_read_buffer": (_i32, [_P, _u32, _P, C.c_size_t, C.POINTER(C.c_size_t)]),

@@ -128,14 +128,16 @@ class Renderer:
         self.ctx = h
         self.width, self.height = width, height
         self.cache = Cache(self)
+        self._pending_read = None   # the array an asynchronous image read is copying into
 
     def _c(self, status: int) -> None:
         L.check(status, self.ctx)
 
     def close(self) -> None:
         if self.ctx:
-            self._lib.xr_destroy(self.ctx)
+            self._lib.xr_destroy(self.ctx)   # finishes a pending image read first
             self.ctx = None
+        self._pending_read = None
 
     def __del__(self):
         try:
@@ -260,6 +262,20 @@ class Renderer:
         out = np.empty((self.width * self.height, 3), np.float64)
         self._c(self._lib.xr_render_reference(self.ctx, C.byref(ubo), frame0, spp, _ptr(out)))
         return out
+
+    def read_output_async(self, out: np.ndarray) -> None:
+        """Starts copying the last frame's RGBA8 image into `out` (width*height*4
+        bytes, preferably page-locked: PinnedBuffer.array) and returns at once; the
+        image is there after wait_output().  `out` is kept alive until then."""
+        if out.nbytes < self.width * self.height * 4 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("read_output_async: need a contiguous array of width*height*4 bytes")
+        self._c(self._lib.xr_read_output_async(self.ctx, _ptr(out), out.nbytes))
+        self._pending_read = out
+
+    def wait_output(self) -> None:
+        """Blocks until the last read_output_async() copy has landed."""
+        self._c(self._lib.xr_wait_output(self.ctx))
+        self._pending_read = None
 
     def output_device_ptr(self, which: int = L.XR_OUT_LDR8) -> int:
         p = C.c_void_p()

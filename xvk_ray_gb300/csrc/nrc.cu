@@ -692,18 +692,29 @@ __global__ void k_cache_adam_mlp(float* w, float* g, float* m, float* v, uint8_t
 }
 
 // Sparse update: a table value changes only where its gradient is non-zero.
+// A thread takes 4 entries (two 16-byte gradient loads: the pass over the whole
+// gradient is a stream; a few percent of the entries are non-zero).
+constexpr uint32_t kAdamGridPer = 4;
+
 __global__ void k_cache_adam_grid(float2* w, float2* g, float2* m, float2* v, __half2* table, AdamArgs a) {
-    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= kGridParams / 2) return;
-    const float2 gr = g[e];
-    if (gr.x == 0.0f && gr.y == 0.0f) return;
-    float2 wi = w[e], mi = m[e], vi = v[e];
-    const float bc1 = a.state[2], bc2 = a.state[3];
-    if (gr.x != 0.0f) adam_step(wi.x, mi.x, vi.x, gr.x, a, bc1, bc2);
-    if (gr.y != 0.0f) adam_step(wi.y, mi.y, vi.y, gr.y, a, bc1, bc2);
-    w[e] = wi; m[e] = mi; v[e] = vi;
-    g[e] = make_float2(0.0f, 0.0f);
-    table[e] = __floats2half2_rn(wi.x, wi.y);
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= kGridParams / 2 / kAdamGridPer) return;
+    const float4 q0 = reinterpret_cast<const float4*>(g)[2 * t], q1 = reinterpret_cast<const float4*>(g)[2 * t + 1];
+    const float2 grs[kAdamGridPer] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y),
+                                      make_float2(q1.z, q1.w)};
+#pragma unroll
+    for (uint32_t j = 0; j < kAdamGridPer; ++j) {
+        const float2 gr = grs[j];
+        if (gr.x == 0.0f && gr.y == 0.0f) continue;
+        const size_t e = t * kAdamGridPer + j;
+        float2 wi = w[e], mi = m[e], vi = v[e];
+        const float bc1 = a.state[2], bc2 = a.state[3];
+        if (gr.x != 0.0f) adam_step(wi.x, mi.x, vi.x, gr.x, a, bc1, bc2);
+        if (gr.y != 0.0f) adam_step(wi.y, mi.y, vi.y, gr.y, a, bc1, bc2);
+        w[e] = wi; m[e] = mi; v[e] = vi;
+        g[e] = make_float2(0.0f, 0.0f);
+        table[e] = __floats2half2_rn(wi.x, wi.y);
+    }
 }
 
 __global__ void k_cache_init_grid(float2* w, __half2* table, uint32_t seed) {
@@ -899,7 +910,7 @@ void launch_cache_adam(CacheState& cs, cudaStream_t st) {
     k_cache_adam_advance<<<1, 32, 0, st>>>(cs.adam, cs.params.beta1, cs.params.beta2);
     k_cache_adam_mlp<<<(kMlpParams + 255) / 256, 256, 0, st>>>(cs.mlp, cs.mlp_grad, cs.mlp_m, cs.mlp_v, cs.w_fwd,
                                                                 cs.w_bwd, a, 1);
-    const uint32_t n2 = (uint32_t)(kGridParams / 2);
+    const uint32_t n2 = (uint32_t)(kGridParams / 2 / kAdamGridPer);
     k_cache_adam_grid<<<(n2 + 255) / 256, 256, 0, st>>>(
         reinterpret_cast<float2*>(cs.grid), reinterpret_cast<float2*>(cs.grid_grad),
         reinterpret_cast<float2*>(cs.grid_m), reinterpret_cast<float2*>(cs.grid_v), cs.table, a);

@@ -62,6 +62,10 @@ uint32_t trace_grid(int sm_count, bool instances);
 namespace {
 
 void free_pixels(Context* c) {
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);   // reads still in flight from the images
+    c->ldr[0] = c->ldr[1] = nullptr;
+    c->ldr_copy_pending[0] = c->ldr_copy_pending[1] = false;
+    c->ldr_last_copy = -1;
     if (c->pix_mem) cudaFree(c->pix_mem);
     c->pix_mem = nullptr;
     c->pix_bytes = 0;
@@ -125,7 +129,8 @@ xr_status alloc_pixels(Context* c) {
     }
     add((void**)&fa.hits, N * 16);
     add((void**)&fa.hit_inst, N * 4);
-    add((void**)&fa.out_ldr, N * 4);
+    add((void**)&c->ldr[0], N * 4);   // LDR image of even / odd frames
+    add((void**)&c->ldr[1], N * 4);
     if (P.write_hdr) add((void**)&fa.out_hdr, N * 16);
     for (int i = 0; i < 2; i++)
         for (int k = 0; k < 3; k++) add((void**)&c->q[i][k], N * 16);
@@ -138,6 +143,7 @@ xr_status alloc_pixels(Context* c) {
     if (s) { cudaFree(mem); return s; }
     size_t off = 0;
     for (auto& it : items) { *it.dst = (char*)mem + off; off += align256(it.bytes); }
+    fa.out_ldr = c->ldr[0];
     c->pix_mem = mem;
     c->pix_bytes = total;
     if (!compat)
@@ -175,6 +181,14 @@ void set_frame_pointers(Context* c, uint32_t parity) {
     FrameArgs& fa = c->fa;
     const XrParams& P = c->params;
     fa.parity = parity;
+    if (c->ldr[parity]) {
+        fa.out_ldr = c->ldr[parity];
+        // work that writes this image waits until an asynchronous read of it has finished
+        if (c->ldr_copy_pending[parity]) {
+            cudaStreamWaitEvent(c->stream, c->ldr_copied[parity], 0);
+            c->ldr_copy_pending[parity] = false;
+        }
+    }
     fa.compat = P.compat_reference; fa.temporal_on = P.temporal_on; fa.spatial_on = P.spatial_on;
     fa.visibility = P.visibility; fa.write_pt = P.write_pt; fa.seed = P.seed;
     fa.m_cap_t = P.m_cap_temporal; fa.m_cap_s = P.m_cap_spatial; fa.n_nb = P.n_neighbours; fa.radius = P.radius_px;
@@ -312,6 +326,11 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     if (prop.major < 10) { s = fail(c, XR_ERR_UNSUPPORTED, "create: this library is built for sm_103a (GB300)"); goto bad; }
     c->sm_count = prop.multiProcessorCount;
     if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) goto bad;
+    if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "copy stream"))) goto bad;
+    for (int i = 0; i < 2; i++) {
+        if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->ldr_ready[i], cudaEventDisableTiming), "event"))) goto bad;
+        if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->ldr_copied[i], cudaEventDisableTiming), "event"))) goto bad;
+    }
     {   // the context's own pool: freed scratch stays cached for the next build instead of going back to the driver
         cudaMemPoolProps pp{};
         pp.allocType = cudaMemAllocationTypePinned;
@@ -367,6 +386,11 @@ void xr_destroy(XrContext* c) {
     for (int i = 0; i < 8; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
     for (int i = 0; i < 2; i++) if (c->refit_ev[i]) cudaEventDestroy(c->refit_ev[i]);
+    for (int i = 0; i < 2; i++) {
+        if (c->ldr_ready[i]) cudaEventDestroy(c->ldr_ready[i]);
+        if (c->ldr_copied[i]) cudaEventDestroy(c->ldr_copied[i]);
+    }
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamSynchronize(c->stream);   // pool frees queued by free_instances
     if (c->pool) cudaMemPoolDestroy(c->pool);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -894,6 +918,7 @@ xr_status xr_sync(XrContext* c) {
     DeviceGuard g(c->device);
     xr_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
     if (s) return s;
+    if (c->copy_stream && (s = cuda_check(c, cudaStreamSynchronize(c->copy_stream), "sync (image reads)"))) return s;
     return check_flags(c);
 }
 
@@ -917,6 +942,31 @@ xr_status xr_read_output(XrContext* c, uint32_t which, void* host, size_t bytes)
     xr_status s = cuda_check(c, cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, c->stream), "read_output copy");
     if (s) return s;
     return xr_sync(c);
+}
+
+xr_status xr_read_output_async(XrContext* c, void* host, size_t bytes) {
+    if (!c || !host) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_output_async: null argument");
+    const size_t need = (size_t)c->N * 4;
+    if (bytes < need) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_output_async: host buffer too small");
+    if (!c->frames) return fail(c, XR_ERR_STATE, "read_output_async: no frame rendered yet");
+    DeviceGuard g(c->device);
+    const uint32_t p = c->fa.parity;   // the buffer the last frame wrote
+    xr_status s = cuda_check(c, cudaEventRecord(c->ldr_ready[p], c->stream), "read_output_async event");
+    if (!s) s = cuda_check(c, cudaStreamWaitEvent(c->copy_stream, c->ldr_ready[p], 0), "read_output_async wait");
+    if (!s) s = cuda_check(c, cudaMemcpyAsync(host, c->ldr[p], need, cudaMemcpyDeviceToHost, c->copy_stream),
+                           "read_output_async copy");
+    if (!s) s = cuda_check(c, cudaEventRecord(c->ldr_copied[p], c->copy_stream), "read_output_async event");
+    if (s) return s;
+    c->ldr_copy_pending[p] = true;
+    c->ldr_last_copy = (int)p;
+    return XR_OK;
+}
+
+xr_status xr_wait_output(XrContext* c) {
+    if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "wait_output: null context");
+    if (c->ldr_last_copy < 0) return XR_OK;
+    DeviceGuard g(c->device);
+    return cuda_check(c, cudaEventSynchronize(c->ldr_copied[c->ldr_last_copy]), "wait_output");
 }
 
 xr_status xr_output_device_ptr(XrContext* c, uint32_t which, void** dptr) {

@@ -328,6 +328,14 @@ struct Context {
     uint32_t error_flags = 0;
     cudaEvent_t ev[8] = {};          // 0..3 frame passes, 5 UBO staging, 6/7 cache inference / training
     cudaEvent_t user_ev[8] = {};
+    // asynchronous image reads (xr_read_output_async): the LDR image is double-buffered by
+    // frame parity; a read copies the last frame's buffer on copy_stream once the frame is done
+    cudaStream_t copy_stream = nullptr;
+    uchar4* ldr[2] = {nullptr, nullptr};
+    cudaEvent_t ldr_ready[2] = {};   // recorded on the frame stream: the buffer's frame is complete
+    cudaEvent_t ldr_copied[2] = {};  // recorded on copy_stream: the buffer has been read
+    bool ldr_copy_pending[2] = {false, false};   // a frame that writes the buffer waits for the read first
+    int ldr_last_copy = -1;          // the buffer of the last asynchronous read (-1: none)
     XrStats stats{};
     CacheState cache;
 
