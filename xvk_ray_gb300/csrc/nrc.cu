@@ -68,12 +68,21 @@ __device__ __forceinline__ void load_row64(const uint8_t* base, uint32_t r, floa
     }
 }
 
-// Column `col` (a sample) of a K-major [rows][128] operand <- rows values.
+// The transposed operands of the weight-gradient MMAs (dZ^T, H^T: K = 128 samples)
+// use the K-major canonical layout with the core matrices adjacent in K 144 bytes
+// apart instead of 128 (LBO = 144, 8-row groups 16 x 144 = 2304 bytes apart).  A
+// warp writes one column per lane: 32 consecutive samples, four core matrices'
+// 16-byte rows, which then start on banks 0, 4, 8 and 12 instead of all on bank 0
+// (no 4-way conflict on the 64 two-byte stores of each column).
+constexpr uint32_t kTLbo = 144, kTSbo = 16u * kTLbo;
+__host__ __device__ __forceinline__ uint32_t t_offset(uint32_t r, uint32_t k) {
+    return (r >> 3) * kTSbo + (k >> 3) * kTLbo + (r & 7u) * 16u + (k & 7u) * 2u;
+}
 template <int ROWS>
-__device__ __forceinline__ void store_col128(uint8_t* base, uint32_t col, const float* v) {
+__device__ __forceinline__ void store_col_t(uint8_t* base, uint32_t col, const float* v) {
 #pragma unroll
     for (int r = 0; r < ROWS; ++r)
-        *reinterpret_cast<uint16_t*>(base + umma::kmajor_offset(r, col, 128)) = umma::bf16_bits(v[r]);
+        *reinterpret_cast<uint16_t*>(base + t_offset((uint32_t)r, col)) = umma::bf16_bits(v[r]);
 }
 
 __device__ __forceinline__ void copy_image(uint8_t* dst, const uint8_t* __restrict__ src, uint32_t bytes) {
@@ -98,6 +107,18 @@ __device__ __forceinline__ void gemm(uint32_t d_tmem, const uint8_t* A, const ui
     for (uint32_t s = 0; s < steps; ++s) {
         const uint64_t ad = umma::smem_desc(a0 + 256u * s, 128u, K * 16u);
         const uint64_t bd = umma::smem_desc(b0 + 256u * s, 128u, K * 16u);
+        umma::mma_bf16(d_tmem, ad, bd, id, (accumulate || s > 0) ? 1u : 0u);
+    }
+}
+
+// D (+)= A[128][128] * B[N][128]^T over the transposed (padded) layout; one thread.
+__device__ __forceinline__ void gemm_t(uint32_t d_tmem, const uint8_t* A, const uint8_t* B, uint32_t N,
+                                       bool accumulate) {
+    const uint32_t id = umma::idesc_bf16_f32(128, N);
+    const uint32_t a0 = umma::smem_u32(A), b0 = umma::smem_u32(B);
+    for (uint32_t s = 0; s < 8u; ++s) {   // K = 16 per step: two core matrices
+        const uint64_t ad = umma::smem_desc(a0 + 2u * kTLbo * s, kTLbo, kTSbo);
+        const uint64_t bd = umma::smem_desc(b0 + 2u * kTLbo * s, kTLbo, kTSbo);
         umma::mma_bf16(d_tmem, ad, bd, id, (accumulate || s > 0) ? 1u : 0u);
     }
 }
@@ -473,13 +494,14 @@ __global__ void __launch_bounds__(256) k_cache_scatter(const float4* __restrict_
 }
 
 // Forward + backward of every tile.
-// Shared memory (217,088 B): forward image, backward image, H_0..H_4, dZ,
-// dZ^T [128][128] (rows beyond the layer's outputs zero), H^T [64][128].
+// Shared memory (223,232 B): forward image, backward image, H_0..H_4, dZ,
+// dZ^T [128][128] (rows beyond the layer's outputs zero) and H^T [64][128] in
+// the padded transposed layout.
 // Tensor memory (512 columns): 0..63 forward / dX accumulator, 64 + 64 l: dW_l.
 constexpr uint32_t kOffWf = 0, kOffWb = kImageBytes, kOffX = 2 * kImageBytes;
-constexpr uint32_t kOffDZ = kOffX + 5 * kActBytes, kOffDZT = kOffDZ + kActBytes, kOffHT = kOffDZT + 2 * kActBytes;
-constexpr uint32_t kTrainSmem = kOffHT + kActBytes;
-static_assert(kTrainSmem == 217088, "training shared memory layout");
+constexpr uint32_t kOffDZ = kOffX + 5 * kActBytes, kOffDZT = kOffDZ + kActBytes, kOffHT = kOffDZT + 16u * kTSbo;
+constexpr uint32_t kTrainSmem = kOffHT + 8u * kTSbo;
+static_assert(kTrainSmem == 223232 && kTrainSmem <= 232448, "training shared memory layout");
 
 __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict__ rec, const uint32_t* __restrict__ perm,
                                                         const uint32_t* count_ptr,
@@ -506,9 +528,9 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict_
     if (tid == 0) { umma::mbar_init(&bar, 1); umma::mbar_fence_init(); }
     copy_image(sWf, w_fwd, kImageBytes);
     copy_image(sWb, w_bwd, kImageBytes);
-    // rows 64..127 of dZ^T (bytes 16384..32767: row groups 8..15 of 2048 B) stay
-    // zero -- the padding of the M = 128 weight-gradient MMAs
-    for (uint32_t off = 16384u + tid * 16u; off < 32768u; off += 128u * 16u)
+    // rows 64..127 of dZ^T (row groups 8..15) stay zero -- the padding of the
+    // M = 128 weight-gradient MMAs
+    for (uint32_t off = 8u * kTSbo + tid * 16u; off < 16u * kTSbo; off += 128u * 16u)
         *reinterpret_cast<uint4*>(sDZT + off) = make_uint4(0, 0, 0, 0);
     umma::fence_before_sync();
     __syncthreads();
@@ -570,21 +592,21 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict_
             }
         }
         store_row<16>(sDZ, tid, dz);
-        store_col128<16>(sDZT, tid, dz);
-        // rows 16..63 of dZ^T (bytes 4096..16383): zero -- the previous tile's
-        // hidden layers left values there
-        for (uint32_t off = 4096u + tid * 16u; off < 16384u; off += 128u * 16u)
+        store_col_t<16>(sDZT, tid, dz);
+        // rows 16..63 of dZ^T (row groups 2..7): zero -- the previous tile's hidden
+        // layers left values there
+        for (uint32_t off = 2u * kTSbo + tid * 16u; off < 8u * kTSbo; off += 128u * 16u)
             *reinterpret_cast<uint4*>(sDZT + off) = make_uint4(0, 0, 0, 0);
         // ---- backward: layer 4 .. 0 ----
         for (int l = kHidden; l >= 0 && ok; --l) {
             // H_l^T from this thread's own row of H_l
             load_row64(sX + l * kActBytes, tid, v);
-            store_col128<64>(sHT, tid, v);
+            store_col_t<64>(sHT, tid, v);
             publish();
             if (tid == 0) {
                 const uint32_t K = l == kHidden ? 16u : 64u;
                 gemm(tmem, sDZ, sWb + l * kLayerBytes, K, 64u, K / 16u, false);                  // dX = dZ W_l
-                gemm(tmem + 64u + 64u * (uint32_t)l, sDZT, sHT, 128u, 64u, 8u, !first);       // dW_l += dZ^T H_l
+                gemm_t(tmem + 64u + 64u * (uint32_t)l, sDZT, sHT, 64u, !first);                // dW_l += dZ^T H_l
                 umma::commit(&bar);
             }
             ok = wait_mma(&bar, phase);
@@ -599,7 +621,7 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(const uint4* __restrict_
                 // the bf16-rounded values of dz, as the MMA will see them
 #pragma unroll
                 for (int j = 0; j < kWidth; ++j) dz[j] = umma::bf16_value(umma::bf16_bits(dz[j]));
-                store_col128<64>(sDZT, tid, dz);
+                store_col_t<64>(sDZT, tid, dz);
             } else {
                 // gradients of the 32 encoding features, feature-major over the tile's inputs (every
                 // thread's loads of the tile completed before the first barrier of this tile)
