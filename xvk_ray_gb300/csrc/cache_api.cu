@@ -230,14 +230,30 @@ void cache_after_paths(Context* c) {
     CacheState& cs = c->cache;
     if (!c->fa.cache_on) return;
     uint32_t* err = c->d_counters + kCntError;
+    // The training updates the network for the next frame and touches nothing the
+    // inference or the reservoir passes write: its gradients run on the side stream
+    // beside the inference, Adam (which overwrites the table and weights the
+    // inference reads) after it, and the side stream joins before the frame ends
+    // (enqueue_frame).
+    if (cs.frame_trained) {
+        cudaEventRecord(c->fork_ev, c->stream);
+        cudaStreamWaitEvent(c->side_stream, c->fork_ev, 0);
+        launch_cache_grads(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap, err, c->sm_count,
+                           c->side_stream);
+        launch_cache_select_next(cs.sel, c->d_counters + kCntCacheTrain, cs.sel_target, c->N, 0u, c->side_stream);
+    }
     record_event(c, c->ev[6]);
     launch_cache_infer(cs, cs.queries, c->d_counters + kCntCacheQuery, 0u, nullptr, c->fa.cand_b, err, c->sm_count,
                        c->stream);
     record_event(c, c->ev[7]);
     if (cs.frame_trained) {
-        launch_cache_train(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap, true, err, c->sm_count,
-                           c->stream);
-        launch_cache_select_next(cs.sel, c->d_counters + kCntCacheTrain, cs.sel_target, c->N, 0u, c->stream);
+        cudaEventRecord(c->infer_ev, c->stream);
+        cudaStreamWaitEvent(c->side_stream, c->infer_ev, 0);
+        launch_cache_adam(cs, c->side_stream);
+        record_event_on(c->side_stream, c->ev[4]);
+        c->side_pending = true;
+    } else {
+        record_event(c, c->ev[4]);
     }
 }
 
@@ -458,7 +474,7 @@ xr_status xr_cache_get_stats(XrContext* c, XrCacheStats* out) {
         o.queries = cnt[0];
         o.train_samples = cnt[1];
         cudaEventElapsedTime(&o.ms_infer, c->ev[6], c->ev[7]);
-        cudaEventElapsedTime(&o.ms_train, c->ev[7], c->ev[1]);
+        cudaEventElapsedTime(&o.ms_train, c->ev[6], c->ev[4]);   // from the inference's start: the two overlap
     }
     *out = o;
     return s;

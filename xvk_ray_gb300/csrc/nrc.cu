@@ -879,6 +879,15 @@ void launch_cache_infer(CacheState& cs, const uint4* rec, const uint32_t* count_
 
 void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
                         uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st) {
+    launch_cache_grads(cs, rec, count_ptr, count_host, cap, err, sm_count, st);
+    if (apply) launch_cache_adam(cs, st);
+}
+
+// The gradients of one training batch (spatial order, encoding, forward + backward,
+// table-gradient scatter); they read the table and weights and write only the
+// gradient buffers, the loss and their own scratch.
+void launch_cache_grads(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                        uint32_t cap, uint32_t* err, int sm_count, cudaStream_t st) {
     uint32_t grid = (uint32_t)sm_count;
     if (!count_ptr) {
         const uint32_t tiles = (count_host < cap ? count_host : cap) / kTile;
@@ -911,7 +920,6 @@ void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_
         k_cache_scatter<<<wide, 256, 0, st>>>(upos, count_ptr, count_host, cap, reinterpret_cast<const float*>(cs.tiles),
                                               reinterpret_cast<float2*>(cs.grid_grad), err);
     }
-    if (apply) launch_cache_adam(cs, st);
 }
 
 void launch_cache_select_next(uint32_t* sel, const uint32_t* got, uint32_t target, uint32_t n, uint32_t set_to,

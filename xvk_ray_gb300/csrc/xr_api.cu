@@ -217,13 +217,15 @@ xr_status stage_ubos(Context* c, const XrUniformBufferObject* ubos, uint32_t n) 
 // wait on it and time with it when the graph is replayed.
 }  // namespace
 
-cudaError_t record_event(Context* c, cudaEvent_t e) {
+cudaError_t record_event_on(cudaStream_t st, cudaEvent_t e) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    cudaError_t q = cudaStreamIsCapturing(c->stream, &cs);
+    cudaError_t q = cudaStreamIsCapturing(st, &cs);
     if (q != cudaSuccess) return q;
-    if (cs == cudaStreamCaptureStatusActive) return cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal);
-    return cudaEventRecord(e, c->stream);
+    if (cs == cudaStreamCaptureStatusActive) return cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+    return cudaEventRecord(e, st);
 }
+
+cudaError_t record_event(Context* c, cudaEvent_t e) { return record_event_on(c->stream, e); }
 
 namespace {
 
@@ -327,6 +329,10 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     c->sm_count = prop.multiProcessorCount;
     if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) goto bad;
     if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "copy stream"))) goto bad;
+    if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking), "side stream"))) goto bad;
+    if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event"))) goto bad;
+    if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming), "event"))) goto bad;
+    if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->infer_ev, cudaEventDisableTiming), "event"))) goto bad;
     for (int i = 0; i < 2; i++) {
         if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->ldr_ready[i], cudaEventDisableTiming), "event"))) goto bad;
         if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->ldr_copied[i], cudaEventDisableTiming), "event"))) goto bad;
@@ -391,6 +397,10 @@ void xr_destroy(XrContext* c) {
         if (c->ldr_copied[i]) cudaEventDestroy(c->ldr_copied[i]);
     }
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->infer_ev) cudaEventDestroy(c->infer_ev);
+    if (c->side_stream) { cudaStreamSynchronize(c->side_stream); cudaStreamDestroy(c->side_stream); }
     if (c->stream) cudaStreamSynchronize(c->stream);   // pool frees queued by free_instances
     if (c->pool) cudaMemPoolDestroy(c->pool);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -641,6 +651,11 @@ static xr_status enqueue_frame(Context* c, uint32_t n_ubo, uint32_t nb, bool reu
     launch_temporal(c->fa, temporal_writes_image, c->stream);
     record_event(c, c->ev[2]);
     if (compat || c->params.spatial_on) launch_spatial(c->fa, c->stream);
+    if (c->side_pending) {   // the cache's training (cache_after_paths) joins here
+        cudaEventRecord(c->join_ev, c->side_stream);
+        cudaStreamWaitEvent(c->stream, c->join_ev, 0);
+        c->side_pending = false;
+    }
     record_event(c, c->ev[3]);
     return cuda_check(c, cudaGetLastError(), "render launch");
 }

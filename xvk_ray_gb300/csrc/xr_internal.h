@@ -326,7 +326,13 @@ struct Context {
     unsigned long long* d_work = nullptr;   // node visits, triangle tests of the last ray query
     uint64_t query_rays = 0;
     uint32_t error_flags = 0;
-    cudaEvent_t ev[8] = {};          // 0..3 frame passes, 5 UBO staging, 6/7 cache inference / training
+    cudaEvent_t ev[8] = {};          // 0..3 frame passes, 4 end of cache training, 5 UBO staging, 6/7 cache inference
+    // the cache's training runs on side_stream beside the inference and the reservoir
+    // passes: forked after the paths (fork_ev), Adam after the inference (infer_ev),
+    // joined before the frame's end (join_ev)
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, infer_ev = nullptr, join_ev = nullptr;
+    bool side_pending = false;
     cudaEvent_t user_ev[8] = {};
     // asynchronous image reads (xr_read_output_async): the LDR image is double-buffered by
     // frame parity; a read copies the last frame's buffer on copy_stream once the frame is done
@@ -358,6 +364,7 @@ constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
 void invalidate_graphs(Context* c);
 // Records `e` on the context's stream (an external event node when the stream is being captured).
 cudaError_t record_event(Context* c, cudaEvent_t e);
+cudaError_t record_event_on(cudaStream_t st, cudaEvent_t e);
 xr_status realloc_pixels(Context* c);   // per-pixel buffers and view table for the current views / params
 
 xr_status fail(const Context* ctx, xr_status code, const std::string& msg);
@@ -429,6 +436,8 @@ void launch_cache_infer(CacheState& cs, const uint4* rec, const uint32_t* count_
                         float4* cand_b, uint32_t* err, int sm_count, cudaStream_t st);
 void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
                         uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st);
+void launch_cache_grads(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                        uint32_t cap, uint32_t* err, int sm_count, cudaStream_t st);
 void launch_cache_adam(CacheState& cs, cudaStream_t st);   // one Adam step on the gradients (bias correction on the device)
 void launch_cache_adam_reset(CacheState& cs, cudaStream_t st);
 void launch_cache_wait_selftest(uint64_t limit_ns, uint32_t* err, cudaStream_t st);   // a wait that runs out
