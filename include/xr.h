@@ -433,9 +433,8 @@ typedef struct XrCacheStats {
     uint32_t queries;            /* cache queries of the last frame */
     uint32_t train_samples;      /* training samples of the last frame (before rounding to 128) */
     float loss;                  /* mean relative L2 loss of the last training step */
-    float ms_infer, ms_train;    /* last frame (CUDA events): inference; training + Adam, which run on a side
-                                    stream beside the inference and the reservoir passes, timed from the
-                                    inference's start to the end of Adam */
+    float ms_infer, ms_train;    /* last frame (CUDA events): inference and training + Adam, each on its own
+                                    side stream beside the rest of the frame, from its start to its end */
     float bounds_lo[3];          /* scene cube: unit position = (x - lo) * inv_extent */
     float inv_extent;
 } XrCacheStats;

@@ -226,34 +226,66 @@ xr_status cache_prepare_frame(Context* c, uint32_t frame) {
     return XR_OK;
 }
 
+// Once bounce 1's shading is enqueued the frame's query records are complete: the
+// inference runs on the inference stream beside the rest of the bounce loop, which
+// from bounce 2 on traces only the training paths and writes only their records
+// (no candidate, no query).
+void cache_after_bounce1(void* ctx) {
+    Context* c = static_cast<Context*>(ctx);
+    CacheState& cs = c->cache;
+    if (!c->fa.cache_on) return;
+    cudaEventRecord(c->infer_fork_ev, c->stream);
+    cudaStreamWaitEvent(c->infer_stream, c->infer_fork_ev, 0);
+    if (cs.frame_trained) {
+        // the training's first stage needs only bounce 1's record words (not the targets
+        // the later bounces accumulate): it runs beside them on the side stream too
+        cudaStreamWaitEvent(c->side_stream, c->infer_fork_ev, 0);
+        record_event_on(c->side_stream, c->ev_train0);
+        launch_cache_encode_stage(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap, c->sm_count,
+                                  c->side_stream);
+        c->side_pending = true;
+    }
+    record_event_on(c->infer_stream, c->ev[6]);
+    launch_cache_infer(cs, cs.queries, c->d_counters + kCntCacheQuery, 0u, nullptr, c->fa.cand_b,
+                       c->d_counters + kCntError, c->sm_count, c->infer_stream);
+    record_event_on(c->infer_stream, c->ev[7]);
+    cudaEventRecord(c->infer_ev, c->infer_stream);
+    c->infer_pending = true;
+}
+
+// After the bounce loop: the training (gradients, then Adam once the inference,
+// which reads the table and weights Adam overwrites, is done) runs on the side
+// stream beside the reservoir passes and joins before the frame ends
+// (enqueue_frame); the frame stream waits for the inference before the temporal pass.
 void cache_after_paths(Context* c) {
     CacheState& cs = c->cache;
     if (!c->fa.cache_on) return;
     uint32_t* err = c->d_counters + kCntError;
-    // The training updates the network for the next frame and touches nothing the
-    // inference or the reservoir passes write: its gradients run on the side stream
-    // beside the inference, Adam (which overwrites the table and weights the
-    // inference reads) after it, and the side stream joins before the frame ends
-    // (enqueue_frame).
     if (cs.frame_trained) {
+        if (!c->side_pending) {   // no bounce 1 (a single-bounce frame): the first stage runs here
+            cudaEventRecord(c->fork_ev, c->stream);
+            cudaStreamWaitEvent(c->side_stream, c->fork_ev, 0);
+            record_event_on(c->side_stream, c->ev_train0);
+            launch_cache_encode_stage(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap,
+                                      c->sm_count, c->side_stream);
+        }
+        // the second stage reads the records' targets: after the whole bounce loop
         cudaEventRecord(c->fork_ev, c->stream);
         cudaStreamWaitEvent(c->side_stream, c->fork_ev, 0);
-        launch_cache_grads(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap, err, c->sm_count,
-                           c->side_stream);
+        launch_cache_grad_stage(cs, cs.train, c->d_counters + kCntCacheTrain, 0u, c->fa.cache_t_cap, err, c->sm_count,
+                                c->side_stream);
         launch_cache_select_next(cs.sel, c->d_counters + kCntCacheTrain, cs.sel_target, c->N, 0u, c->side_stream);
-    }
-    record_event(c, c->ev[6]);
-    launch_cache_infer(cs, cs.queries, c->d_counters + kCntCacheQuery, 0u, nullptr, c->fa.cand_b, err, c->sm_count,
-                       c->stream);
-    record_event(c, c->ev[7]);
-    if (cs.frame_trained) {
-        cudaEventRecord(c->infer_ev, c->stream);
-        cudaStreamWaitEvent(c->side_stream, c->infer_ev, 0);
+        if (c->infer_pending) cudaStreamWaitEvent(c->side_stream, c->infer_ev, 0);
         launch_cache_adam(cs, c->side_stream);
         record_event_on(c->side_stream, c->ev[4]);
         c->side_pending = true;
     } else {
+        record_event(c, c->ev_train0);
         record_event(c, c->ev[4]);
+    }
+    if (c->infer_pending) {
+        cudaStreamWaitEvent(c->stream, c->infer_ev, 0);
+        c->infer_pending = false;
     }
 }
 
@@ -474,7 +506,7 @@ xr_status xr_cache_get_stats(XrContext* c, XrCacheStats* out) {
         o.queries = cnt[0];
         o.train_samples = cnt[1];
         cudaEventElapsedTime(&o.ms_infer, c->ev[6], c->ev[7]);
-        cudaEventElapsedTime(&o.ms_train, c->ev[6], c->ev[4]);   // from the inference's start: the two overlap
+        cudaEventElapsedTime(&o.ms_train, c->ev_train0, c->ev[4]);
     }
     *out = o;
     return s;

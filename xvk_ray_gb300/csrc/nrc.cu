@@ -879,47 +879,63 @@ void launch_cache_infer(CacheState& cs, const uint4* rec, const uint32_t* count_
 
 void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
                         uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st) {
-    launch_cache_grads(cs, rec, count_ptr, count_host, cap, err, sm_count, st);
+    launch_cache_encode_stage(cs, rec, count_ptr, count_host, cap, sm_count, st);
+    launch_cache_grad_stage(cs, rec, count_ptr, count_host, cap, err, sm_count, st);
     if (apply) launch_cache_adam(cs, st);
 }
 
-// The gradients of one training batch (spatial order, encoding, forward + backward,
-// table-gradient scatter); they read the table and weights and write only the
-// gradient buffers, the loss and their own scratch.
-void launch_cache_grads(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
-                        uint32_t cap, uint32_t* err, int sm_count, cudaStream_t st) {
+static uint32_t train_grid(int sm_count, const uint32_t* count_ptr, uint32_t count_host, uint32_t cap) {
     uint32_t grid = (uint32_t)sm_count;
     if (!count_ptr) {
         const uint32_t tiles = (count_host < cap ? count_host : cap) / kTile;
         if (tiles < grid) grid = tiles;
     }
+    return grid;
+}
+
+// Stage 1 of a training batch: spatial order and the encoded inputs.  It reads the
+// records' position, normal, direction and material words (not the targets), the
+// table, and writes its own scratch and the zeroed loss.
+void launch_cache_encode_stage(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                               uint32_t cap, int sm_count, cudaStream_t st) {
     cudaMemsetAsync(cs.loss, 0, sizeof(float), st);
-    if (grid) {
-        const nrc::Bounds bnd = bounds_of(cs);
-        const uint32_t wide = (uint32_t)sm_count * 8u;   // 8 x 256 threads per SM, grid-stride
-        uint32_t* k0 = cs.order;
-        uint32_t* v0 = cs.order + cs.train_cap;
-        uint32_t* k1 = cs.order + 2 * (size_t)cs.train_cap;
-        uint32_t* v1 = cs.order + 3 * (size_t)cs.train_cap;
-        k_cache_order_keys<<<kOrderBlocks, kOrderThreads, 0, st>>>(rec, count_ptr, count_host, cap, bnd, k0, v0,
-                                                                   cs.order_hist);
-        for (uint32_t shift = 0; shift < 24u; shift += 8u) {
-            if (shift)
-                k_cache_order_hist<<<kOrderBlocks, kOrderThreads, 0, st>>>(k0, count_ptr, count_host, cap, shift,
-                                                                           cs.order_hist);
-            k_cache_order_scatter<<<kOrderBlocks, kOrderThreads, 0, st>>>(k0, v0, k1, v1, count_ptr, count_host, cap,
-                                                                          shift, cs.order_hist);
-            std::swap(k0, k1);
-            std::swap(v0, v1);
-        }
-        const uint32_t* perm = v0;   // the last pass's output
-        float4* upos = reinterpret_cast<float4*>(cs.order + 4 * (size_t)cs.train_cap);
-        k_cache_encode<<<wide, 256, 0, st>>>(rec, perm, count_ptr, count_host, cap, bnd, cs.table, cs.tiles, upos);
-        k_cache_train<<<grid, 128, kTrainSmem, st>>>(rec, perm, count_ptr, count_host, cap, cs.tiles, cs.w_fwd,
-                                                     cs.w_bwd, cs.mlp_grad, cs.loss, err);
-        k_cache_scatter<<<wide, 256, 0, st>>>(upos, count_ptr, count_host, cap, reinterpret_cast<const float*>(cs.tiles),
-                                              reinterpret_cast<float2*>(cs.grid_grad), err);
+    if (!train_grid(sm_count, count_ptr, count_host, cap)) return;
+    const nrc::Bounds bnd = bounds_of(cs);
+    const uint32_t wide = (uint32_t)sm_count * 8u;   // 8 x 256 threads per SM, grid-stride
+    uint32_t* k0 = cs.order;
+    uint32_t* v0 = cs.order + cs.train_cap;
+    uint32_t* k1 = cs.order + 2 * (size_t)cs.train_cap;
+    uint32_t* v1 = cs.order + 3 * (size_t)cs.train_cap;
+    k_cache_order_keys<<<kOrderBlocks, kOrderThreads, 0, st>>>(rec, count_ptr, count_host, cap, bnd, k0, v0,
+                                                               cs.order_hist);
+    for (uint32_t shift = 0; shift < 24u; shift += 8u) {
+        if (shift)
+            k_cache_order_hist<<<kOrderBlocks, kOrderThreads, 0, st>>>(k0, count_ptr, count_host, cap, shift,
+                                                                       cs.order_hist);
+        k_cache_order_scatter<<<kOrderBlocks, kOrderThreads, 0, st>>>(k0, v0, k1, v1, count_ptr, count_host, cap,
+                                                                      shift, cs.order_hist);
+        std::swap(k0, k1);
+        std::swap(v0, v1);
     }
+    // three passes: the order ends in the second key / value pair
+    float4* upos = reinterpret_cast<float4*>(cs.order + 4 * (size_t)cs.train_cap);
+    k_cache_encode<<<wide, 256, 0, st>>>(rec, v0, count_ptr, count_host, cap, bnd, cs.table, cs.tiles, upos);
+}
+
+// Stage 2: forward + backward (which read the records' targets) and the
+// table-gradient scatter; they read the weights and write only the gradients,
+// the loss and the tiles.
+void launch_cache_grad_stage(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                             uint32_t cap, uint32_t* err, int sm_count, cudaStream_t st) {
+    const uint32_t grid = train_grid(sm_count, count_ptr, count_host, cap);
+    if (!grid) return;
+    const uint32_t wide = (uint32_t)sm_count * 8u;
+    const uint32_t* perm = cs.order + 3 * (size_t)cs.train_cap;   // the sort's result (second value array)
+    const float4* upos = reinterpret_cast<const float4*>(cs.order + 4 * (size_t)cs.train_cap);
+    k_cache_train<<<grid, 128, kTrainSmem, st>>>(rec, perm, count_ptr, count_host, cap, cs.tiles, cs.w_fwd, cs.w_bwd,
+                                                 cs.mlp_grad, cs.loss, err);
+    k_cache_scatter<<<wide, 256, 0, st>>>(upos, count_ptr, count_host, cap, reinterpret_cast<const float*>(cs.tiles),
+                                          reinterpret_cast<float2*>(cs.grid_grad), err);
 }
 
 void launch_cache_select_next(uint32_t* sel, const uint32_t* got, uint32_t target, uint32_t n, uint32_t set_to,

@@ -1446,7 +1446,7 @@ uint32_t trace_grid(int sm_count, bool instances) {
     return (uint32_t)(o * sm_count);
 }
 
-void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
+void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st, void (*after_bounce1)(void*), void* arg) {
     const uint32_t grid0 = fa.n_tiles;
     FrameArgs a = fa;
     if (fa.compat) k_raygen<true><<<grid0, kBlock, 0, st>>>(a, fa.ubo, nb);
@@ -1467,8 +1467,10 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st) {
         if (nee) cudaMemsetAsync(fa.counters + kCntCacheNee, 0, 2 * sizeof(uint32_t), st);   // count + fetch
         if (fa.compat) k_shade<true><<<fa.grid_persistent, kShadeBlock, 0, st>>>(a, fa.ubo, b, nb);
         else k_shade<false><<<fa.grid_persistent, kShadeBlock, 0, st>>>(a, fa.ubo, b, nb);
+        if (b == 1u && after_bounce1) after_bounce1(arg);   // bounce 1's records are complete
         if (nee) k_trace_nee<<<fa.grid_trace, kTraceBlock, 0, st>>>(a);
     }
+    if (nb < 2u && after_bounce1) after_bounce1(arg);
 }
 
 void launch_temporal(const FrameArgs& fa, bool write_image, cudaStream_t st) {

@@ -333,6 +333,10 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event"))) goto bad;
     if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming), "event"))) goto bad;
     if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->infer_ev, cudaEventDisableTiming), "event"))) goto bad;
+    if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->infer_fork_ev, cudaEventDisableTiming), "event"))) goto bad;
+    if ((s = cuda_check(c, cudaEventCreate(&c->ev_train0), "event"))) goto bad;
+    if ((s = cuda_check(c, cudaStreamCreateWithFlags(&c->infer_stream, cudaStreamNonBlocking), "inference stream")))
+        goto bad;
     for (int i = 0; i < 2; i++) {
         if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->ldr_ready[i], cudaEventDisableTiming), "event"))) goto bad;
         if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->ldr_copied[i], cudaEventDisableTiming), "event"))) goto bad;
@@ -400,6 +404,9 @@ void xr_destroy(XrContext* c) {
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     if (c->infer_ev) cudaEventDestroy(c->infer_ev);
+    if (c->infer_fork_ev) cudaEventDestroy(c->infer_fork_ev);
+    if (c->ev_train0) cudaEventDestroy(c->ev_train0);
+    if (c->infer_stream) { cudaStreamSynchronize(c->infer_stream); cudaStreamDestroy(c->infer_stream); }
     if (c->side_stream) { cudaStreamSynchronize(c->side_stream); cudaStreamDestroy(c->side_stream); }
     if (c->stream) cudaStreamSynchronize(c->stream);   // pool frees queued by free_instances
     if (c->pool) cudaMemPoolDestroy(c->pool);
@@ -644,8 +651,8 @@ static xr_status enqueue_frame(Context* c, uint32_t n_ubo, uint32_t nb, bool reu
     cudaMemsetAsync(c->d_counters, 0, kCntError * 4, c->stream);   // keep the sticky error word
     const bool compat = c->params.compat_reference != 0;
     record_event(c, c->ev[0]);
-    launch_initial(c->fa, nb, c->stream);
-    cache_after_paths(c);   // radiance-cache inference and training (when enabled)
+    launch_initial(c->fa, nb, c->stream, c->fa.cache_on ? cache_after_bounce1 : nullptr, c);
+    cache_after_paths(c);   // radiance-cache training; the temporal pass waits for the inference (when enabled)
     record_event(c, c->ev[1]);
     bool temporal_writes_image = compat ? !reuse0 : (c->params.spatial_on == 0u);
     launch_temporal(c->fa, temporal_writes_image, c->stream);

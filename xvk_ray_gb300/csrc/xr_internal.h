@@ -327,12 +327,15 @@ struct Context {
     uint64_t query_rays = 0;
     uint32_t error_flags = 0;
     cudaEvent_t ev[8] = {};          // 0..3 frame passes, 4 end of cache training, 5 UBO staging, 6/7 cache inference
-    // the cache's training runs on side_stream beside the inference and the reservoir
-    // passes: forked after the paths (fork_ev), Adam after the inference (infer_ev),
-    // joined before the frame's end (join_ev)
-    cudaStream_t side_stream = nullptr;
-    cudaEvent_t fork_ev = nullptr, infer_ev = nullptr, join_ev = nullptr;
-    bool side_pending = false;
+    // The cache's inference runs on infer_stream beside the training paths' bounces 2..
+    // (forked at infer_fork_ev once bounce 1's queries exist, joined by the temporal pass
+    // at infer_ev); its training runs on side_stream beside the reservoir passes (forked
+    // after the paths at fork_ev, Adam after infer_ev, joined before the frame's end at
+    // join_ev).  ev_train0 times the training's start.
+    cudaStream_t side_stream = nullptr, infer_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, infer_fork_ev = nullptr, infer_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t ev_train0 = nullptr;
+    bool side_pending = false, infer_pending = false;
     cudaEvent_t user_ev[8] = {};
     // asynchronous image reads (xr_read_output_async): the LDR image is double-buffered by
     // frame parity; a read copies the last frame's buffer on copy_stream once the frame is done
@@ -414,7 +417,10 @@ void launch_trace(const DeviceScene& sc, const float* rays, uint32_t n, int any_
                   cudaStream_t st);
 
 // ---- launch wrappers (restir.cu) ----
-void launch_initial(const FrameArgs& fa, uint32_t number_of_bounces, cudaStream_t st);
+// after_bounce1(arg), when given, is called once bounce 1's shading is enqueued (or after the
+// loop for a single bounce): the enqueue point of work that needs only bounce 1's records.
+void launch_initial(const FrameArgs& fa, uint32_t number_of_bounces, cudaStream_t st,
+                    void (*after_bounce1)(void*) = nullptr, void* arg = nullptr);
 void launch_temporal(const FrameArgs& fa, bool write_image, cudaStream_t st);
 void launch_spatial(const FrameArgs& fa, cudaStream_t st);
 void launch_accumulate_sample(const FrameArgs& fa, double* acc, cudaStream_t st);
@@ -436,8 +442,10 @@ void launch_cache_infer(CacheState& cs, const uint4* rec, const uint32_t* count_
                         float4* cand_b, uint32_t* err, int sm_count, cudaStream_t st);
 void launch_cache_train(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
                         uint32_t cap, bool apply, uint32_t* err, int sm_count, cudaStream_t st);
-void launch_cache_grads(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
-                        uint32_t cap, uint32_t* err, int sm_count, cudaStream_t st);
+void launch_cache_encode_stage(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                               uint32_t cap, int sm_count, cudaStream_t st);
+void launch_cache_grad_stage(CacheState& cs, const uint4* rec, const uint32_t* count_ptr, uint32_t count_host,
+                             uint32_t cap, uint32_t* err, int sm_count, cudaStream_t st);
 void launch_cache_adam(CacheState& cs, cudaStream_t st);   // one Adam step on the gradients (bias correction on the device)
 void launch_cache_adam_reset(CacheState& cs, cudaStream_t st);
 void launch_cache_wait_selftest(uint64_t limit_ns, uint32_t* err, cudaStream_t st);   // a wait that runs out
@@ -447,7 +455,8 @@ void launch_cache_select_next(uint32_t* sel, const uint32_t* got, uint32_t targe
                               cudaStream_t st);
 // ---- cache_api.cu ----
 xr_status cache_prepare_frame(Context* c, uint32_t frame);   // capacities; sets the FrameArgs cache fields
-void cache_after_paths(Context* c);           // inference (+ training) after the bounce loop
+void cache_after_bounce1(void* ctx);          // the cache's inference, forked once bounce 1's queries exist
+void cache_after_paths(Context* c);           // its training after the bounce loop; the frame waits for the inference
 void cache_free(Context* c);
 void cache_scene_bounds(Context* c, const float* vertices, uint32_t nv);
 
