@@ -3,6 +3,8 @@ import sys
 from pathlib import Path
 
 sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+
+
 def test_bench_camera_stays_on_the_32_frame_path():
     """Runs longer than the configuration's 32-frame camera path play it forward, then
     back: every frame is one path step (0.01 units, 0.2 degrees) away from the last
