@@ -39,4 +39,3 @@ def test_replicas_take_the_slowest_rank():
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
     assert res[0] == res[1] == (55.0, 55.0 / (32 * 2))
-
