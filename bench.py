@@ -12,7 +12,8 @@ value: device time per frame (CUDA events around K frames, all inputs resident).
 e2e:   the same frames (same warm-up, a fresh context) through the C ABI with
        host buffers: each step uploads the frame's UBO from host memory and reads
        the RGBA8 image back into page-locked host memory, one frame in flight
-       (xr_read_output_async: frame k renders while frame k-1's image is copied).
+       (xr_read_output_async, two frames in flight: frame k renders while the
+       images of frames k-1 and k-2 are copied).
 --impl reference: the CPU restatement of the reference pipeline (oracle) on the
        host cores, per step one bounded sample of the workload.
 
@@ -468,9 +469,11 @@ def run_ours(args):
     # ---- e2e through the C ABI with host buffers ----
     # The same frames as the device-timed region on a fresh context, after the same
     # warm-up: a frame's cost depends on the reservoirs' history, so both legs render
-    # identical frames from identical states.  One frame in flight, as a real-time
-    # host runs: frame k renders while frame k-1's RGBA8 image is copied into
-    # page-locked host memory (two host images).
+    # identical frames from identical states.  Two frames in flight, as a real-time
+    # host runs: frame k renders while the RGBA8 images of frames k-1 and k-2 are
+    # copied into page-locked host memory (three host images); the host waits for
+    # frame k-2's image, so a stall of the host thread shorter than two frames does
+    # not stall the GPU.
     r = xr.Renderer(W, H, device=local)
     r.set_params(xr.params_default(W, H))
     r.upload_scene(scene)
@@ -479,21 +482,22 @@ def run_ours(args):
     for u in ubos[:args.warmup]:
         r.render(u)
     r.sync()
-    pinned = [xr.PinnedBuffer(W * H * 4) for _ in range(2)]
+    pinned = [xr.PinnedBuffer(W * H * 4) for _ in range(3)]
     outs = [pb.array for pb in pinned]
     host_ubos = [L.XrUniformBufferObject.from_buffer_copy(u) for u in ubos[args.warmup:args.warmup + args.steps]]
     _barrier(dist, local)
     t0 = time.perf_counter()
     for k, u in enumerate(host_ubos):
         L.check(lib.xr_render_frame(r.ctx, C.byref(u)), r.ctx)
-        if k:
-            L.check(lib.xr_wait_output(r.ctx), r.ctx)   # frame k-1's image is in host memory
-        L.check(lib.xr_read_output_async(r.ctx, outs[k % 2].ctypes.data, outs[k % 2].nbytes), r.ctx)
-    L.check(lib.xr_wait_output(r.ctx), r.ctx)
+        if k >= 2:
+            L.check(lib.xr_wait_output(r.ctx), r.ctx)   # frame k-2's image is in host memory
+        L.check(lib.xr_read_output_async(r.ctx, outs[k % 3].ctypes.data, outs[k % 3].nbytes), r.ctx)
+    for _ in range(min(args.steps, 2)):
+        L.check(lib.xr_wait_output(r.ctx), r.ctx)
     e2e_ms = (time.perf_counter() - t0) * 1e3
     L.check(lib.xr_sync(r.ctx), r.ctx)   # device error flags of the e2e frames
     e2e_ms = whole_job_ms_per_frame(_max_over_ranks(dist, e2e_ms, f"cuda:{local}"), args.steps, ws)
-    img_mean = float(outs[(args.steps - 1) % 2].reshape(-1, 4)[:, :3].mean())
+    img_mean = float(outs[(args.steps - 1) % 3].reshape(-1, 4)[:, :3].mean())
     for pb in pinned:
         pb.free()
     st.error_flags |= r.stats().error_flags

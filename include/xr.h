@@ -189,10 +189,13 @@ xr_status xr_read_output(XrContext* ctx, uint32_t which, void* host, size_t byte
    stream and returns at once; the next frames render while it runs.  The RGBA8
    image alternates between two device buffers by frame parity, and a frame that
    would overwrite a buffer still being read waits for that read on the device.
-   `host` must stay valid, and should be page-locked for the copy to overlap,
-   until xr_wait_output() returns.  Device error flags are reported by xr_sync(). */
+   At most two reads are in flight (XR_ERR_STATE for a third).  `host` must stay
+   valid, and should be page-locked for the copy to overlap, until the
+   xr_wait_output() that covers it returns.  Device error flags are reported by
+   xr_sync(). */
 xr_status xr_read_output_async(XrContext* ctx, void* host, size_t bytes);
-/* Blocks until the last xr_read_output_async() copy has landed in host memory. */
+/* Blocks until the oldest xr_read_output_async() copy not yet waited for has
+   landed in host memory (returns at once when none is in flight). */
 xr_status xr_wait_output(XrContext* ctx);
 /* Device pointer of an output image as the last frame wrote it (valid until the
    next xr_set_params/xr_destroy; the RGBA8 image's buffer alternates with the

@@ -3,9 +3,11 @@
 Two contexts render the same frames.  One reads every image synchronously
 (xr_read_output).  The other reads asynchronously while the next frames render,
 and its images must be identical:
-* one frame in flight (the host loop bench.py's e2e leg runs);
+* one frame in flight;
 * a read still pending when two more frames are submitted, the second of which
   writes the buffer being read: that frame waits for the read on the device;
+* two frames in flight (the host loop bench.py's e2e leg runs): reads are waited
+  for oldest first, a third read in flight is refused;
 * the same through replayed frame graphs.
 Misuse is refused before anything is enqueued.
 """
@@ -74,6 +76,33 @@ def test_async_reads_match_sync_reads(graphs):
             assert np.array_equal(pinned[0].array.view(np.uint32), ref[6].reshape(-1).view(np.uint32))
             r.sync()
             assert np.array_equal(r.read_output(L.XR_OUT_LDR8), ref[8])
+    finally:
+        for p in pinned:
+            p.free()
+
+
+def test_two_frames_in_flight():
+    scene = _scene()
+    ubos = camera_sequence(scene, W, H, 9, 4)
+    ref = _sync_images(scene, ubos)
+    pinned = [xr.PinnedBuffer(W * H * 4) for _ in range(3)]
+    try:
+        with _renderer(scene, True) as r:
+            got = {}
+            for f, u in enumerate(ubos):
+                r.render(u)
+                if f >= 2:
+                    r.wait_output()                       # frame f-2's image
+                    got[f - 2] = pinned[(f - 2) % 3].array.copy()
+                r.read_output_async(pinned[f % 3].array)
+                if f == 4:                                # a third read in flight is refused
+                    with pytest.raises(xr.XrError, match="two reads"):
+                        r.read_output_async(pinned[(f + 1) % 3].array)
+            for f in (len(ubos) - 2, len(ubos) - 1):
+                r.wait_output()
+                got[f] = pinned[f % 3].array.copy()
+            for f in range(len(ubos)):
+                assert np.array_equal(got[f].view(np.uint32), ref[f].reshape(-1).view(np.uint32)), f"frame {f}"
     finally:
         for p in pinned:
             p.free()

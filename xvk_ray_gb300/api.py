@@ -128,7 +128,7 @@ class Renderer:
         self.ctx = h
         self.width, self.height = width, height
         self.cache = Cache(self)
-        self._pending_read = None   # the array an asynchronous image read is copying into
+        self._pending_reads = []    # the arrays asynchronous image reads copy into, oldest first
 
     def _c(self, status: int) -> None:
         L.check(status, self.ctx)
@@ -137,7 +137,7 @@ class Renderer:
         if self.ctx:
             self._lib.xr_destroy(self.ctx)   # finishes a pending image read first
             self.ctx = None
-        self._pending_read = None
+        self._pending_reads = []
 
     def __del__(self):
         try:
@@ -266,16 +266,18 @@ class Renderer:
     def read_output_async(self, out: np.ndarray) -> None:
         """Starts copying the last frame's RGBA8 image into `out` (width*height*4
         bytes, preferably page-locked: PinnedBuffer.array) and returns at once; the
-        image is there after wait_output().  `out` is kept alive until then."""
+        image is there after the wait_output() that covers it (reads are waited for
+        oldest first; at most two in flight).  `out` is kept alive until then."""
         if out.nbytes < self.width * self.height * 4 or not out.flags["C_CONTIGUOUS"]:
             raise ValueError("read_output_async: need a contiguous array of width*height*4 bytes")
         self._c(self._lib.xr_read_output_async(self.ctx, _ptr(out), out.nbytes))
-        self._pending_read = out
+        self._pending_reads.append(out)
 
     def wait_output(self) -> None:
-        """Blocks until the last read_output_async() copy has landed."""
+        """Blocks until the oldest read_output_async() copy not yet waited for has landed."""
         self._c(self._lib.xr_wait_output(self.ctx))
-        self._pending_read = None
+        if self._pending_reads:
+            self._pending_reads.pop(0)
 
     def output_device_ptr(self, which: int = L.XR_OUT_LDR8) -> int:
         p = C.c_void_p()

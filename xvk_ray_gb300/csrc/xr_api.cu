@@ -65,7 +65,7 @@ void free_pixels(Context* c) {
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);   // reads still in flight from the images
     c->ldr[0] = c->ldr[1] = nullptr;
     c->ldr_copy_pending[0] = c->ldr_copy_pending[1] = false;
-    c->ldr_last_copy = -1;
+    c->ldr_nreads = 0;
     if (c->pix_mem) cudaFree(c->pix_mem);
     c->pix_mem = nullptr;
     c->pix_bytes = 0;
@@ -971,6 +971,8 @@ xr_status xr_read_output_async(XrContext* c, void* host, size_t bytes) {
     const size_t need = (size_t)c->N * 4;
     if (bytes < need) return fail(c, XR_ERR_INVALID_ARGUMENT, "read_output_async: host buffer too small");
     if (!c->frames) return fail(c, XR_ERR_STATE, "read_output_async: no frame rendered yet");
+    if (c->ldr_nreads == 2u)
+        return fail(c, XR_ERR_STATE, "read_output_async: two reads in flight already (call xr_wait_output)");
     DeviceGuard g(c->device);
     const uint32_t p = c->fa.parity;   // the buffer the last frame wrote
     xr_status s = cuda_check(c, cudaEventRecord(c->ldr_ready[p], c->stream), "read_output_async event");
@@ -980,15 +982,18 @@ xr_status xr_read_output_async(XrContext* c, void* host, size_t bytes) {
     if (!s) s = cuda_check(c, cudaEventRecord(c->ldr_copied[p], c->copy_stream), "read_output_async event");
     if (s) return s;
     c->ldr_copy_pending[p] = true;
-    c->ldr_last_copy = (int)p;
+    c->ldr_reads[c->ldr_nreads++] = p;
     return XR_OK;
 }
 
 xr_status xr_wait_output(XrContext* c) {
     if (!c) return fail(nullptr, XR_ERR_INVALID_ARGUMENT, "wait_output: null context");
-    if (c->ldr_last_copy < 0) return XR_OK;
+    if (c->ldr_nreads == 0u) return XR_OK;
     DeviceGuard g(c->device);
-    return cuda_check(c, cudaEventSynchronize(c->ldr_copied[c->ldr_last_copy]), "wait_output");
+    const xr_status s = cuda_check(c, cudaEventSynchronize(c->ldr_copied[c->ldr_reads[0]]), "wait_output");
+    c->ldr_reads[0] = c->ldr_reads[1];
+    c->ldr_nreads--;
+    return s;
 }
 
 xr_status xr_output_device_ptr(XrContext* c, uint32_t which, void** dptr) {

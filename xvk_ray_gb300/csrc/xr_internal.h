@@ -344,7 +344,8 @@ struct Context {
     cudaEvent_t ldr_ready[2] = {};   // recorded on the frame stream: the buffer's frame is complete
     cudaEvent_t ldr_copied[2] = {};  // recorded on copy_stream: the buffer has been read
     bool ldr_copy_pending[2] = {false, false};   // a frame that writes the buffer waits for the read first
-    int ldr_last_copy = -1;          // the buffer of the last asynchronous read (-1: none)
+    uint32_t ldr_reads[2] = {0u, 0u};    // buffers of the reads xr_wait_output has not waited for, oldest first
+    uint32_t ldr_nreads = 0;
     XrStats stats{};
     CacheState cache;
 
