@@ -354,7 +354,12 @@ __device__ __forceinline__ bool shade_step(const FrameArgs& fa, const XrUniformB
     if (!COMPAT && fa.cache_on && bounce >= 1u && bounce + 1u < nb &&
         (bounce >= 2u || cache_training_pixel(fa, p)))
         ce.nee = next_event(fa.sc, mat, pl.pos, pl.normal, pl.geo, wo, s.thr, s.rng);
-    float3 f = sample_bsdf<COMPAT>(pl.normal, mat, wo, &wi, &pdf, &cos_theta, s.rng);
+    // Corrected mode without the cache: at the last bounce (past bounce 1) the path
+    // ends and nothing below reads the sampled direction, its pdf or the throughput,
+    // so the BSDF is not sampled (the path's random state is not used again).
+    const bool last = !COMPAT && !fa.cache_on && bounce >= 2u && bounce + 1u >= nb;
+    float3 f = f3(0.0f, 0.0f, 0.0f);
+    if (!last) f = sample_bsdf<COMPAT>(pl.normal, mat, wo, &wi, &pdf, &cos_theta, s.rng);
     float3 factor = div3(f * cos_theta, pdf);
     if (!COMPAT && !(pdf > 0.0f)) factor = f3(0.0f, 0.0f, 0.0f);
     bool alive = COMPAT ? true : (pdf > 0.0f);
@@ -577,7 +582,8 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
         const uint32_t i = base + ty * 8u * VW + tx * 16u * rows + in_tile;
         fa.q_out[0][i] = f4(s.o, __uint_as_float(s.pixel));
         fa.q_out[1][i] = f4(s.d, __uint_as_float(s.rng));
-        fa.q_out[2][i] = f4(s.thr, s.pq);
+        // corrected mode: bounce 0's shading starts from unit throughput itself (k_shade)
+        if (COMPAT) fa.q_out[2][i] = f4(s.thr, s.pq);
     }
     if (blockIdx.x == 0u && threadIdx.x == 0u) fa.counters[0] = nb ? fa.N : 0u;   // the paths of bounce 0
 }
@@ -635,7 +641,9 @@ __global__ void __launch_bounds__(kShadeBlock, XR_SHADE_MIN_BLOCKS * 128 / kShad
         ce.train = false;
         ce.nee.valid = false;
         if (i < count) {
-            float4 a = fa.q_in[0][i], b = fa.q_in[1][i], c = fa.q_in[2][i];
+            float4 a = fa.q_in[0][i], b = fa.q_in[1][i];
+            // corrected mode: a camera path's throughput is 1 and its p_q 0 (raygen's values), not read back
+            const float4 c = (COMPAT || bounce > 0u) ? fa.q_in[2][i] : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
             uint4 hr = fa.hits[i];
             s.o = xyz(a); s.pixel = __float_as_uint(a.w);
             s.d = xyz(b); s.rng = __float_as_uint(b.w);
