@@ -253,10 +253,10 @@ void cache_after_bounce1(void* ctx) {
     c->infer_pending = true;
 }
 
-// After the bounce loop: the training (gradients, then Adam once the inference,
-// which reads the table and weights Adam overwrites, is done) runs on the side
-// stream beside the reservoir passes and joins before the frame ends
-// (enqueue_frame); the frame stream waits for the inference before the temporal pass.
+// After the bounce loop: the training's second stage (gradients, then Adam once
+// the inference, which reads the table and weights Adam overwrites, is done) on
+// the side stream, which the frame stream joins before the temporal pass
+// (enqueue_frame); the frame stream also waits for the inference.
 void cache_after_paths(Context* c) {
     CacheState& cs = c->cache;
     if (!c->fa.cache_on) return;

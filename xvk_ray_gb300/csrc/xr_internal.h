@@ -329,9 +329,9 @@ struct Context {
     cudaEvent_t ev[8] = {};          // 0..3 frame passes, 4 end of cache training, 5 UBO staging, 6/7 cache inference
     // The cache's inference runs on infer_stream beside the training paths' bounces 2..
     // (forked at infer_fork_ev once bounce 1's queries exist, joined by the temporal pass
-    // at infer_ev); its training runs on side_stream beside the reservoir passes (forked
-    // after the paths at fork_ev, Adam after infer_ev, joined before the frame's end at
-    // join_ev).  ev_train0 times the training's start.
+    // at infer_ev); its training on side_stream (first stage forked with the inference,
+    // second stage after the paths at fork_ev, Adam after infer_ev, joined before the
+    // temporal pass at join_ev).  ev_train0 times the training's start.
     cudaStream_t side_stream = nullptr, infer_stream = nullptr;
     cudaEvent_t fork_ev = nullptr, infer_fork_ev = nullptr, infer_ev = nullptr, join_ev = nullptr;
     cudaEvent_t ev_train0 = nullptr;
