@@ -163,7 +163,9 @@ xr_status xr_get_params(XrContext* ctx, XrParams* params);
 /* ---- replaces ApplicationReSTIRGI::Render (ApplicationReSTIRGI.cpp:150-275):
         initial sample -> temporal reuse -> spatial reuse + shading, stream ordered.
         The UBO is the one PathTracer::GetUniformBufferObject builds
-        (src/pathTracer.cpp:169-201). ---- */
+        (src/pathTracer.cpp:169-201).  Enqueues the frame and returns; the UBO is
+        staged in one of two page-locked slots (by frame parity), so a call waits
+        only until the frame two before it has started on the device. ---- */
 xr_status xr_render_frame(XrContext* ctx, const XrUniformBufferObject* ubo);
 
 /* Converged reference: the plain path tracer with the initial-sample pass's path

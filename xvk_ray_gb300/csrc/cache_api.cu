@@ -255,8 +255,8 @@ void cache_after_bounce1(void* ctx) {
 
 // After the bounce loop: the training's second stage (gradients, then Adam once
 // the inference, which reads the table and weights Adam overwrites, is done) on
-// the side stream, which the frame stream joins before the temporal pass
-// (enqueue_frame); the frame stream also waits for the inference.
+// the side stream, which the frame stream joins after the temporal pass
+// (enqueue_frame); the frame stream waits for the inference before that pass.
 void cache_after_paths(Context* c) {
     CacheState& cs = c->cache;
     if (!c->fa.cache_on) return;

@@ -167,7 +167,7 @@ xr_status alloc_pixels(Context* c) {
         c->h_ubo = nullptr;
         c->ubo_cap = 0;
         if ((s = cuda_check(c, cudaMalloc((void**)&c->d_ubo, views.size() * sizeof(XrUniformBufferObject)), "ubo")) ||
-            (s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, views.size() * sizeof(XrUniformBufferObject)), "ubo staging")))
+            (s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, 2 * views.size() * sizeof(XrUniformBufferObject)), "ubo staging")))
             return s;
         c->ubo_cap = (uint32_t)views.size();
     }
@@ -204,12 +204,16 @@ void set_frame_pointers(Context* c, uint32_t parity) {
     apply_tuning(c);
 }
 
-// Host side of a frame's UBO upload: wait until the previous frame's transfer has
-// read the pinned staging copy, then overwrite it with the n views' UBOs.
+// Host side of a frame's UBO upload: wait until the last transfer from the frame
+// parity's pinned staging slot has read it (the frame two before), then overwrite the
+// slot with the n views' UBOs.
 xr_status stage_ubos(Context* c, const XrUniformBufferObject* ubos, uint32_t n) {
-    xr_status s = cuda_check(c, cudaEventSynchronize(c->ev[5]), "ubo staging");
+    const uint32_t slot = ubos[0].current_frame & 1u;
+    xr_status s = cuda_check(c, cudaEventSynchronize(c->ubo_ev[slot]), "ubo staging");
     if (s) return s;
-    for (uint32_t i = 0; i < n; i++) c->h_ubo[i] = ubos[i];
+    XrUniformBufferObject* h = c->h_ubo + (size_t)slot * c->ubo_cap;
+    for (uint32_t i = 0; i < n; i++) h[i] = ubos[i];
+    c->ubo_slot = slot;
     return XR_OK;
 }
 // Records `e` on the context's stream; inside a stream capture it becomes an
@@ -229,12 +233,15 @@ cudaError_t record_event(Context* c, cudaEvent_t e) { return record_event_on(c->
 
 namespace {
 
-// Stream side: the transfer itself (also what a captured frame graph replays).
+// Stream side: the transfer from the slot staged last (also what a captured frame
+// graph replays; the graph of a frame parity reads that parity's slot).
 xr_status enqueue_ubos(Context* c, uint32_t n) {
-    xr_status s = cuda_check(c, cudaMemcpyAsync(c->d_ubo, c->h_ubo, n * sizeof(XrUniformBufferObject),
-                                                cudaMemcpyHostToDevice, c->stream), "ubo upload");
+    const uint32_t slot = c->ubo_slot;
+    xr_status s = cuda_check(c, cudaMemcpyAsync(c->d_ubo, c->h_ubo + (size_t)slot * c->ubo_cap,
+                                                n * sizeof(XrUniformBufferObject), cudaMemcpyHostToDevice, c->stream),
+                             "ubo upload");
     if (s) return s;
-    return cuda_check(c, record_event(c, c->ev[5]), "ubo event");
+    return cuda_check(c, record_event(c, c->ubo_ev[slot]), "ubo event");
 }
 
 }  // namespace
@@ -357,14 +364,15 @@ xr_status xr_create(const XrDeviceDesc* desc, XrContext** out) {
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_work, 2 * sizeof(unsigned long long)), "work counters"))) goto bad;
     if ((s = cuda_check(c, cudaMemset(c->d_work, 0, 2 * sizeof(unsigned long long)), "work counters"))) goto bad;
     if ((s = cuda_check(c, cudaMalloc((void**)&c->d_ubo, sizeof(XrUniformBufferObject)), "ubo"))) goto bad;
-    if ((s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, sizeof(XrUniformBufferObject)), "ubo staging"))) goto bad;
+    if ((s = cuda_check(c, cudaMallocHost((void**)&c->h_ubo, 2 * sizeof(XrUniformBufferObject)), "ubo staging"))) goto bad;
     for (int i = 0; i < 8; i++)
         if ((s = cuda_check(c, cudaEventCreate(&c->ev[i]), "event"))) goto bad;
     for (int i = 0; i < 8; i++)
         if ((s = cuda_check(c, cudaEventCreate(&c->user_ev[i]), "event"))) goto bad;
     for (int i = 0; i < 2; i++)
         if ((s = cuda_check(c, cudaEventCreate(&c->refit_ev[i]), "event"))) goto bad;
-    cudaEventRecord(c->ev[5], c->stream);
+    for (int i = 0; i < 2; i++)
+        if ((s = cuda_check(c, cudaEventCreateWithFlags(&c->ubo_ev[i], cudaEventDisableTiming), "event"))) goto bad;
     {
         XrParams p;
         xr_params_default(&p, desc->width ? desc->width : 1, desc->height ? desc->height : 1);
@@ -396,6 +404,7 @@ void xr_destroy(XrContext* c) {
     for (int i = 0; i < 8; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 8; i++) if (c->user_ev[i]) cudaEventDestroy(c->user_ev[i]);
     for (int i = 0; i < 2; i++) if (c->refit_ev[i]) cudaEventDestroy(c->refit_ev[i]);
+    for (int i = 0; i < 2; i++) if (c->ubo_ev[i]) cudaEventDestroy(c->ubo_ev[i]);
     for (int i = 0; i < 2; i++) {
         if (c->ldr_ready[i]) cudaEventDestroy(c->ldr_ready[i]);
         if (c->ldr_copied[i]) cudaEventDestroy(c->ldr_copied[i]);
@@ -653,17 +662,18 @@ static xr_status enqueue_frame(Context* c, uint32_t n_ubo, uint32_t nb, bool reu
     record_event(c, c->ev[0]);
     launch_initial(c->fa, nb, c->stream, c->fa.cache_on ? cache_after_bounce1 : nullptr, c);
     cache_after_paths(c);   // radiance-cache training; the temporal pass waits for the inference (when enabled)
-    // The cache's training joins the frame stream here: beside the reservoir passes it
-    // costs them more than it saves (4 x 4K: 49.9 ms joined here, 51.5 ms joined before
-    // the shadow rays), while its first stage still runs beside the bounce loop.
+    record_event(c, c->ev[1]);
+    bool temporal_writes_image = compat ? !reuse0 : (c->params.spatial_on == 0u);
+    launch_temporal(c->fa, temporal_writes_image, c->stream);
+    // The cache's training joins the frame stream here: it runs beside the temporal pass
+    // (HBM-bound, while the training waits on latency) but not beside the spatial pass,
+    // whose shadow-ray traversal it slows by more than it saves (4 x 4K: 51.5 ms joined
+    // before the shadow rays, 49.9 ms joined here).
     if (c->side_pending) {
         cudaEventRecord(c->join_ev, c->side_stream);
         cudaStreamWaitEvent(c->stream, c->join_ev, 0);
         c->side_pending = false;
     }
-    record_event(c, c->ev[1]);
-    bool temporal_writes_image = compat ? !reuse0 : (c->params.spatial_on == 0u);
-    launch_temporal(c->fa, temporal_writes_image, c->stream);
     record_event(c, c->ev[2]);
     if (compat || c->params.spatial_on) launch_spatial(c->fa, c->stream);
     record_event(c, c->ev[3]);

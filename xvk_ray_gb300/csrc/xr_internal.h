@@ -318,7 +318,12 @@ struct Context {
     float4* q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     uint32_t* d_counters = nullptr;
     XrUniformBufferObject* d_ubo = nullptr;
-    XrUniformBufferObject* h_ubo = nullptr;   // pinned staging
+    // Pinned staging of the UBOs, one slot per frame parity (2 x ubo_cap): the host fills
+    // frame k's slot once frame k-2's upload has read it (ubo_ev), so it can enqueue a
+    // frame while the two before it are still in flight.
+    XrUniformBufferObject* h_ubo = nullptr;
+    cudaEvent_t ubo_ev[2] = {};
+    uint32_t ubo_slot = 0;                    // slot of the UBOs staged last
 
     // statistics
     uint32_t frames = 0;
@@ -326,11 +331,11 @@ struct Context {
     unsigned long long* d_work = nullptr;   // node visits, triangle tests of the last ray query
     uint64_t query_rays = 0;
     uint32_t error_flags = 0;
-    cudaEvent_t ev[8] = {};          // 0..3 frame passes, 4 end of cache training, 5 UBO staging, 6/7 cache inference
+    cudaEvent_t ev[8] = {};          // 0..3 frame passes, 4 end of cache training, 5 unused, 6/7 cache inference
     // The cache's inference runs on infer_stream beside the training paths' bounces 2..
     // (forked at infer_fork_ev once bounce 1's queries exist, joined by the temporal pass
     // at infer_ev); its training on side_stream (first stage forked with the inference,
-    // second stage after the paths at fork_ev, Adam after infer_ev, joined before the
+    // second stage after the paths at fork_ev, Adam after infer_ev, joined after the
     // temporal pass at join_ev).  ev_train0 times the training's start.
     cudaStream_t side_stream = nullptr, infer_stream = nullptr;
     cudaEvent_t fork_ev = nullptr, infer_fork_ev = nullptr, infer_ev = nullptr, join_ev = nullptr;
@@ -353,7 +358,7 @@ struct Context {
     std::vector<XrView> views;
     std::vector<ViewInfo> view_info;      // host copy of the device view table
     ViewInfo* d_views = nullptr;
-    uint32_t ubo_cap = 1;                 // UBOs d_ubo / h_ubo hold
+    uint32_t ubo_cap = 1;                 // UBOs d_ubo (and each slot of h_ubo) hold
     std::vector<uint32_t> scene_roots;    // first node of each scene (kNoRoot: empty scene)
     // CUDA graphs of one frame per parity of the frame index (xr_render_views)
     bool graphs_on = false;
