@@ -8,7 +8,9 @@ and its images must be identical:
   writes the buffer being read: that frame waits for the read on the device;
 * two frames in flight (the host loop bench.py's e2e leg runs): reads are waited
   for oldest first, a third read in flight is refused;
-* the same through replayed frame graphs.
+* the same through replayed frame graphs;
+* frames of one parity back to back: they share the UBO staging slot and the
+  RGBA8 buffer, so each waits for the previous frame's upload and image read.
 Misuse is refused before anything is enqueued.
 """
 import numpy as np
@@ -98,6 +100,35 @@ def test_two_frames_in_flight():
                 if f == 4:                                # a third read in flight is refused
                     with pytest.raises(xr.XrError, match="two reads"):
                         r.read_output_async(pinned[(f + 1) % 3].array)
+            for f in (len(ubos) - 2, len(ubos) - 1):
+                r.wait_output()
+                got[f] = pinned[f % 3].array.copy()
+            for f in range(len(ubos)):
+                assert np.array_equal(got[f].view(np.uint32), ref[f].reshape(-1).view(np.uint32)), f"frame {f}"
+    finally:
+        for p in pinned:
+            p.free()
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_frames_of_one_parity_back_to_back(graphs):
+    scene = _scene()
+    ubos = []
+    for f, u in enumerate(camera_sequence(scene, W, H, 7, 4)):
+        v = L.XrUniformBufferObject.from_buffer_copy(u)
+        v.current_frame = 2 * f                           # every frame even
+        ubos.append(v)
+    ref = _sync_images(scene, ubos)
+    pinned = [xr.PinnedBuffer(W * H * 4) for _ in range(3)]
+    try:
+        with _renderer(scene, graphs) as r:
+            got = {}
+            for f, u in enumerate(ubos):
+                r.render(u)
+                if f >= 2:
+                    r.wait_output()
+                    got[f - 2] = pinned[(f - 2) % 3].array.copy()
+                r.read_output_async(pinned[f % 3].array)
             for f in (len(ubos) - 2, len(ubos) - 1):
                 r.wait_output()
                 got[f] = pinned[f % 3].array.copy()
