@@ -38,6 +38,11 @@ struct RayIn {
     float3 o, d;
     float tmin, tmax;
     uint32_t root;   // first node of the ray's scene (0 unless several scenes share the node array)
+    // Closest-hit rays only: tmax_full > tmax makes tmax a guess at where the ray hits.
+    // Boxes beyond it are culled from the start; a ray that ends without a hit inside
+    // it is traced again up to tmax_full.  The result is the same either way: when a
+    // hit lies within tmax, the closest hit (and every hit tied with it) does too.
+    float tmax_full = 0.0f;
 };
 
 // Byte k of `word` placed in mantissa bits 8..15 of 1.0f by one byte permute:
@@ -116,6 +121,55 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
         idz = 1.0f / copysignf(fmaxf(fabsf(d.z), kMinDir), d.z);
         flip = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) | ((__float_as_uint(d.z) >> 31) << 2);
     };
+    // closest-hit rays without instances: the ray is traced again up to tmax_full
+    // when it ends without a hit inside its first tmax
+    bool retry = false;
+    // the lane's state at the start of ray r, searched up to t_end
+    auto begin_ray = [&](const RayIn& r, float t_end) {
+        o = r.o;
+        tmin = r.tmin;
+        tmin_box = r.tmin * (1.0f - 1e-6f) - 1e-30f;
+        // Box-test reciprocals of the direction with each component kept at
+        // least kMinDir in magnitude (sign kept): an exactly zero component
+        // would give an infinite reciprocal, and inf - inf in the per-node
+        // plane constants below is NaN, which drops that axis from every slab
+        // test and walks the whole tree.  The box test then follows a ray that
+        // departs from the true one by at most kMinDir * t, far inside the
+        // slack of the stored boxes, so no box holding a hit is culled;
+        // the triangle test uses the true direction.
+        // The sign bits select the near planes (so that -0 picks the same
+        // planes as its infinite reciprocal).
+        set_dir(r.d);
+        rt = prep_ray(r.o, r.d);
+        if (INST) { wo = r.o; wd = r.d; widx = idx; widy = idy; widz = idz; wflip = flip; }
+        h.prim = -1; h.t = t_end; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = -1;
+        sp = 0;
+        tg_mask = 0;
+        if (INST) {
+            // every instance may be entered once: bound the visits accordingly
+            const unsigned long long lim = ((unsigned long long)sc.n_nodes + sc.n_tlas_nodes) *
+                                           (unsigned long long)max(sc.n_inst, 1u);
+            visits_left = lim > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)lim;
+            in_blas = false;
+            cur_inst = -1;
+            ng_base = 0u;   // the top-level root
+            ng_bits = sc.n_tlas_nodes ? (1u | ((1u << flip) << 8)) : 0u;
+        } else {
+            visits_left = sc.n_nodes;
+            // a virtual group whose only child is the root (node 0)
+            ng_base = r.root;
+            ng_bits = (r.root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;   // no root: a miss
+        }
+        // A non-finite origin or direction (or a zero direction) can hit
+        // nothing -- every triangle test fails -- but would make every box
+        // test pass through NaN slabs and walk the whole tree: end it as a miss.
+        const float chk = r.o.x + r.o.y + r.o.z + r.d.x + r.d.y + r.d.z;
+        if (!isfinite(chk) || (r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f)) {
+            ng_bits = 0u;
+            retry = false;
+            n_nonfinite++;
+        }
+    };
 
     while (true) {
         // ---- refill idle lanes ----
@@ -129,51 +183,11 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
             if (!active) {
                 const uint32_t my = base + __popc(idle & lt_mask);
                 if (my < count) {
-                    RayIn r = load(my);
+                    const RayIn r = load(my);
                     ray_id = my;
                     active = true;
-                    o = r.o;
-                    tmin = r.tmin;
-                    tmin_box = r.tmin * (1.0f - 1e-6f) - 1e-30f;
-                    // Box-test reciprocals of the direction with each component kept at
-                    // least kMinDir in magnitude (sign kept): an exactly zero component
-                    // would give an infinite reciprocal, and inf - inf in the per-node
-                    // plane constants below is NaN, which drops that axis from every slab
-                    // test and walks the whole tree.  The box test then follows a ray that
-                    // departs from the true one by at most kMinDir * t, far inside the
-                    // slack of the stored boxes, so no box holding a hit is culled;
-                    // the triangle test uses the true direction.
-                    // The sign bits select the near planes (so that -0 picks the same
-                    // planes as its infinite reciprocal).
-                    set_dir(r.d);
-                    rt = prep_ray(r.o, r.d);
-                    if (INST) { wo = r.o; wd = r.d; widx = idx; widy = idy; widz = idz; wflip = flip; }
-                    h.prim = -1; h.t = r.tmax; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = -1;
-                    sp = 0;
-                    tg_mask = 0;
-                    if (INST) {
-                        // every instance may be entered once: bound the visits accordingly
-                        const unsigned long long lim = ((unsigned long long)sc.n_nodes + sc.n_tlas_nodes) *
-                                                       (unsigned long long)max(sc.n_inst, 1u);
-                        visits_left = lim > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)lim;
-                        in_blas = false;
-                        cur_inst = -1;
-                        ng_base = 0u;   // the top-level root
-                        ng_bits = sc.n_tlas_nodes ? (1u | ((1u << flip) << 8)) : 0u;
-                    } else {
-                        visits_left = sc.n_nodes;
-                        // a virtual group whose only child is the root (node 0)
-                        ng_base = r.root;
-                        ng_bits = (r.root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;   // no root: a miss
-                    }
-                    // A non-finite origin or direction (or a zero direction) can hit
-                    // nothing -- every triangle test fails -- but would make every box
-                    // test pass through NaN slabs and walk the whole tree: end it as a miss.
-                    const float chk = r.o.x + r.o.y + r.o.z + r.d.x + r.d.y + r.d.z;
-                    if (!isfinite(chk) || (r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f)) {
-                        ng_bits = 0u;
-                        n_nonfinite++;
-                    }
+                    retry = !ANY && !INST && r.tmax_full > r.tmax;
+                    begin_ray(r, r.tmax);
                 }
             }
         }
@@ -319,8 +333,15 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 cur_inst = -1;
             }
             if (sp == 0) {
-                store(ray_id, h);
-                active = false;
+                if (!ANY && !INST && retry && h.prim < 0) {
+                    // nothing within the first tmax: the same ray up to its full length
+                    retry = false;
+                    const RayIn r = load(ray_id);
+                    begin_ray(r, r.tmax_full);
+                } else {
+                    store(ray_id, h);
+                    active = false;
+                }
             } else {
                 const uint2 e = stack[--sp];
                 if (e.y & kTriGroupBit) { tg_base = e.x; tg_mask = e.y & 0x00FFFFFFu; ng_bits = 0u; }
