@@ -600,16 +600,16 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 // ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
 // With several scenes each ray starts at its view's root; a path whose pixel slot
 // holds a cache training record (pixel_is_record) finds its pixel in the record.
-// camera_bound (corrected mode, bounce 0): each camera ray first searches up to just
-// past its pixel's previous visible point (RayIn::tmax_full), with the same hits.
-template <bool INST>
+// BOUND (corrected mode, bounce 0, one level): each camera ray first searches up to
+// just past its pixel's previous visible point, then (on a miss) up to TMax, with the
+// same hits (trace_persistent's RETRY).
+template <bool INST, bool BOUND>
 __global__ void __launch_bounds__(trace_block<INST>(), 1) k_trace_paths(FrameArgs fa, const float4* __restrict__ q0,
                                                         const float4* __restrict__ q1, uint4* __restrict__ hits,
                                                         const uint32_t* count_ptr, uint32_t* next, uint32_t* err,
-                                                        uint32_t* nonfinite, uint32_t pixel_is_record,
-                                                        uint32_t camera_bound) {
+                                                        uint32_t* nonfinite, uint32_t pixel_is_record) {
     const uint32_t count = *(volatile const uint32_t*)count_ptr;
-    trace_persistent<false, INST>(
+    trace_persistent<false, INST, BOUND>(
         fa.sc, count, next,
         [&](uint32_t i) {
             float4 a = q0[i], b = q1[i];
@@ -621,15 +621,12 @@ __global__ void __launch_bounds__(trace_block<INST>(), 1) k_trace_paths(FrameArg
                 if (pixel_is_record) p = fa.cache_t[(size_t)p * 3u].w;
                 r.root = root_of_pixel(fa, p);
             }
-            if (!INST && XR_CAMERA_BOUND_MARGIN > 0.0f && camera_bound) {
+            if (BOUND) {
                 const uint32_t p = __float_as_uint(a.w);
                 if (fa.gb_mat_prev[p] != kInvalid) {
                     const float3 dx = xyz(fa.gb_pos_prev[p]) - r.o;
                     const float bound = sqrtf(dot(dx, dx)) * XR_CAMERA_BOUND_MARGIN;
-                    if (bound > r.tmin && bound < r.tmax) {   // false for NaN
-                        r.tmax_full = r.tmax;
-                        r.tmax = bound;
-                    }
+                    if (bound > r.tmin && bound < r.tmax) r.tmax = bound;   // false for NaN
                 }
             }
             return r;
@@ -638,7 +635,7 @@ __global__ void __launch_bounds__(trace_block<INST>(), 1) k_trace_paths(FrameArg
             hits[i] = make_uint4((uint32_t)h.prim, __float_as_uint(h.t), __float_as_uint(h.b1), __float_as_uint(h.b2));
             if (INST) fa.hit_inst[i] = h.inst;
         },
-        err, nullptr, nonfinite);
+        err, nullptr, nonfinite, 10000.0f);
 }
 
 // Shading of one bounce over the queue (persistent grid): coherent per-path
@@ -1469,8 +1466,8 @@ uint32_t trace_grid(int sm_count, bool instances) {
     int& o = occ[instances ? 1 : 0];
     if (o == 0) {
         int v = 0;
-        if (instances) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<true>, kTraceBlockInst, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<false>, kTraceBlock, 0);
+        if (instances) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<true, false>, kTraceBlockInst, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_paths<false, false>, kTraceBlock, 0);
         o = v > 0 ? v : 4;
     }
     return (uint32_t)(o * sm_count);
@@ -1485,15 +1482,19 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st, void (*af
     for (uint32_t b = 0; b < nb; b++) {
         // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
+        const uint32_t rec = (cache && b >= 2u) ? 1u : 0u;
         if (fa.sc.n_inst)
-            k_trace_paths<true><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
-                                                              fa.counters + kCntFetchPath + b, fa.counters + kCntError,
-                                                              fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u, 0u);
+            k_trace_paths<true, false><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+                                                                     fa.counters + kCntFetchPath + b, fa.counters + kCntError,
+                                                                     fa.counters + kCntNonFinite, rec);
+        else if (XR_CAMERA_BOUND_MARGIN > 0.0f && !fa.compat && b == 0u)
+            k_trace_paths<false, true><<<fa.grid_trace, kTraceBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+                                                                     fa.counters + kCntFetchPath + b, fa.counters + kCntError,
+                                                                     fa.counters + kCntNonFinite, rec);
         else
-            k_trace_paths<false><<<fa.grid_trace, kTraceBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
-                                                               fa.counters + kCntFetchPath + b, fa.counters + kCntError,
-                                                               fa.counters + kCntNonFinite, (cache && b >= 2u) ? 1u : 0u,
-                                                               (!fa.compat && b == 0u) ? 1u : 0u);
+            k_trace_paths<false, false><<<fa.grid_trace, kTraceBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+                                                                      fa.counters + kCntFetchPath + b, fa.counters + kCntError,
+                                                                      fa.counters + kCntNonFinite, rec);
         const bool nee = cache && b >= 1u && b + 1u < nb;
         if (nee) cudaMemsetAsync(fa.counters + kCntCacheNee, 0, 2 * sizeof(uint32_t), st);   // count + fetch
         if (fa.compat) k_shade<true><<<fa.grid_persistent, kShadeBlock, 0, st>>>(a, fa.ubo, b, nb);

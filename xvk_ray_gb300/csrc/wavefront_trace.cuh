@@ -38,11 +38,6 @@ struct RayIn {
     float3 o, d;
     float tmin, tmax;
     uint32_t root;   // first node of the ray's scene (0 unless several scenes share the node array)
-    // Closest-hit rays only: tmax_full > tmax makes tmax a guess at where the ray hits.
-    // Boxes beyond it are culled from the start; a ray that ends without a hit inside
-    // it is traced again up to tmax_full.  The result is the same either way: when a
-    // hit lies within tmax, the closest hit (and every hit tied with it) does too.
-    float tmax_full = 0.0f;
 };
 
 // Byte k of `word` placed in mantissa bits 8..15 of 1.0f by one byte permute:
@@ -81,10 +76,18 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // world-to-object rows; t is unchanged) and continues at the root of its
 // bottom-level BVH in sc.nodes.  Popping the marker restores the world-space ray
 // (kept in the lane's registers or local memory since the ray's start).  Hits compare t, then instance, then primitive.
-template <bool ANY, bool INST = false, typename LoadRay, typename StoreHit>
+//
+// RETRY (closest hit, one level): a ray whose tmax is below retry_tmax treats its tmax
+// as a guess at where it hits.  Boxes beyond it are culled from the start; a ray that
+// ends without a hit inside it is traced again up to retry_tmax.  The result is the
+// same either way: when a hit lies within tmax, the closest hit (and every hit tied
+// with it) does too.
+template <bool ANY, bool INST = false, bool RETRY = false, typename LoadRay, typename StoreHit>
 __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t count, uint32_t* next,
                                                  LoadRay load, StoreHit store, uint32_t* err,
-                                                 unsigned long long* work = nullptr, uint32_t* nonfinite = nullptr) {
+                                                 unsigned long long* work = nullptr, uint32_t* nonfinite = nullptr,
+                                                 float retry_tmax = 0.0f) {
+    static_assert(!RETRY || (!ANY && !INST), "the retry is for one-level closest-hit traversal");
     const uint32_t FULL = 0xFFFFFFFFu;
     uint32_t n_visits = 0, n_tests = 0, n_nonfinite = 0;
     // queue tuning of the context (0: the defaults kRefillMin / kPostponeBelow)
@@ -93,6 +96,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
     bool active = false, drained = false;
+    bool retry = false;   // RETRY: the lane's ray is traced again up to retry_tmax on a miss
     uint32_t ray_id = 0;
     float3 o = f3(0, 0, 0);
     float idx = 0, idy = 0, idz = 0, tmin = 0, tmin_box = 0;
@@ -121,55 +125,6 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
         idz = 1.0f / copysignf(fmaxf(fabsf(d.z), kMinDir), d.z);
         flip = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) | ((__float_as_uint(d.z) >> 31) << 2);
     };
-    // closest-hit rays without instances: the ray is traced again up to tmax_full
-    // when it ends without a hit inside its first tmax
-    bool retry = false;
-    // the lane's state at the start of ray r, searched up to t_end
-    auto begin_ray = [&](const RayIn& r, float t_end) {
-        o = r.o;
-        tmin = r.tmin;
-        tmin_box = r.tmin * (1.0f - 1e-6f) - 1e-30f;
-        // Box-test reciprocals of the direction with each component kept at
-        // least kMinDir in magnitude (sign kept): an exactly zero component
-        // would give an infinite reciprocal, and inf - inf in the per-node
-        // plane constants below is NaN, which drops that axis from every slab
-        // test and walks the whole tree.  The box test then follows a ray that
-        // departs from the true one by at most kMinDir * t, far inside the
-        // slack of the stored boxes, so no box holding a hit is culled;
-        // the triangle test uses the true direction.
-        // The sign bits select the near planes (so that -0 picks the same
-        // planes as its infinite reciprocal).
-        set_dir(r.d);
-        rt = prep_ray(r.o, r.d);
-        if (INST) { wo = r.o; wd = r.d; widx = idx; widy = idy; widz = idz; wflip = flip; }
-        h.prim = -1; h.t = t_end; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = -1;
-        sp = 0;
-        tg_mask = 0;
-        if (INST) {
-            // every instance may be entered once: bound the visits accordingly
-            const unsigned long long lim = ((unsigned long long)sc.n_nodes + sc.n_tlas_nodes) *
-                                           (unsigned long long)max(sc.n_inst, 1u);
-            visits_left = lim > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)lim;
-            in_blas = false;
-            cur_inst = -1;
-            ng_base = 0u;   // the top-level root
-            ng_bits = sc.n_tlas_nodes ? (1u | ((1u << flip) << 8)) : 0u;
-        } else {
-            visits_left = sc.n_nodes;
-            // a virtual group whose only child is the root (node 0)
-            ng_base = r.root;
-            ng_bits = (r.root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;   // no root: a miss
-        }
-        // A non-finite origin or direction (or a zero direction) can hit
-        // nothing -- every triangle test fails -- but would make every box
-        // test pass through NaN slabs and walk the whole tree: end it as a miss.
-        const float chk = r.o.x + r.o.y + r.o.z + r.d.x + r.d.y + r.d.z;
-        if (!isfinite(chk) || (r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f)) {
-            ng_bits = 0u;
-            retry = false;
-            n_nonfinite++;
-        }
-    };
 
     while (true) {
         // ---- refill idle lanes ----
@@ -183,11 +138,53 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
             if (!active) {
                 const uint32_t my = base + __popc(idle & lt_mask);
                 if (my < count) {
-                    const RayIn r = load(my);
+                    RayIn r = load(my);
                     ray_id = my;
                     active = true;
-                    retry = !ANY && !INST && r.tmax_full > r.tmax;
-                    begin_ray(r, r.tmax);
+                    o = r.o;
+                    tmin = r.tmin;
+                    tmin_box = r.tmin * (1.0f - 1e-6f) - 1e-30f;
+                    // Box-test reciprocals of the direction with each component kept at
+                    // least kMinDir in magnitude (sign kept): an exactly zero component
+                    // would give an infinite reciprocal, and inf - inf in the per-node
+                    // plane constants below is NaN, which drops that axis from every slab
+                    // test and walks the whole tree.  The box test then follows a ray that
+                    // departs from the true one by at most kMinDir * t, far inside the
+                    // slack of the stored boxes, so no box holding a hit is culled;
+                    // the triangle test uses the true direction.
+                    // The sign bits select the near planes (so that -0 picks the same
+                    // planes as its infinite reciprocal).
+                    set_dir(r.d);
+                    rt = prep_ray(r.o, r.d);
+                    if (INST) { wo = r.o; wd = r.d; widx = idx; widy = idy; widz = idz; wflip = flip; }
+                    if constexpr (RETRY) retry = r.tmax < retry_tmax;
+                    h.prim = -1; h.t = r.tmax; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = -1;
+                    sp = 0;
+                    tg_mask = 0;
+                    if (INST) {
+                        // every instance may be entered once: bound the visits accordingly
+                        const unsigned long long lim = ((unsigned long long)sc.n_nodes + sc.n_tlas_nodes) *
+                                                       (unsigned long long)max(sc.n_inst, 1u);
+                        visits_left = lim > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)lim;
+                        in_blas = false;
+                        cur_inst = -1;
+                        ng_base = 0u;   // the top-level root
+                        ng_bits = sc.n_tlas_nodes ? (1u | ((1u << flip) << 8)) : 0u;
+                    } else {
+                        visits_left = sc.n_nodes;
+                        // a virtual group whose only child is the root (node 0)
+                        ng_base = r.root;
+                        ng_bits = (r.root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;   // no root: a miss
+                    }
+                    // A non-finite origin or direction (or a zero direction) can hit
+                    // nothing -- every triangle test fails -- but would make every box
+                    // test pass through NaN slabs and walk the whole tree: end it as a miss.
+                    const float chk = r.o.x + r.o.y + r.o.z + r.d.x + r.d.y + r.d.z;
+                    if (!isfinite(chk) || (r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f)) {
+                        ng_bits = 0u;
+                        n_nonfinite++;
+                        if constexpr (RETRY) retry = false;
+                    }
                 }
             }
         }
@@ -332,16 +329,20 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                 in_blas = false;
                 cur_inst = -1;
             }
-            if (sp == 0) {
-                if (!ANY && !INST && retry && h.prim < 0) {
-                    // nothing within the first tmax: the same ray up to its full length
-                    retry = false;
-                    const RayIn r = load(ray_id);
-                    begin_ray(r, r.tmax_full);
-                } else {
-                    store(ray_id, h);
-                    active = false;
-                }
+            bool again = false;
+            if constexpr (RETRY) again = sp == 0 && retry && h.prim < 0;
+            if (again) {
+                // nothing within the first tmax: the same ray again from the root, up to
+                // retry_tmax (direction state and triangle-test set-up are kept)
+                retry = false;
+                h.t = retry_tmax;
+                visits_left = sc.n_nodes;
+                const uint32_t root = load(ray_id).root;
+                ng_base = root;
+                ng_bits = (root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;
+            } else if (sp == 0) {
+                store(ray_id, h);
+                active = false;
             } else {
                 const uint2 e = stack[--sp];
                 if (e.y & kTriGroupBit) { tg_base = e.x; tg_mask = e.y & 0x00FFFFFFu; ng_bits = 0u; }
