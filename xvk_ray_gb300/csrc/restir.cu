@@ -595,6 +595,9 @@ __global__ void __launch_bounds__(kBlock) k_raygen(FrameArgs fa, const XrUniform
 #ifndef XR_CAMERA_BOUND_MARGIN
 #define XR_CAMERA_BOUND_MARGIN 1.02f
 #endif
+// In a BVH of fewer nodes the bound has little to cull and its G-buffer reads cost more
+// than it saves (Cornell box, 4 nodes: 0.192 -> 0.196-0.203 ms per 256 x 256 frame).
+constexpr uint32_t kCameraBoundMinNodes = 256;
 
 // Closest hits of the paths of one bounce (TMin 1e-4, TMax 1e4,
 // ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
@@ -1487,7 +1490,7 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st, void (*af
             k_trace_paths<true, false><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                                      fa.counters + kCntFetchPath + b, fa.counters + kCntError,
                                                                      fa.counters + kCntNonFinite, rec);
-        else if (XR_CAMERA_BOUND_MARGIN > 0.0f && !fa.compat && b == 0u)
+        else if (XR_CAMERA_BOUND_MARGIN > 0.0f && !fa.compat && b == 0u && fa.sc.n_nodes >= kCameraBoundMinNodes)
             k_trace_paths<false, true><<<fa.grid_trace, kTraceBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                                      fa.counters + kCntFetchPath + b, fa.counters + kCntError,
                                                                      fa.counters + kCntNonFinite, rec);
