@@ -603,7 +603,7 @@ constexpr uint32_t kCameraBoundMinNodes = 256;
 // ReSTIRGIInitialSample.rgen.hlsl:79-80), one 16-byte hit record per queue slot.
 // With several scenes each ray starts at its view's root; a path whose pixel slot
 // holds a cache training record (pixel_is_record) finds its pixel in the record.
-// BOUND (corrected mode, bounce 0, one level): each camera ray first searches up to
+// BOUND (corrected mode, bounce 0): each camera ray first searches up to
 // just past its pixel's previous visible point, then (on a miss) up to TMax, with the
 // same hits (trace_persistent's RETRY).
 template <bool INST, bool BOUND>
@@ -1486,11 +1486,16 @@ void launch_initial(const FrameArgs& fa, uint32_t nb, cudaStream_t st, void (*af
         // queues alternate: bounce b reads what raygen / bounce b-1 appended
         for (int k = 0; k < 3; k++) std::swap(a.q_in[k], a.q_out[k]);
         const uint32_t rec = (cache && b >= 2u) ? 1u : 0u;
-        if (fa.sc.n_inst)
+        const bool bound = XR_CAMERA_BOUND_MARGIN > 0.0f && !fa.compat && b == 0u && fa.sc.n_nodes >= kCameraBoundMinNodes;
+        if (fa.sc.n_inst && bound)
+            k_trace_paths<true, true><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
+                                                                    fa.counters + kCntFetchPath + b, fa.counters + kCntError,
+                                                                    fa.counters + kCntNonFinite, rec);
+        else if (fa.sc.n_inst)
             k_trace_paths<true, false><<<fa.grid_trace, kTraceBlockInst, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                                      fa.counters + kCntFetchPath + b, fa.counters + kCntError,
                                                                      fa.counters + kCntNonFinite, rec);
-        else if (XR_CAMERA_BOUND_MARGIN > 0.0f && !fa.compat && b == 0u && fa.sc.n_nodes >= kCameraBoundMinNodes)
+        else if (bound)
             k_trace_paths<false, true><<<fa.grid_trace, kTraceBlock, 0, st>>>(a, a.q_in[0], a.q_in[1], fa.hits, fa.counters + b,
                                                                      fa.counters + kCntFetchPath + b, fa.counters + kCntError,
                                                                      fa.counters + kCntNonFinite, rec);

@@ -77,7 +77,7 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // bottom-level BVH in sc.nodes.  Popping the marker restores the world-space ray
 // (kept in the lane's registers or local memory since the ray's start).  Hits compare t, then instance, then primitive.
 //
-// RETRY (closest hit, one level): a ray whose tmax is below retry_tmax treats its tmax
+// RETRY (closest hit): a ray whose tmax is below retry_tmax treats its tmax
 // as a guess at where it hits.  Boxes beyond it are culled from the start; a ray that
 // ends without a hit inside it is traced again up to retry_tmax.  The result is the
 // same either way: when a hit lies within tmax, the closest hit (and every hit tied
@@ -87,7 +87,7 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
                                                  LoadRay load, StoreHit store, uint32_t* err,
                                                  unsigned long long* work = nullptr, uint32_t* nonfinite = nullptr,
                                                  float retry_tmax = 0.0f) {
-    static_assert(!RETRY || (!ANY && !INST), "the retry is for one-level closest-hit traversal");
+    static_assert(!RETRY || !ANY, "the retry is for closest-hit traversal");
     const uint32_t FULL = 0xFFFFFFFFu;
     uint32_t n_visits = 0, n_tests = 0, n_nonfinite = 0;
     // queue tuning of the context (0: the defaults kRefillMin / kPostponeBelow)
@@ -333,13 +333,26 @@ __device__ __forceinline__ void trace_persistent(const DeviceScene& sc, uint32_t
             if constexpr (RETRY) again = sp == 0 && retry && h.prim < 0;
             if (again) {
                 // nothing within the first tmax: the same ray again from the root, up to
-                // retry_tmax (direction state and triangle-test set-up are kept)
+                // retry_tmax.  The lane holds the world-space ray here (an emptied stack
+                // has popped every level marker), so its direction state is kept; the
+                // triangle-test set-up of a one-level ray is kept too, and a two-level
+                // ray sets it up again at each instance it enters.
                 retry = false;
                 h.t = retry_tmax;
-                visits_left = sc.n_nodes;
-                const uint32_t root = load(ray_id).root;
-                ng_base = root;
-                ng_bits = (root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;
+                if (INST) {
+                    const unsigned long long lim = ((unsigned long long)sc.n_nodes + sc.n_tlas_nodes) *
+                                                   (unsigned long long)max(sc.n_inst, 1u);
+                    visits_left = lim > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)lim;
+                    in_blas = false;
+                    cur_inst = -1;
+                    ng_base = 0u;   // the top-level root
+                    ng_bits = sc.n_tlas_nodes ? (1u | ((1u << flip) << 8)) : 0u;
+                } else {
+                    visits_left = sc.n_nodes;
+                    const uint32_t root = load(ray_id).root;
+                    ng_base = root;
+                    ng_bits = (root < sc.n_nodes) ? (1u | ((1u << flip) << 8)) : 0u;
+                }
             } else if (sp == 0) {
                 store(ray_id, h);
                 active = false;
